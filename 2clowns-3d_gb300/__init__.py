@@ -1,0 +1,375 @@
+"""clowns3d -- GB300 pressure-Poisson solve for 2CLOWNS-3D (host-side mirror).
+
+The compute path is ``libclowns_gpu.so`` (hand-written CUDA for sm_103a, C ABI in
+``include/clowns_gpu.h``).  This module binds it with ctypes and mirrors the
+reference's call sequence of the pressure-correction loop
+(src2LOWNS/1sub-momentum.F90:42-60):
+
+    set_nflag -> init_matrix -> cal_err_of_continuity (rows + RHS)
+              -> cal_matrix_element -> PCGPME -> p -= xe, estimate_velocity2
+
+with the same argument meaning and error behaviour.  PyTorch only provides
+device memory and the CUDA stream.  There is no CPU fallback: every entry point
+raises if the library is missing or no GPU is present.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import dataclasses
+import pathlib
+import threading
+from typing import Optional
+
+import numpy as np
+
+from . import workload  # noqa: F401  (re-exported)
+
+PKG = pathlib.Path(__file__).resolve().parent
+LIB_PATH = PKG / "libclowns_gpu.so"
+
+IER_MAXITER = 3000
+IER_NONFINITE = 9101
+IER_DEVICE = 9102
+IER_ARG = 9104
+STOP_NAMES = {0: "tolerance", 1: "stagnation", 2: "amu_zero", 3: "c1_zero", 4: "iteration_cap",
+              5: "non_finite"}
+
+_lock = threading.Lock()
+_lib = None
+
+
+class ClownsError(RuntimeError):
+    pass
+
+
+class SolveInfo(C.Structure):
+    _fields_ = [("eps", C.c_double), ("bn", C.c_double), ("iter", C.c_int), ("ier", C.c_int),
+                ("reason", C.c_int), ("outer", C.c_int)]
+
+    def as_dict(self):
+        return {"eps": self.eps, "bn": self.bn, "iter": self.iter, "ier": self.ier,
+                "reason": STOP_NAMES.get(self.reason, str(self.reason)), "outer": self.outer}
+
+
+def build(verbose: bool = False) -> pathlib.Path:
+    from . import buildlib as _b
+    return _b.build(verbose=verbose)
+
+
+_SIGS = {
+    "clowns_last_error": (C.c_char_p, []),
+    "clowns_version": (C.c_int, []),
+    "pcgpme_gpu": (None, [C.c_void_p] * 13),
+    "pcgpme_": (None, [C.c_void_p] * 13),
+    "clowns_pcgpme_workspace_bytes": (C.c_size_t, [C.c_int, C.c_int]),
+    "clowns_pcgpme_dev": (C.c_int, [C.c_void_p, C.c_int, C.c_int, C.c_void_p, C.c_void_p, C.c_int,
+                                    C.c_void_p, C.c_void_p, C.c_double, C.c_double, C.c_int,
+                                    C.c_void_p, C.c_size_t, C.c_void_p, C.c_void_p]),
+    "clowns_pcgpme_setup_dev": (C.c_int, [C.c_void_p, C.c_int, C.c_int, C.c_void_p, C.c_void_p,
+                                          C.c_int, C.c_void_p, C.c_double, C.c_void_p, C.c_void_p,
+                                          C.c_void_p, C.c_void_p, C.c_int, C.c_void_p, C.c_size_t,
+                                          C.c_void_p]),
+    "clowns_apply_pm_a_dev": (C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_int, C.c_int,
+                                        C.c_int, C.c_void_p, C.c_void_p, C.c_void_p, C.c_size_t,
+                                        C.c_void_p]),
+    "clowns_set_nflag_workspace_bytes": (C.c_size_t, [C.c_void_p, C.c_int]),
+    "clowns_set_nflag_dev": (C.c_int, [C.c_void_p, C.c_int, C.c_int, C.c_int] + [C.c_void_p] * 17
+                             + [C.c_size_t, C.c_void_p]),
+    "clowns_init_matrix_dev": (C.c_int, [C.c_void_p, C.c_int, C.c_int] + [C.c_void_p] * 14),
+    "clowns_rows_rhs_workspace_bytes": (C.c_size_t, [C.c_int]),
+    "clowns_rows_rhs_dev": (C.c_int, [C.c_void_p, C.c_int, C.c_int] + [C.c_void_p] * 12
+                            + [C.c_double, C.c_int, C.c_void_p, C.c_int] + [C.c_void_p] * 8
+                            + [C.c_size_t, C.c_void_p]),
+    "clowns_assemble_dev": (C.c_int, [C.c_void_p, C.c_int, C.c_int, C.c_int] + [C.c_void_p] * 8
+                            + [C.c_int] + [C.c_void_p] * 5 + [C.c_int] + [C.c_void_p] * 5),
+    "clowns_correct_dev": (C.c_int, [C.c_void_p, C.c_int, C.c_int] + [C.c_void_p] * 8
+                           + [C.c_double, C.c_int] + [C.c_void_p] * 6),
+}
+
+
+def lib():
+    """The loaded C-ABI library (raises if it was not built)."""
+    global _lib
+    with _lock:
+        if _lib is None:
+            if not LIB_PATH.exists():
+                raise ClownsError(f"{LIB_PATH.name} is not built; run build() first")
+            L = C.CDLL(str(LIB_PATH))
+            for name, (res, args) in _SIGS.items():
+                fn = getattr(L, name, None)
+                if fn is None:
+                    continue
+                fn.restype = res
+                fn.argtypes = args
+            _lib = L
+    return _lib
+
+
+def declared_symbols() -> list[str]:
+    """Function names declared in include/clowns_gpu.h."""
+    import re
+    hdr = (PKG.parent / "include" / "clowns_gpu.h").read_text()
+    hdr = re.sub(r"/\*.*?\*/", "", hdr, flags=re.S)
+    hdr = "\n".join(ln for ln in hdr.splitlines() if not ln.lstrip().startswith("#"))
+    return sorted(set(re.findall(r"\b([A-Za-z_][A-Za-z0-9_]*)\s*\(", hdr)))
+
+
+def last_error() -> str:
+    return lib().clowns_last_error().decode(errors="replace")
+
+
+def _check(rc: int, what: str):
+    if rc != 0:
+        raise ClownsError(f"{what} failed ({rc}): {last_error()}")
+
+
+# ---------------------------------------------------------------------------
+# Host-array drop-in: same arguments as SUBROUTINE PCGPME
+
+def pcgpme(al: np.ndarray, ll: np.ndarray, d: np.ndarray, b: np.ndarray, x: np.ndarray, n: int,
+           eps: float = 1e-10, parm: float = 5.0, itmax: int = 10000):
+    """Solve through ``pcgpme_gpu`` with HOST arrays (the Fortran call shape).
+
+    ``al``/``ll`` are (nl, na) C-order == AL(NA,NL) column-major; ``d``, ``b``
+    hold rows 1..n at [0..n); ``x`` is X(N+N2), updated in place.
+    Returns (eps_out, iter_out, ier)."""
+    L = lib()
+    nl, na = al.shape
+    assert al.dtype == np.float64 and ll.dtype == np.int32 and al.flags.c_contiguous
+    e = np.array([eps, 0.0])
+    c_nl, c_na, c_n, c_n2 = C.c_int(nl), C.c_int(na), C.c_int(n), C.c_int(64)
+    c_parm = C.c_double(parm)
+    c_it = C.c_int(itmax)
+    c_ier = C.c_int(0)
+    L.pcgpme_gpu(al.ctypes.data, C.addressof(c_nl), C.addressof(c_na), ll.ctypes.data, d.ctypes.data,
+                 C.addressof(c_n), C.addressof(c_n2), b.ctypes.data, x.ctypes.data, e.ctypes.data,
+                 C.addressof(c_parm), C.addressof(c_it), C.addressof(c_ier))
+    return float(e[0]), c_it.value, c_ier.value
+
+
+# ---------------------------------------------------------------------------
+# Device-resident pipeline (torch tensors as device memory)
+
+def _torch():
+    import torch
+    if not torch.cuda.is_available():
+        raise ClownsError("no CUDA device: the GPU path has no CPU fallback")
+    return torch
+
+
+def _ptr(t) -> int:
+    return t.data_ptr()
+
+
+def _stream():
+    torch = _torch()
+    return C.c_void_p(torch.cuda.current_stream().cuda_stream)
+
+
+@dataclasses.dataclass
+class DeviceCase:
+    """Module arrays of one case resident in HBM."""
+    case: object
+    dims: object
+    x: object
+    dx: object
+    mn: object
+    in_: object
+    jn: object
+    kn: object
+    nf: object
+    nfb: object
+    f: object
+    fb: object
+    a: object
+    un: object
+    sp: object
+    objno: object
+
+    @staticmethod
+    def upload(case, device="cuda"):
+        torch = _torch()
+
+        def t(a):
+            return torch.from_numpy(np.ascontiguousarray(a)).to(device)
+        return DeviceCase(case=case, dims=torch.from_numpy(case.dims.copy()), x=t(case.x), dx=t(case.dx),
+                          mn=t(case.mn), in_=t(case.in_), jn=t(case.jn), kn=t(case.kn), nf=t(case.nf),
+                          nfb=t(case.nfb), f=t(case.f), fb=t(case.fb), a=t(case.a), un=t(case.un),
+                          sp=t(case.sp), objno=t(case.objno))
+
+
+@dataclasses.dataclass
+class DeviceSystem:
+    """Everything the pressure-correction loop builds on the device."""
+    ifln: int
+    isfn: int
+    passes: int
+    fln: object          # int32 (ifln,) == fln(1:ifln)
+    sfn: object
+    mp: object           # f64 (1,)
+    alu_c: object        # (6, inne)
+    ll_c: object
+    de_c: object
+    mm2: int
+    mnoe: int
+    dmax: float
+    mno: object          # (je, ke, ie)
+    mno2mn: object       # (mm2,) == mno2mn(1:mm2)
+    b: object            # (mm2,) == b(1:mm2)
+    xe: object           # (mm2+1,) == xe(0:mm2)
+    de: object           # (mm2,)
+    alu: object          # (6, mm2)
+    llu: object          # (6, mm2)
+
+
+def set_nflag_dev(dc: DeviceCase):
+    torch = _torch()
+    L = lib()
+    case = dc.case
+    ncell = case.inne2 + 2
+    fln = torch.zeros(ncell + 1, dtype=torch.int32, device="cuda")
+    sfn = torch.zeros(ncell + 1, dtype=torch.int32, device="cuda")
+    wbytes = L.clowns_set_nflag_workspace_bytes(dc.dims.numpy().ctypes.data, case.inne2)
+    work = torch.empty(max(1, wbytes), dtype=torch.uint8, device="cuda")
+    ifln, isfn, passes = C.c_int(0), C.c_int(0), C.c_int(0)
+    dims = dc.dims.numpy()
+    rc = L.clowns_set_nflag_dev(dims.ctypes.data, case.inne, case.inne2, case.mx2, _ptr(dc.mn), _ptr(dc.in_),
+                                _ptr(dc.jn), _ptr(dc.kn), _ptr(dc.nf), _ptr(dc.nfb), _ptr(dc.f), _ptr(dc.fb),
+                                _ptr(dc.a), _ptr(dc.dx), _ptr(dc.objno), _ptr(fln), C.byref(ifln), _ptr(sfn),
+                                C.byref(isfn), C.byref(passes), _ptr(work), wbytes, _stream())
+    _check(rc, "set_nflag")
+    return fln[:ifln.value], ifln.value, sfn[:isfn.value], isfn.value, passes.value
+
+
+def init_matrix_dev(dc: DeviceCase):
+    torch = _torch()
+    L = lib()
+    case = dc.case
+    mp = torch.zeros(1, dtype=torch.float64, device="cuda")
+    alu_c = torch.empty((6, case.inne), dtype=torch.float64, device="cuda")
+    ll_c = torch.empty((6, case.inne), dtype=torch.int32, device="cuda")
+    de_c = torch.empty(case.inne, dtype=torch.float64, device="cuda")
+    dims = dc.dims.numpy()
+    rc = L.clowns_init_matrix_dev(dims.ctypes.data, case.inne, case.mx2, _ptr(dc.mn), _ptr(dc.in_), _ptr(dc.jn),
+                                  _ptr(dc.kn), _ptr(dc.nf), _ptr(dc.nfb), _ptr(dc.a), _ptr(dc.fb), _ptr(dc.dx),
+                                  _ptr(mp), _ptr(alu_c), _ptr(ll_c), _ptr(de_c), _stream())
+    _check(rc, "init_matrix")
+    return mp, alu_c, ll_c, de_c
+
+
+def rows_rhs_assemble_dev(dc: DeviceCase, fln, ifln: int, mp, alu_c, ll_c, de_c, mm2: Optional[int] = None):
+    torch = _torch()
+    L = lib()
+    case = dc.case
+    if mm2 is None:
+        mm2 = ifln + 5000                       # m_alloc = ifln + 5000 (1sub-momentum.F90:254)
+    is_, js, ks, ie, je, ke = (int(v) for v in case.dims)
+    dims = dc.dims.numpy()
+    mno = torch.empty((je, ke, ie), dtype=torch.int32, device="cuda")
+    mno2mn = torch.zeros(mm2, dtype=torch.int32, device="cuda")
+    b = torch.empty(mm2, dtype=torch.float64, device="cuda")
+    xe = torch.zeros(mm2 + 1, dtype=torch.float64, device="cuda")
+    de = torch.empty(mm2, dtype=torch.float64, device="cuda")
+    wbytes = L.clowns_rows_rhs_workspace_bytes(ifln)
+    work = torch.empty(max(1, wbytes), dtype=torch.uint8, device="cuda")
+    mnoe = C.c_int(0)
+    dmax = C.c_double(0.0)
+    flnp = _ptr(fln) if ifln > 0 else _ptr(mno2mn)
+    rc = L.clowns_rows_rhs_dev(dims.ctypes.data, case.inne2, case.mx2, _ptr(dc.mn), _ptr(dc.in_), _ptr(dc.jn),
+                               _ptr(dc.kn), _ptr(dc.nf), _ptr(dc.nfb), _ptr(dc.f), _ptr(dc.fb), _ptr(dc.a),
+                               _ptr(dc.un), _ptr(dc.dx), _ptr(mp), case.dt, ifln, flnp, mm2, _ptr(mno),
+                               _ptr(mno2mn), _ptr(b), _ptr(xe) + 8, _ptr(de), C.byref(mnoe), C.byref(dmax),
+                               _ptr(work), wbytes, _stream())
+    _check(rc, "rows_rhs")
+    alu = torch.zeros((6, mm2), dtype=torch.float64, device="cuda")
+    llu = torch.zeros((6, mm2), dtype=torch.int32, device="cuda")
+    err = torch.zeros(1, dtype=torch.int32, device="cuda")
+    rc = L.clowns_assemble_dev(dims.ctypes.data, case.inne, case.inne2, case.mx2, _ptr(dc.in_), _ptr(dc.jn),
+                               _ptr(dc.kn), _ptr(dc.nf), _ptr(dc.nfb), _ptr(dc.x), _ptr(dc.dx), _ptr(dc.sp),
+                               ifln, flnp, _ptr(mno), _ptr(alu_c), _ptr(ll_c), _ptr(de_c), mm2, _ptr(alu),
+                               _ptr(llu), _ptr(de), _ptr(err), _stream())
+    _check(rc, "assemble")
+    bad = int(err.item())
+    if bad:
+        raise ClownsError(f"cal_matrix_element: unexpected flag on row cell {bad}")
+    return dict(mm2=mm2, mnoe=mnoe.value, dmax=dmax.value, mno=mno, mno2mn=mno2mn, b=b, xe=xe, de=de,
+                alu=alu, llu=llu)
+
+
+def prepare_dev(case) -> tuple[DeviceCase, DeviceSystem]:
+    """Upload a case and run classification, static coefficients, rows, RHS and
+    assembly on the GPU."""
+    dc = DeviceCase.upload(case)
+    fln, ifln, sfn, isfn, passes = set_nflag_dev(dc)
+    mp, alu_c, ll_c, de_c = init_matrix_dev(dc)
+    r = rows_rhs_assemble_dev(dc, fln, ifln, mp, alu_c, ll_c, de_c)
+    sy = DeviceSystem(ifln=ifln, isfn=isfn, passes=passes, fln=fln, sfn=sfn, mp=mp, alu_c=alu_c, ll_c=ll_c,
+                      de_c=de_c, **r)
+    return dc, sy
+
+
+class Solver:
+    """Device-resident PCGPME with a persistent workspace (one per size)."""
+
+    def __init__(self, n: int, nl: int = 6):
+        torch = _torch()
+        L = lib()
+        self.n = n
+        self.nl = nl
+        self.wbytes = L.clowns_pcgpme_workspace_bytes(n, nl)
+        self.work = torch.empty(self.wbytes, dtype=torch.uint8, device="cuda")
+
+    def solve(self, alu, llu, de, b, x, eps: float = 1e-10, parm: float = 5.0, itmax: int = 10000,
+              stream=None) -> SolveInfo:
+        """alu/llu: (nl, na) device tensors; de/b: >= n; x: >= n (in/out)."""
+        L = lib()
+        nl, na = alu.shape
+        info = SolveInfo()
+        st = C.c_void_p(stream) if stream is not None else _stream()
+        rc = L.clowns_pcgpme_dev(_ptr(alu), nl, na, _ptr(llu), _ptr(de), self.n, _ptr(b), _ptr(x), eps, parm,
+                                 itmax, _ptr(self.work), self.wbytes, st, C.byref(info))
+        _check(rc, "pcgpme_dev")
+        return info
+
+
+def setup_scaled_dev(alu, llu, de, b, n: int, parm: float = 5.0):
+    """Scaling + per-row sort only (test hook): returns al_s, ll_s (0-based), d_s, b_s."""
+    torch = _torch()
+    L = lib()
+    nl, na = alu.shape
+    al_s = torch.zeros((nl, n), dtype=torch.float64, device="cuda")
+    ll_s = torch.zeros((nl, n), dtype=torch.int32, device="cuda")
+    d_s = torch.zeros(n, dtype=torch.float64, device="cuda")
+    b_s = torch.zeros(n, dtype=torch.float64, device="cuda")
+    wbytes = L.clowns_pcgpme_workspace_bytes(n, nl)
+    work = torch.empty(wbytes, dtype=torch.uint8, device="cuda")
+    rc = L.clowns_pcgpme_setup_dev(_ptr(alu), nl, na, _ptr(llu), _ptr(de), n, _ptr(b), parm, _ptr(al_s),
+                                   _ptr(ll_s), _ptr(d_s), _ptr(b_s), n, _ptr(work), wbytes, _stream())
+    _check(rc, "pcgpme_setup")
+    return al_s, ll_s, d_s, b_s
+
+
+def apply_pm_a_dev(al_s, ll_s, d_s, n: int, x):
+    torch = _torch()
+    L = lib()
+    nl, na = al_s.shape
+    y = torch.zeros(n, dtype=torch.float64, device="cuda")
+    wbytes = L.clowns_pcgpme_workspace_bytes(n, nl)
+    work = torch.empty(wbytes, dtype=torch.uint8, device="cuda")
+    rc = L.clowns_apply_pm_a_dev(_ptr(al_s), _ptr(ll_s), _ptr(d_s), nl, na, n, _ptr(x), _ptr(y), _ptr(work),
+                                 wbytes, _stream())
+    _check(rc, "apply_pm_a")
+    return y
+
+
+def correct_dev(dc: DeviceCase, sy: DeviceSystem, x, p, un):
+    """p -= xe ; estimate_velocity2 with xe = x (rows 1..mnoe)."""
+    L = lib()
+    case = dc.case
+    sy.xe.zero_()
+    sy.xe[1:sy.mnoe + 1] = x[:sy.mnoe]
+    dims = dc.dims.numpy()
+    rc = L.clowns_correct_dev(dims.ctypes.data, case.inne, case.mx2, _ptr(dc.mn), _ptr(dc.in_), _ptr(dc.jn),
+                              _ptr(dc.kn), _ptr(dc.nf), _ptr(dc.nfb), _ptr(dc.a), _ptr(dc.dx), case.dt, sy.mnoe,
+                              _ptr(sy.mno2mn), _ptr(sy.mno), _ptr(sy.xe), _ptr(p), _ptr(un), _stream())
+    _check(rc, "correct")

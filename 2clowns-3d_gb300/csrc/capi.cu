@@ -1,0 +1,122 @@
+// capi.cu -- error reporting and the host-array drop-in for PCGPME.
+#include <cmath>
+#include <cstdio>
+#include <cstring>
+#include <mutex>
+
+#include "common.cuh"
+#include "solver_internal.cuh"
+
+namespace clowns {
+
+static thread_local char g_err[512] = "";
+
+void set_last_error(cudaError_t e, const char* what, const char* file, int line) {
+    snprintf(g_err, sizeof(g_err), "%s: %s (%s:%d)", cudaGetErrorString(e), what, file, line);
+}
+void set_last_error_msg(const char* msg) { snprintf(g_err, sizeof(g_err), "%s", msg); }
+
+// Device buffers backing the host-array drop-in: grow-only, one set per process,
+// reused by every call so that repeated solves of one size replay one cached
+// CUDA graph.
+struct HostPath {
+    std::mutex mu;
+    char* dev = nullptr;
+    size_t cap = 0;
+    cudaStream_t stream = nullptr;
+};
+static HostPath g_host;
+
+static int host_reserve(size_t bytes) {
+    if (!g_host.stream) CLOWNS_CUDA_TRY(cudaStreamCreateWithFlags(&g_host.stream, cudaStreamNonBlocking));
+    if (bytes <= g_host.cap) return CLOWNS_OK;
+    if (g_host.dev) {
+        CLOWNS_CUDA_TRY(cudaStreamSynchronize(g_host.stream));
+        release_all_graphs();
+        cudaFree(g_host.dev);
+        g_host.dev = nullptr;
+        g_host.cap = 0;
+    }
+    size_t want = bytes + bytes / 8;
+    CLOWNS_CUDA_TRY(cudaMalloc((void**)&g_host.dev, want));
+    g_host.cap = want;
+    return CLOWNS_OK;
+}
+
+// Host-array solve: packs AL/LL rows 1..N (leading dimension NA) into device
+// buffers, solves, and copies X(1:N) back.
+static int pcgpme_host(const double* al, int nl, int na, const int* ll, const double* d, int n,
+                       const double* b, double* x, double* eps, double parm, int* iter,
+                       clowns_solve_info* info) {
+    size_t o = 0;
+    auto take = [&](size_t bytes) { size_t at = o; o = align_up(o + bytes, 256); return at; };
+    size_t o_al = take(sizeof(double) * (size_t)nl * n);
+    size_t o_ll = take(sizeof(int) * (size_t)nl * n);
+    size_t o_d = take(sizeof(double) * n);
+    size_t o_b = take(sizeof(double) * n);
+    size_t o_x = take(sizeof(double) * n);
+    size_t wbytes = ws_layout(n, nl).total;
+    size_t o_w = take(wbytes);
+    int rc = host_reserve(o);
+    if (rc) return rc;
+    char* base = g_host.dev;
+    cudaStream_t s = g_host.stream;
+    double* d_al = (double*)(base + o_al);
+    int* d_ll = (int*)(base + o_ll);
+    double* d_d = (double*)(base + o_d);
+    double* d_b = (double*)(base + o_b);
+    double* d_x = (double*)(base + o_x);
+    CLOWNS_CUDA_TRY(cudaMemcpy2DAsync(d_al, sizeof(double) * n, al, sizeof(double) * (size_t)na,
+                                      sizeof(double) * n, nl, cudaMemcpyHostToDevice, s));
+    CLOWNS_CUDA_TRY(cudaMemcpy2DAsync(d_ll, sizeof(int) * n, ll, sizeof(int) * (size_t)na,
+                                      sizeof(int) * n, nl, cudaMemcpyHostToDevice, s));
+    CLOWNS_CUDA_TRY(cudaMemcpyAsync(d_d, d, sizeof(double) * n, cudaMemcpyHostToDevice, s));
+    CLOWNS_CUDA_TRY(cudaMemcpyAsync(d_b, b, sizeof(double) * n, cudaMemcpyHostToDevice, s));
+    CLOWNS_CUDA_TRY(cudaMemcpyAsync(d_x, x, sizeof(double) * n, cudaMemcpyHostToDevice, s));
+    rc = pcgpme_dev_impl(d_al, nl, n, d_ll, d_d, n, d_b, d_x, eps[0], parm, *iter, base + o_w,
+                         wbytes, s, info);
+    if (rc) return rc;
+    CLOWNS_CUDA_TRY(cudaMemcpyAsync(x, d_x, sizeof(double) * n, cudaMemcpyDeviceToHost, s));
+    CLOWNS_CUDA_TRY(cudaStreamSynchronize(s));
+    return CLOWNS_OK;
+}
+
+}  // namespace clowns
+
+using namespace clowns;
+
+extern "C" const char* clowns_last_error(void) { return g_err; }
+extern "C" int clowns_version(void) { return 10000; }
+
+extern "C" void pcgpme_gpu(double* al, const int* nl, const int* na, int* ll, double* d,
+                           const int* n, const int* n2, double* b, double* x, double* eps,
+                           const double* parm, int* iter, int* ier) {
+    if (!al || !nl || !na || !ll || !d || !n || !n2 || !b || !x || !eps || !parm || !iter || !ier) {
+        if (ier) *ier = CLOWNS_IER_ARG;
+        set_last_error_msg("pcgpme_gpu: NULL argument");
+        return;
+    }
+    const int NL = *nl, NA = *na, N = *n;
+    if (N < 1 || NA < N || (NL != 6 && NL != 4) || *n2 < 0) {
+        *ier = CLOWNS_IER_ARG;
+        set_last_error_msg("pcgpme_gpu: invalid sizes");
+        return;
+    }
+    std::lock_guard<std::mutex> lk(g_host.mu);
+    clowns_solve_info info;
+    memset(&info, 0, sizeof(info));
+    int rc = pcgpme_host(al, NL, NA, ll, d, N, b, x, eps, *parm, iter, &info);
+    if (rc) {
+        *ier = CLOWNS_IER_DEVICE;
+        return;
+    }
+    eps[0] = info.eps;
+    *iter = info.iter;
+    *ier = info.ier;
+}
+
+extern "C" void pcgpme_(double* al, const int* nl, const int* na, int* ll, double* d, const int* n,
+                        const int* n2, double* b, double* x, double* eps, const double* parm,
+                        int* iter, int* ier) {
+    pcgpme_gpu(al, nl, na, ll, d, n, n2, b, x, eps, parm, iter, ier);
+}

@@ -1,0 +1,284 @@
+"""Benchmark: pressure solves/s on the 256x256x96 sloping-beach workload.
+
+One step = one PCGPME solve (setup + BiCGSTAB to ERR <= 1e-10, the reference's
+stop tests) of the assembled pressure system.  ``value`` is measured with the
+matrix, right-hand side and workspace resident in HBM (as inside the
+reference's ik loop); ``e2e`` is the same solve through the host-array drop-in
+``pcgpme_gpu`` (the call the Fortran model makes), with the host->device copy
+of AL, LL, D, B, X and the device->host copy of X inside the timed region.
+
+``--impl reference`` times the reference algorithm on the host cores instead:
+the oracle's OpenMP restatement of PCGPME (the Fortran reference cannot be
+compiled here: ifort-only, no Fortran compiler on either machine).
+
+Multi-GPU: the solve is one coupled system, so N GPUs run N independent
+replicas (one solve each per step, weak scaling, no collective).
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import pathlib
+import statistics
+import subprocess
+import sys
+import time
+
+import numpy as np
+
+ROOT = pathlib.Path(__file__).resolve().parent
+sys.path.insert(0, str(ROOT))
+import __graft_entry__ as ge  # noqa: E402
+
+WORKLOAD = "beach_256x256x96"
+
+
+def measured_peaks():
+    p = ROOT / "MEASURED_PEAKS.json"
+    if p.exists():
+        d = json.loads(p.read_text())
+        return float(d["hbm_gbs"]), "measured"
+    return 6800.0, "fallback"
+
+
+def bytes_solve_fp64(n: int, iters: int) -> float:
+    """Algorithmic bytes of one FP64 solve: N (62 + 68 iters) words of 8 B
+    (floating-point streams only; see the design doc for the per-part count)."""
+    return float(n) * (62 + 68 * iters) * 8.0
+
+
+class Clocks:
+    """nvidia-smi sampler running during the timed region."""
+
+    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, gpu_index: int):
+        self.proc = None
+        self.gpu_index = gpu_index
+        self.path = ROOT / "gpurun_out" / f"clocks_{os.getpid()}.csv"
+
+    def start(self):
+        try:
+            self.path.parent.mkdir(exist_ok=True)
+            self.fh = open(self.path, "w")
+            self.proc = subprocess.Popen(["nvidia-smi", f"--id={self.gpu_index}", f"--query-gpu={self.FIELDS}",
+                                          "--format=csv,noheader,nounits", "-lms", "200"],
+                                         stdout=self.fh, stderr=subprocess.DEVNULL)
+        except Exception:
+            self.proc = None
+
+    def stop(self):
+        if self.proc is None:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["unsampled"]}
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except Exception:
+            self.proc.kill()
+        self.fh.close()
+        sm, smax, reasons = [], None, set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for ln in self.path.read_text().splitlines():
+            parts = [p.strip() for p in ln.split(",")]
+            if len(parts) < 9:
+                continue
+            try:
+                sm.append(float(parts[1]))
+                smax = float(parts[2])
+            except ValueError:
+                continue
+            for nm, v in zip(names, parts[5:9]):
+                if v.lower().startswith("active"):
+                    reasons.add(nm)
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": smax,
+                "reasons": sorted(reasons), "samples": len(sm)}
+
+
+def dist_init():
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    if world > 1:
+        import torch.distributed as dist
+        backend = "nccl" if os.environ.get("CLOWNS_BACKEND", "nccl") == "nccl" else "gloo"
+        dist.init_process_group(backend=backend)
+    return world, rank, local
+
+
+def barrier(world):
+    if world > 1:
+        import torch.distributed as dist
+        dist.barrier()
+
+
+def max_over_ranks(v: float, world: int) -> float:
+    if world <= 1:
+        return v
+    import torch
+    import torch.distributed as dist
+    t = torch.tensor([v], dtype=torch.float64, device="cuda")
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+def cpu_reference_solve(ora, sy, eps, threads):
+    t0 = time.perf_counter()
+    r = ora.pcgpme(sy.alu, sy.llu, sy.de[1:], sy.b[1:], sy.mnoe, eps=eps, nthreads=threads)
+    return time.perf_counter() - t0, r
+
+
+def run_reference(args, world, rank):
+    """Reference arm: the oracle's OpenMP PCGPME on all host cores."""
+    if rank != 0:
+        return
+    pkg = ge.load_package()
+    ora = ge.load_oracle()
+    ora.build()
+    case = pkg.workload.beach_256x256x96()
+    cls, sm, sy = ora.prepare(case)
+    threads = os.cpu_count() or 1
+    for _ in range(args.warmup):
+        cpu_reference_solve(ora, sy, case.eps0, threads)
+    times = []
+    last = None
+    for _ in range(args.steps):
+        t, last = cpu_reference_solve(ora, sy, case.eps0, threads)
+        times.append(t)
+    tot = sum(times)
+    value = args.steps / tot
+    line = {
+        "impl": "reference", "metric": "pressure solves/s", "value": value, "unit": "solves/s",
+        "n_gpus": args.gpus, "steps": args.steps, "warmup": args.warmup,
+        "ms_per_step": 1000.0 * tot / args.steps, "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "f64", "data": "synthetic (seeded generator)",
+        "config": {"workload": WORKLOAD, "rows": sy.mnoe, "tol": case.eps0, "iters": last.iters},
+        "cpu_baseline": {"value": value, "unit": "solves/s", "cores": threads, "kind": "port",
+                         "sample": f"full solves of {WORKLOAD} (N={sy.mnoe}, {last.iters} iterations), "
+                                   f"OpenMP restatement of pcgpme_para.F90, {threads} threads"},
+        "e2e": {"value": value, "unit": "solves/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(line), flush=True)
+
+
+def run_gpu(args, world, rank, local):
+    import torch
+    torch.cuda.set_device(local)
+    pkg = ge.load_package()
+    pkg.build()
+    case = pkg.workload.beach_256x256x96(seed=1)
+    dc, ds = pkg.prepare_dev(case)
+    n = ds.mnoe
+    solver = pkg.Solver(n)
+    x = torch.zeros(ds.mm2, dtype=torch.float64, device="cuda")
+    stream = torch.cuda.current_stream()
+    # warm-up (builds and caches the solve graph)
+    info = None
+    for _ in range(args.warmup):
+        info = solver.solve(ds.alu, ds.llu, ds.de, ds.b, x, eps=case.eps0)
+    # ---- device-resident timing
+    clocks = Clocks(local)
+    barrier(world)
+    torch.cuda.synchronize()
+    clocks.start()
+    ev0 = torch.cuda.Event(enable_timing=True)
+    ev1 = torch.cuda.Event(enable_timing=True)
+    ev0.record(stream)
+    iters = []
+    for _ in range(args.steps):
+        info = solver.solve(ds.alu, ds.llu, ds.de, ds.b, x, eps=case.eps0)
+        iters.append(info.iter)
+    ev1.record(stream)
+    torch.cuda.synchronize()
+    barrier(world)
+    clk = clocks.stop()
+    ms = ev0.elapsed_time(ev1)
+    ms = max_over_ranks(ms, world)
+    per_solve_s = ms / 1000.0 / args.steps
+    value = world * args.steps / (ms / 1000.0)
+    it = int(round(statistics.mean(iters)))
+    peak, peak_kind = measured_peaks()
+    alg = bytes_solve_fp64(n, it)
+    achieved = alg / per_solve_s / 1e9
+
+    # ---- end-to-end through the host-array drop-in (Fortran call shape)
+    al = ds.alu.cpu().numpy()
+    ll = ds.llu.cpu().numpy()
+    de = ds.de.cpu().numpy()
+    b = ds.b.cpu().numpy()
+    xh = np.zeros(ds.mm2)
+    for _ in range(max(1, args.warmup)):
+        xh[:] = 0.0
+        pkg.pcgpme(al, ll, de, b, xh, n, eps=case.eps0)
+    barrier(world)
+    torch.cuda.synchronize()
+    e2e_times = []
+    for _ in range(args.steps):
+        xh[:] = 0.0
+        t0 = time.perf_counter()
+        eps_o, it_o, ier = pkg.pcgpme(al, ll, de, b, xh, n, eps=case.eps0)
+        e2e_times.append(time.perf_counter() - t0)
+    barrier(world)
+    e2e_s = max_over_ranks(sum(e2e_times), world)
+    e2e_value = world * args.steps / e2e_s
+    h2d = n * 6 * 8 + n * 6 * 4 + 3 * n * 8
+    d2h = n * 8
+
+    # ---- CPU baseline: the oracle on the host cores (rank 0, N=1 only)
+    cpu = None
+    if rank == 0 and world == 1 and not args.no_cpu:
+        ora = ge.load_oracle()
+        ora.build()
+        cls, sm, sy = ora.prepare(case)
+        threads = os.cpu_count() or 1
+        t, r = cpu_reference_solve(ora, sy, case.eps0, threads)
+        cpu = {"value": 1.0 / t, "unit": "solves/s", "cores": threads, "kind": "port",
+               "sample": f"one full solve of {WORKLOAD} (N={sy.mnoe}, {r.iters} iterations), OpenMP "
+                         f"restatement of pcgpme_para.F90 on {threads} threads"}
+
+    if rank == 0:
+        line = {
+            "metric": "pressure solves/s", "value": value, "unit": "solves/s", "n_gpus": world,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms / args.steps,
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+            "data": "synthetic (seeded generator)",
+            "config": {"workload": WORKLOAD, "rows": n, "tol": case.eps0, "iters": it,
+                       "stop": pkg.STOP_NAMES.get(info.reason), "eps": info.eps,
+                       "l2": "inputs larger than L2 (matrix %.0f MB)" % (n * 80 / 1e6),
+                       "path": "plain FP64", "parallelism": f"replicas x{world}"},
+            "roofline": {"bound": "hbm", "kernel": "pcgpme solve (one graph launch)",
+                         "achieved": achieved, "peak": peak, "peak_kind": peak_kind, "unit": "GB/s",
+                         "frac": achieved / peak, "traffic": None,
+                         "algorithmic_bytes_per_solve": alg},
+            "e2e": {"value": e2e_value, "unit": "solves/s", "h2d_bytes_per_step": h2d,
+                    "d2h_bytes_per_step": d2h},
+            "gpu_launches": args.steps * (3 + 17 + 16 * it),
+            "clocks": clk,
+        }
+        if cpu:
+            line["cpu_baseline"] = cpu
+        print(json.dumps(line), flush=True)
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=10)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="gpu", choices=["gpu", "reference"])
+    ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline leg")
+    args = ap.parse_args()
+    world, rank, local = dist_init()
+    if args.impl == "reference":
+        run_reference(args, world, rank)
+    else:
+        run_gpu(args, world, rank, local)
+    if world > 1:
+        import torch.distributed as dist
+        dist.destroy_process_group()
+
+
+if __name__ == "__main__":
+    main()

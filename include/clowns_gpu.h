@@ -1,0 +1,198 @@
+/*
+ * clowns_gpu.h -- C ABI of the GB300 pressure-Poisson solve for 2CLOWNS-3D.
+ *
+ * The library (libclowns_gpu.so, sm_103a) replaces the reference's pressure
+ * correction path: the static matrix coefficients (init_matrix), the row
+ * numbering and right-hand side (cal_err_of_continuity), the per-step matrix
+ * assembly (cal_matrix_element), the left-preconditioned BiCGSTAB solve
+ * (PCGPME) and the pressure / velocity correction.  Every entry point takes
+ * plain pointers and sizes in the reference's own array layouts:
+ *
+ *   dims[6]   = is, js, ks, ie, je, ke  (computational cells i = is..ie-1 ...)
+ *   mn        : mn(is-2:ie+2, ks-2:ke+2, js-2:je+2), int32, i fastest
+ *   mno       : mno(1:ie, 1:ke, 1:je), int32, i fastest
+ *   x, dx     : x(0:2, 1:mx2), component fastest
+ *   in/jn/kn  : in(1:inne2) etc., passed as a pointer to element 0 (unused)
+ *   nf, nfb   : nff(0:inne2+1)%f and %b as two plain int32 arrays
+ *   f, fb     : f(0:inne2+1), fb(0:inne2+1)
+ *   a, un     : a(0:2, 0:inne2+1), component fastest
+ *   sp        : sp(0:inne2+1, 0:2), cell index fastest
+ *   alu_c     : ALU_C(1:inne, 1:6) column-major (leading dimension inne); ll_c alike
+ *   alu, llu  : alu(1:na, 1:nl) column-major (leading dimension na = mm2)
+ *   b, de, xe : 1-based row arrays passed as a pointer to their element 1
+ *               (xe(0) is not touched by the solver)
+ *   fln, sfn  : fln(1:ifln) passed as a pointer to element 1
+ *
+ * Functions whose name ends in _dev take DEVICE pointers and a cudaStream_t
+ * (as void*; NULL = legacy default stream) and allocate nothing: scratch space
+ * is a caller-provided device workspace whose size a *_workspace_bytes query
+ * returns.  Functions without the suffix take HOST pointers, manage device
+ * memory inside the library and return when the results are back on the host.
+ *
+ * Return codes: 0 on success, a negative CLOWNS_ERR_* value on failure (the
+ * message is available from clowns_last_error()).  Solver outcomes use the
+ * reference's IER convention (0 converged or stagnated, 3000 iteration cap) plus
+ * the CLOWNS_IER_* codes below, all non-zero and distinct from 3000 so that the
+ * reference's caller maps them to icon = 911 and stops
+ * (1sub-momentum.F90:568-587).
+ */
+#ifndef CLOWNS_GPU_H
+#define CLOWNS_GPU_H
+
+#include <stddef.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* ---- status codes -------------------------------------------------------- */
+#define CLOWNS_OK 0
+#define CLOWNS_ERR_CUDA (-1)      /* a CUDA runtime call failed                 */
+#define CLOWNS_ERR_ARG (-2)       /* invalid argument (sizes, NULL, alignment)  */
+#define CLOWNS_ERR_WORKSPACE (-3) /* workspace smaller than required            */
+#define CLOWNS_ERR_NOCONV (-4)    /* a device fixed point did not settle        */
+#define CLOWNS_ERR_LIMIT (-5)     /* size beyond a stated maximum               */
+
+/* IER values beyond the reference's 0 / 3000 */
+#define CLOWNS_IER_MAXITER 3000   /* iteration cap (pcgpme_para.F90:250-251)     */
+#define CLOWNS_IER_NONFINITE 9101 /* RQ, SS or RN became NaN/Inf                 */
+#define CLOWNS_IER_DEVICE 9102    /* CUDA failure inside the solve               */
+#define CLOWNS_IER_ARG 9104       /* invalid arguments to the drop-in            */
+
+/* Stop reasons reported by the solvers */
+#define CLOWNS_STOP_TOL 0         /* ERR <= EPS(1)            (pcgpme_para.F90:232) */
+#define CLOWNS_STOP_STAGNATION 1  /* |ERR-ERRP| <= 1e-6 ERR   (pcgpme_para.F90:228) */
+#define CLOWNS_STOP_AMU_ZERO 2    /* AMU == 0                 (pcgpme_para.F90:234) */
+#define CLOWNS_STOP_C1_ZERO 3     /* C1 == 0                  (pcgpme_para.F90:240) */
+#define CLOWNS_STOP_MAXITER 4     /* loop exhausted           (pcgpme_para.F90:250) */
+#define CLOWNS_STOP_NONFINITE 5   /* non-finite scalar (new, no reference counterpart) */
+
+typedef struct clowns_solve_info {
+    double eps;     /* final ERR = sqrt(RN/BN), the value PCGPME returns in EPS(1) */
+    double bn;      /* BN = ||PM W b||^2                                           */
+    int iter;       /* the value PCGPME returns in ITER                            */
+    int ier;        /* 0, 3000 or CLOWNS_IER_*                                     */
+    int reason;     /* CLOWNS_STOP_*                                               */
+    int outer;      /* refinement sweeps (mixed precision), else 0                 */
+} clowns_solve_info;
+
+const char* clowns_last_error(void);
+int clowns_version(void);
+
+/* ========================================================================== */
+/* PCGPME -- left-preconditioned BiCGSTAB, plain FP64                          */
+/* ========================================================================== */
+
+/* Drop-in for SUBROUTINE PCGPME(AL,NL,NA,LL,D,N,N2,B,X,EPS,PARM,ITER,IER)
+ * (src2LOWNS/pcgpme_para.F90:1-354), called by cal_poisson_equation at
+ * src2LOWNS/1sub-momentum.F90:564.  Same by-reference arguments, host arrays:
+ *   AL(NA,NL), LL(NA,NL) column-major (LL 1-based, 0 = no neighbour), D(N),
+ *   B(N), X(N+N2) (initial guess in, solution out), EPS(2) (tolerance in,
+ *   final ERR out), PARM, ITER (cap in, iterations used out), IER out.
+ * Differences from the reference, by design: AL, LL, D and B are left unmodified
+ * (the reference scales/sorts them in place and leaves the final residual in B;
+ * its only caller rebuilds all four before the next call, 1sub-momentum.F90:48
+ * and 267-360), and a NaN/Inf in RQ, SS or RN ends the solve with
+ * IER = CLOWNS_IER_NONFINITE instead of running on to the iteration cap. */
+void pcgpme_gpu(double* al, const int* nl, const int* na, int* ll, double* d, const int* n,
+                const int* n2, double* b, double* x, double* eps, const double* parm,
+                int* iter, int* ier);
+
+/* Link-level alias with the name ifort gives the Fortran subroutine, so that an
+ * executable linked against this library instead of pcgpme_para.o calls the GPU
+ * solve with no source change. */
+void pcgpme_(double* al, const int* nl, const int* na, int* ll, double* d, const int* n,
+             const int* n2, double* b, double* x, double* eps, const double* parm,
+             int* iter, int* ier);
+
+/* Device-resident variant of the same solve (replaces pcgpme_para.F90:1-354
+ * when the matrix already lives in HBM, as inside the ik loop of
+ * 1sub-momentum.F90:42-60).  al/ll: (na, nl) column-major device arrays,
+ * d/b: length n, x: length >= n (initial guess in, solution out).  The scaled
+ * and sorted copy of the matrix and all Krylov vectors live in `work`. */
+size_t clowns_pcgpme_workspace_bytes(int n, int nl);
+int clowns_pcgpme_dev(const double* al, int nl, int na, const int* ll, const double* d, int n,
+                      const double* b, double* x, double eps, double parm, int iter,
+                      void* work, size_t work_bytes, void* stream, clowns_solve_info* info);
+
+/* Test hooks of the solve's building blocks (device pointers, workspace laid out
+ * as for clowns_pcgpme_dev).  clowns_pcgpme_setup_dev performs only the scaling
+ * and per-row sort of pcgpme_para.F90:77-112 and copies the scaled, sorted
+ * matrix out: al_s/ll_s (na_out, nl) column-major, 0-based ll_s with every empty
+ * slot pointing at row n (a zero pad row); d_s, b_s length n. */
+int clowns_pcgpme_setup_dev(const double* al, int nl, int na, const int* ll, const double* d,
+                            int n, const double* b, double parm, double* al_s, int* ll_s,
+                            double* d_s, double* b_s, int na_out, void* work,
+                            size_t work_bytes, void* stream);
+/* y = PM * A * x with a scaled/sorted matrix as produced above (AXSUB then
+ * LDUSUB, pcgpme_para.F90:263-352).  x, y: device, length n. */
+int clowns_apply_pm_a_dev(const double* al_s, const int* ll_s, const double* d_s, int nl,
+                          int na_s, int n, const double* x, double* y, void* work,
+                          size_t work_bytes, void* stream);
+
+
+/* ========================================================================== */
+/* Classification, static coefficients, rows, right-hand side, assembly       */
+/* ========================================================================== */
+
+/* set_nflag (src2LOWNS/nfd2015.F90:7-306, NORMAL+OBJECT build), called every
+ * step from cal_vof (1sub-vof.F90:37).  Updates nf/nfb/f in place, writes the
+ * fluid list fln(1:ifln) and surface list sfn(1:isfn) (pointers to element 1).
+ * The reference's pruning and orientation loops run as OpenMP loops that read
+ * flags other iterations write; this entry reproduces their serial order
+ * (descending list position).  The isfn2 tail list (nfd2015.F90:285-304),
+ * which only feeds subsystems outside the pressure solve, is not produced. */
+size_t clowns_set_nflag_workspace_bytes(const int* dims, int inne2);
+int clowns_set_nflag_dev(const int* dims, int inne, int inne2, int mx2, const int* mn,
+                         const int* in_, const int* jn, const int* kn, int* nf, int* nfb,
+                         double* f, const double* fb, const double* a, const double* dx,
+                         const int* objno, int* fln, int* ifln, int* sfn, int* isfn,
+                         int* passes, void* work, size_t work_bytes, void* stream);
+
+/* init_matrix (src2LOWNS/1sub-matrix.F90:3-66), 3D: ALU_C, LL_C, DE_C for
+ * cells 1..inne and mp = minval(dx, dx>0)**2 (written to device *mp).  Rows of
+ * cells that are solid or have zero porosity are zero-filled (the reference
+ * leaves them unset; they are never read). */
+int clowns_init_matrix_dev(const int* dims, int inne, int mx2, const int* mn, const int* in_,
+                           const int* jn, const int* kn, const int* nf, const int* nfb,
+                           const double* a, const double* fb, const double* dx, double* mp,
+                           double* alu_c, int* ll_c, double* de_c, void* stream);
+
+/* cal_err_of_continuity at ik == 0 (src2LOWNS/1sub-momentum.F90:235-360): zero
+ * b/xe/de(1:mm2) and mno, number the rows in fluid-list order (mno,
+ * mno2mn(1:mnoe)), and build b(1:mnoe) = mp*DR1/dt for fluid rows.  mp is a
+ * device pointer.  mnoe and dmax = max |DR1| are returned on the host.  Like the
+ * reference, fewer than 10 rows leaves b at zero; mm2 must exceed mnoe by 64
+ * (the reference re-allocates at 302-310; here the caller sizes mm2). */
+size_t clowns_rows_rhs_workspace_bytes(int ifln);
+int clowns_rows_rhs_dev(const int* dims, int inne2, int mx2, const int* mn, const int* in_,
+                        const int* jn, const int* kn, const int* nf, const int* nfb,
+                        const double* f, const double* fb, const double* a, const double* un,
+                        const double* dx, const double* mp, double dt, int ifln, const int* fln,
+                        int mm2, int* mno, int* mno2mn, double* b, double* xe, double* de,
+                        int* mnoe, double* dmax, void* work, size_t work_bytes, void* stream);
+
+/* cal_matrix_element (src2LOWNS/1sub-momentum.F90:465-551), NORMAL build:
+ * alu/llu(1:mm2, 1:6) column-major and de(1:mm2) for every row.  *err_cell
+ * (device int) receives a cell index if a row cell carries a flag other than 1
+ * or 2 (the reference stops there, line 491-492), else 0. */
+int clowns_assemble_dev(const int* dims, int inne, int inne2, int mx2, const int* in_,
+                        const int* jn, const int* kn, const int* nf, const int* nfb,
+                        const double* x, const double* dx, const double* sp, int ifln,
+                        const int* fln, const int* mno, const double* alu_c, const int* ll_c,
+                        const double* de_c, int mm2, double* alu, int* llu, double* de,
+                        int* err_cell, void* stream);
+
+/* Pressure update p(mno2mn(r)) -= xe(r) and estimate_velocity2
+ * (src2LOWNS/1sub-momentum.F90:52-58, 590-651).  xe0 addresses xe(0), which
+ * the reference reads for neighbours that are not rows. */
+int clowns_correct_dev(const int* dims, int inne, int mx2, const int* mn, const int* in_,
+                       const int* jn, const int* kn, const int* nf, const int* nfb,
+                       const double* a, const double* dx, double dt, int mnoe,
+                       const int* mno2mn, const int* mno, const double* xe0, double* p,
+                       double* un, void* stream);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* CLOWNS_GPU_H */

@@ -1,0 +1,184 @@
+"""GPU parity: every stage of the CUDA path against the oracle on the same
+seeded inputs.  Masks, indices and assembled coefficients are compared bit for
+bit; the FP64 solve within 1e-10 relative L2 (floating-point tolerance stated
+per test)."""
+import numpy as np
+import pytest
+
+from cases import small_cases
+
+pytestmark = pytest.mark.gpu
+
+CASES = small_cases()
+IDS = [c[0] for c in CASES]
+
+
+@pytest.fixture(scope="module")
+def prepared(gpu, ora):
+    import torch
+    out = {}
+    for label, case in CASES:
+        cls, sm, sy = ora.prepare(case)
+        dc, ds = gpu.prepare_dev(case)
+        torch.cuda.synchronize()
+        out[label] = (case, cls, sm, sy, dc, ds)
+    return out
+
+
+@pytest.mark.parametrize("label", IDS)
+def test_classification_bit_exact(prepared, label):
+    case, cls, sm, sy, dc, ds = prepared[label]
+    assert ds.ifln == cls.ifln and ds.isfn == cls.isfn
+    assert np.array_equal(dc.nf.cpu().numpy(), cls.nf)
+    assert np.array_equal(dc.nfb.cpu().numpy(), cls.nfb)
+    assert np.array_equal(dc.f.cpu().numpy(), cls.f)
+    assert np.array_equal(ds.fln.cpu().numpy(), cls.fln[1:])
+    assert np.array_equal(ds.sfn.cpu().numpy(), cls.sfn[1:])
+    assert ds.passes == cls.passes
+
+
+@pytest.mark.parametrize("label", IDS)
+def test_init_matrix_bit_exact(prepared, label):
+    case, cls, sm, sy, dc, ds = prepared[label]
+    assert float(ds.mp.item()) == sm.mp
+    assert np.array_equal(ds.ll_c.cpu().numpy(), sm.ll_c)
+    assert np.array_equal(ds.alu_c.cpu().numpy().view(np.int64), sm.alu_c.view(np.int64))
+    assert np.array_equal(ds.de_c.cpu().numpy().view(np.int64), sm.de_c.view(np.int64))
+
+
+@pytest.mark.parametrize("label", IDS)
+def test_rows_rhs_assembly_bit_exact(prepared, label):
+    case, cls, sm, sy, dc, ds = prepared[label]
+    n = sy.mnoe
+    assert ds.mnoe == n and ds.mm2 == sy.mm2
+    assert np.array_equal(ds.mno.cpu().numpy(), sy.mno)
+    assert np.array_equal(ds.mno2mn.cpu().numpy()[:n], sy.mno2mn[1:n + 1])
+    assert ds.dmax == sy.dmax
+    assert np.array_equal(ds.b.cpu().numpy().view(np.int64), sy.b[1:].view(np.int64))
+    assert np.array_equal(ds.llu.cpu().numpy(), sy.llu)
+    assert np.array_equal(ds.alu.cpu().numpy()[:, :n].view(np.int64), sy.alu[:, :n].view(np.int64))
+    assert np.array_equal(ds.de.cpu().numpy()[:n].view(np.int64), sy.de[1:n + 1].view(np.int64))
+
+
+@pytest.mark.parametrize("label", IDS)
+def test_scaling_and_sort_bit_exact(gpu, ora, prepared, label):
+    """Row scaling and per-row exchange sort (pcgpme_para.F90:77-112), ties included."""
+    case, cls, sm, sy, dc, ds = prepared[label]
+    n = sy.mnoe
+    al_s, ll_s, d_s, b_s = gpu.setup_scaled_dev(ds.alu, ds.llu, ds.de, ds.b, n)
+    al_o, ll_o, d_o, b_o = ora.setup_scaled(sy.alu, sy.llu, sy.de[1:], sy.b[1:], n)
+    ll_o0 = np.where(ll_o[:, :n] > n, n, ll_o[:, :n] - 1)      # oracle pads point past N
+    assert np.array_equal(ll_s.cpu().numpy(), ll_o0)
+    assert np.array_equal(al_s.cpu().numpy().view(np.int64), al_o[:, :n].view(np.int64))
+    assert np.array_equal(d_s.cpu().numpy().view(np.int64), d_o.view(np.int64))
+    assert np.array_equal(b_s.cpu().numpy().view(np.int64), b_o.view(np.int64))
+
+
+@pytest.mark.parametrize("label", IDS)
+def test_operator_apply(gpu, ora, prepared, label):
+    """q = PM A x (AXSUB + LDUSUB) within 1e-13 relative (FMA vs separate rounding)."""
+    import torch
+    case, cls, sm, sy, dc, ds = prepared[label]
+    n = sy.mnoe
+    al_s, ll_s, d_s, b_s = gpu.setup_scaled_dev(ds.alu, ds.llu, ds.de, ds.b, n)
+    al_o, ll_o, d_o, b_o = ora.setup_scaled(sy.alu, sy.llu, sy.de[1:], sy.b[1:], n)
+    rng = np.random.default_rng(3)
+    x = rng.standard_normal(n)
+    y = gpu.apply_pm_a_dev(al_s, ll_s, d_s, n, torch.from_numpy(x).cuda()).cpu().numpy()
+    yo = ora.apply_pm_a(al_o, ll_o, d_o, n, x)
+    assert np.linalg.norm(y - yo) <= 1e-13 * np.linalg.norm(yo)
+
+
+@pytest.mark.parametrize("label", IDS)
+def test_solve_matches_oracle(gpu, ora, prepared, label):
+    """Converged pressure within 1e-10 relative L2 of the oracle's PCGPME when both
+    solve to 1e-13 (at the nominal tolerance both carry ~1e-10 solver error)."""
+    import torch
+    case, cls, sm, sy, dc, ds = prepared[label]
+    n = sy.mnoe
+    solver = gpu.Solver(n)
+    for eps in (1e-13, case.eps0):
+        x = torch.zeros(ds.mm2, dtype=torch.float64, device="cuda")
+        info = solver.solve(ds.alu, ds.llu, ds.de, ds.b, x, eps=eps)
+        ref = ora.pcgpme(sy.alu, sy.llu, sy.de[1:], sy.b[1:], n, eps=eps)
+        xg = x.cpu().numpy()[:n]
+        rel = np.linalg.norm(xg - ref.x) / np.linalg.norm(ref.x)
+        assert info.ier == 0 and ref.ier == 0
+        if eps == 1e-13:
+            assert rel <= 1e-10, (label, rel, info.as_dict(), ref.iters)
+        else:
+            assert info.eps <= eps and info.reason in (0, 1)
+            assert rel <= 50 * eps, (label, rel)
+        assert abs(info.iter - ref.iters) <= max(3, ref.iters // 10)
+
+
+def test_solve_vs_direct(gpu, ora, prepared):
+    """Independent check: the GPU pressure solves the assembled system (scipy LU)."""
+    import scipy.sparse.linalg as spl
+    import torch
+    case, cls, sm, sy, dc, ds = prepared["beach_48x40x24"]
+    n = sy.mnoe
+    A = ora.to_csr(sy)
+    xd = spl.spsolve(A.tocsc(), sy.b[1:n + 1])
+    x = torch.zeros(ds.mm2, dtype=torch.float64, device="cuda")
+    gpu.Solver(n).solve(ds.alu, ds.llu, ds.de, ds.b, x, eps=1e-13)
+    xg = x.cpu().numpy()[:n]
+    assert np.linalg.norm(xg - xd) <= 1e-9 * np.linalg.norm(xd)
+
+
+def test_host_dropin_matches_device_and_leaves_inputs(gpu, prepared):
+    """pcgpme_gpu with host arrays == device path; AL, LL, D, B unmodified."""
+    import torch
+    case, cls, sm, sy, dc, ds = prepared["bore_40x24x32"]
+    n = sy.mnoe
+    al = ds.alu.cpu().numpy().copy()
+    ll = ds.llu.cpu().numpy().copy()
+    d = ds.de.cpu().numpy().copy()
+    b = ds.b.cpu().numpy().copy()
+    keep = (al.copy(), ll.copy(), d.copy(), b.copy())
+    x = np.zeros(ds.mm2)
+    eps, it, ier = gpu.pcgpme(al, ll, d, b, x, n, eps=1e-10)
+    xd = torch.zeros(ds.mm2, dtype=torch.float64, device="cuda")
+    info = gpu.Solver(n).solve(ds.alu, ds.llu, ds.de, ds.b, xd, eps=1e-10)
+    assert ier == 0 and it == info.iter and eps == info.eps
+    assert np.array_equal(x[:n], xd.cpu().numpy()[:n])       # same kernels, same order
+    for a0, a1 in zip(keep, (al, ll, d, b)):
+        assert np.array_equal(a0, a1)
+
+
+def test_iteration_cap_and_codes(gpu, prepared):
+    """ITER cap -> IER 3000 and ITER = cap + 1 (Fortran loop exit); NaN -> 9101;
+    bad sizes -> 9104.  Faults are injected on the host, never on the device."""
+    case, cls, sm, sy, dc, ds = prepared["beach_48x40x24"]
+    n = sy.mnoe
+    al = ds.alu.cpu().numpy().copy()
+    ll = ds.llu.cpu().numpy().copy()
+    d = ds.de.cpu().numpy().copy()
+    b = ds.b.cpu().numpy().copy()
+    x = np.zeros(ds.mm2)
+    eps, it, ier = gpu.pcgpme(al, ll, d, b, x, n, eps=1e-14, itmax=5)
+    assert ier == 3000 and it == 6 and eps > 1e-14
+    b2 = b.copy()
+    b2[n // 2] = np.nan
+    x = np.zeros(ds.mm2)
+    eps, it, ier = gpu.pcgpme(al, ll, d, b2, x, n, eps=1e-10)
+    assert ier == gpu.IER_NONFINITE
+    x = np.zeros(ds.mm2)
+    eps, it, ier = gpu.pcgpme(al, ll, d, b, x, 0, eps=1e-10)
+    assert ier == gpu.IER_ARG
+
+
+def test_correction_parity(gpu, ora, prepared):
+    """p -= xe and estimate_velocity2 against the oracle (bit-exact: same ops)."""
+    import torch
+    case, cls, sm, sy, dc, ds = prepared["bore_40x24x32"]
+    n = sy.mnoe
+    rng = np.random.default_rng(9)
+    xe = rng.standard_normal(n) * 1e-3
+    p0 = rng.standard_normal(case.inne2 + 2)
+    p_o, un_o = ora.correct(case, cls, sy, xe, p0, case.un)
+    p_g = torch.from_numpy(p0.copy()).cuda()
+    un_g = torch.from_numpy(case.un.copy()).cuda()
+    gpu.correct_dev(dc, ds, torch.from_numpy(xe).cuda(), p_g, un_g)
+    assert np.array_equal(p_g.cpu().numpy(), p_o)
+    assert np.array_equal(un_g.cpu().numpy().view(np.int64), un_o.view(np.int64))
