@@ -69,9 +69,17 @@ _SIGS = {
                                           C.c_int, C.c_void_p, C.c_double, C.c_void_p, C.c_void_p,
                                           C.c_void_p, C.c_void_p, C.c_int, C.c_void_p, C.c_size_t,
                                           C.c_void_p]),
-    "clowns_apply_pm_a_dev": (C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_int, C.c_int,
-                                        C.c_int, C.c_void_p, C.c_void_p, C.c_void_p, C.c_size_t,
+    "clowns_apply_pm_a_dev": (C.c_int, [C.c_void_p, C.c_int, C.c_int, C.c_void_p, C.c_void_p, C.c_int,
+                                        C.c_double, C.c_void_p, C.c_void_p, C.c_void_p, C.c_size_t,
                                         C.c_void_p]),
+    "clowns_pcgpme_mixed_workspace_bytes": (C.c_size_t, [C.c_int, C.c_int]),
+    "clowns_pcgpme_mixed_dev": (C.c_int, [C.c_void_p, C.c_int, C.c_int, C.c_void_p, C.c_void_p, C.c_int,
+                                          C.c_void_p, C.c_void_p, C.c_double, C.c_double, C.c_double,
+                                          C.c_int, C.c_int, C.c_void_p, C.c_size_t, C.c_void_p, C.c_void_p]),
+    "clowns_pcgpme_batched_workspace_bytes": (C.c_size_t, [C.c_int, C.c_void_p, C.c_int]),
+    "clowns_pcgpme_batched_dev": (C.c_int, [C.c_int, C.c_void_p, C.c_int, C.c_double, C.c_double, C.c_int,
+                                            C.c_double, C.c_int, C.c_int, C.c_void_p, C.c_size_t,
+                                            C.c_void_p, C.c_void_p]),
     "clowns_set_nflag_workspace_bytes": (C.c_size_t, [C.c_void_p, C.c_int]),
     "clowns_set_nflag_dev": (C.c_int, [C.c_void_p, C.c_int, C.c_int, C.c_int] + [C.c_void_p] * 17
                              + [C.c_size_t, C.c_void_p]),
@@ -82,6 +90,8 @@ _SIGS = {
                             + [C.c_size_t, C.c_void_p]),
     "clowns_assemble_dev": (C.c_int, [C.c_void_p, C.c_int, C.c_int, C.c_int] + [C.c_void_p] * 8
                             + [C.c_int] + [C.c_void_p] * 5 + [C.c_int] + [C.c_void_p] * 5),
+    "clowns_transpose_dev": (C.c_int, [C.c_int, C.c_int] + [C.c_void_p] * 8),
+    "clowns_face_grad_dev": (C.c_int, [C.c_void_p, C.c_int, C.c_int, C.c_int] + [C.c_void_p] * 13),
     "clowns_correct_dev": (C.c_int, [C.c_void_p, C.c_int, C.c_int] + [C.c_void_p] * 8
                            + [C.c_double, C.c_int] + [C.c_void_p] * 6),
 }
@@ -308,6 +318,66 @@ def prepare_dev(case) -> tuple[DeviceCase, DeviceSystem]:
     return dc, sy
 
 
+PREC_FP64 = 0
+PREC_MIXED = 1
+
+
+class Member(C.Structure):
+    """clowns_member: one system of an ensemble (device pointers)."""
+    _fields_ = [("al", C.c_void_p), ("ll", C.c_void_p), ("d", C.c_void_p), ("b", C.c_void_p),
+                ("x", C.c_void_p), ("na", C.c_int), ("n", C.c_int), ("nl", C.c_int), ("pad", C.c_int)]
+
+
+class MixedSolver:
+    """FP32-storage BiCGSTAB with FP64 iterative refinement (one system)."""
+
+    def __init__(self, n: int, nl: int = 6):
+        torch = _torch()
+        L = lib()
+        self.n = n
+        self.wbytes = L.clowns_pcgpme_mixed_workspace_bytes(n, nl)
+        self.work = torch.empty(self.wbytes, dtype=torch.uint8, device="cuda")
+
+    def solve(self, alu, llu, de, b, x, eps: float = 1e-10, parm: float = 5.0, inner_tol: float = 0.0,
+              inner_max: int = 0, max_outer: int = 0) -> SolveInfo:
+        L = lib()
+        nl, na = alu.shape
+        info = SolveInfo()
+        rc = L.clowns_pcgpme_mixed_dev(_ptr(alu), nl, na, _ptr(llu), _ptr(de), self.n, _ptr(b), _ptr(x), eps,
+                                       parm, inner_tol, inner_max, max_outer, _ptr(self.work), self.wbytes,
+                                       _stream(), C.byref(info))
+        _check(rc, "pcgpme_mixed_dev")
+        return info
+
+
+class BatchedSolver:
+    """Ensemble of independent systems solved together (FP64 or mixed)."""
+
+    def __init__(self, sizes, precision: int = PREC_MIXED):
+        torch = _torch()
+        L = lib()
+        self.sizes = [int(v) for v in sizes]
+        self.precision = precision
+        arr = (C.c_int * len(self.sizes))(*self.sizes)
+        self.wbytes = L.clowns_pcgpme_batched_workspace_bytes(len(self.sizes), arr, precision)
+        self.work = torch.empty(self.wbytes, dtype=torch.uint8, device="cuda")
+
+    def solve(self, systems, xs, eps: float = 1e-10, parm: float = 5.0, itmax: int = 10000,
+              inner_tol: float = 0.0, inner_max: int = 0, max_outer: int = 0):
+        """systems: list of (alu, llu, de, b) device tensors; xs: list of x tensors."""
+        L = lib()
+        M = len(systems)
+        mem = (Member * M)()
+        for m, ((alu, llu, de, b), x) in enumerate(zip(systems, xs)):
+            nl, na = alu.shape
+            mem[m] = Member(_ptr(alu), _ptr(llu), _ptr(de), _ptr(b), _ptr(x), na, self.sizes[m], nl, 0)
+        infos = (SolveInfo * M)()
+        rc = L.clowns_pcgpme_batched_dev(M, mem, self.precision, eps, parm, itmax, inner_tol, inner_max,
+                                         max_outer, _ptr(self.work), self.wbytes, _stream(), infos)
+        _check(rc, "pcgpme_batched_dev")
+        return list(infos)
+
+
 class Solver:
     """Device-resident PCGPME with a persistent workspace (one per size)."""
 
@@ -349,14 +419,15 @@ def setup_scaled_dev(alu, llu, de, b, n: int, parm: float = 5.0):
     return al_s, ll_s, d_s, b_s
 
 
-def apply_pm_a_dev(al_s, ll_s, d_s, n: int, x):
+def apply_pm_a_dev(alu, llu, de, n: int, x, parm: float = 5.0):
+    """y = PM (W A) x with the scaled, sorted operator built from the assembled matrix."""
     torch = _torch()
     L = lib()
-    nl, na = al_s.shape
+    nl, na = alu.shape
     y = torch.zeros(n, dtype=torch.float64, device="cuda")
     wbytes = L.clowns_pcgpme_workspace_bytes(n, nl)
     work = torch.empty(wbytes, dtype=torch.uint8, device="cuda")
-    rc = L.clowns_apply_pm_a_dev(_ptr(al_s), _ptr(ll_s), _ptr(d_s), nl, na, n, _ptr(x), _ptr(y), _ptr(work),
+    rc = L.clowns_apply_pm_a_dev(_ptr(alu), nl, na, _ptr(llu), _ptr(de), n, parm, _ptr(x), _ptr(y), _ptr(work),
                                  wbytes, _stream())
     _check(rc, "apply_pm_a")
     return y
@@ -373,3 +444,53 @@ def correct_dev(dc: DeviceCase, sy: DeviceSystem, x, p, un):
                               _ptr(dc.kn), _ptr(dc.nf), _ptr(dc.nfb), _ptr(dc.a), _ptr(dc.dx), case.dt, sy.mnoe,
                               _ptr(sy.mno2mn), _ptr(sy.mno), _ptr(sy.xe), _ptr(p), _ptr(un), _stream())
     _check(rc, "correct")
+
+
+# ---------------------------------------------------------------------------
+# Adjoint
+
+def transpose_dev(alu, llu, de, n: int):
+    """Explicit A^T of an assembled ELL matrix (device tensors, 1-based llu)."""
+    torch = _torch()
+    L = lib()
+    nl, na = alu.shape
+    alt = torch.empty_like(alu)
+    llt = torch.empty_like(llu)
+    det = torch.zeros_like(de)
+    bad = torch.zeros(1, dtype=torch.int32, device="cuda")
+    rc = L.clowns_transpose_dev(n, na, _ptr(alu), _ptr(llu), _ptr(de), _ptr(alt), _ptr(llt), _ptr(det), _ptr(bad),
+                                _stream())
+    _check(rc, "transpose")
+    if int(bad.item()):
+        raise ClownsError("transpose: column index out of range")
+    return alt, llt, det
+
+
+def face_grad_dev(dc: DeviceCase, sy: DeviceSystem, x, lam):
+    """dJ/da for the face area fractions, layout of a (inne2+2, 3)."""
+    torch = _torch()
+    L = lib()
+    case = dc.case
+    grad = torch.zeros_like(dc.a)
+    dims = dc.dims.numpy()
+    flnp = _ptr(sy.fln) if sy.ifln > 0 else _ptr(grad)
+    rc = L.clowns_face_grad_dev(dims.ctypes.data, case.inne, case.inne2, sy.ifln, flnp, _ptr(dc.in_), _ptr(dc.jn),
+                                _ptr(dc.kn), _ptr(dc.nf), _ptr(sy.mno), _ptr(sy.alu_c), _ptr(sy.ll_c), _ptr(dc.a),
+                                _ptr(x), _ptr(lam), _ptr(grad), _stream())
+    _check(rc, "face_grad")
+    return grad
+
+
+def adjoint_dev(dc: DeviceCase, sy: DeviceSystem, x, djdx, eps: float = 1e-12, solver=None):
+    """Solve A^T lambda = dJ/dx (PCGPME on the explicit transpose, FP64) and form
+    (dJ/db, dJ/da) = (lambda, face gradient)."""
+    torch = _torch()
+    n = sy.mnoe
+    alt, llt, det = transpose_dev(sy.alu, sy.llu, sy.de, n)
+    lam = torch.zeros(sy.mm2, dtype=torch.float64, device="cuda")
+    rhs = torch.zeros(sy.mm2, dtype=torch.float64, device="cuda")
+    rhs[:n] = djdx[:n]
+    solver = solver or Solver(n)
+    info = solver.solve(alt, llt, det, rhs, lam, eps=eps)
+    grad_a = face_grad_dev(dc, sy, x, lam)
+    return lam[:n], grad_a, info

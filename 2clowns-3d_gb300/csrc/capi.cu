@@ -4,8 +4,8 @@
 #include <cstring>
 #include <mutex>
 
-#include "common.cuh"
-#include "solver_internal.cuh"
+#include "engine.cuh"
+#include "engine_api.h"
 
 namespace clowns {
 
@@ -55,7 +55,7 @@ static int pcgpme_host(const double* al, int nl, int na, const int* ll, const do
     size_t o_d = take(sizeof(double) * n);
     size_t o_b = take(sizeof(double) * n);
     size_t o_x = take(sizeof(double) * n);
-    size_t wbytes = ws_layout(n, nl).total;
+    size_t wbytes = engine_workspace_bytes(1, &n, 0);
     size_t o_w = take(wbytes);
     int rc = host_reserve(o);
     if (rc) return rc;
@@ -73,8 +73,10 @@ static int pcgpme_host(const double* al, int nl, int na, const int* ll, const do
     CLOWNS_CUDA_TRY(cudaMemcpyAsync(d_d, d, sizeof(double) * n, cudaMemcpyHostToDevice, s));
     CLOWNS_CUDA_TRY(cudaMemcpyAsync(d_b, b, sizeof(double) * n, cudaMemcpyHostToDevice, s));
     CLOWNS_CUDA_TRY(cudaMemcpyAsync(d_x, x, sizeof(double) * n, cudaMemcpyHostToDevice, s));
-    rc = pcgpme_dev_impl(d_al, nl, n, d_ll, d_d, n, d_b, d_x, eps[0], parm, *iter, base + o_w,
-                         wbytes, s, info);
+    MemberIn in;
+    in.al = d_al; in.ll = d_ll; in.d = d_d; in.b = d_b; in.x = d_x;
+    in.na = n; in.n = n; in.nl = nl; in.pad = 0;
+    rc = engine_solve_plain(1, &in, eps[0], parm, *iter, base + o_w, wbytes, s, info);
     if (rc) return rc;
     CLOWNS_CUDA_TRY(cudaMemcpyAsync(x, d_x, sizeof(double) * n, cudaMemcpyDeviceToHost, s));
     CLOWNS_CUDA_TRY(cudaStreamSynchronize(s));

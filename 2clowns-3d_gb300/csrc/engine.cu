@@ -1,0 +1,763 @@
+// engine.cu -- host orchestration of the batched BiCGSTAB engine: workspace
+// layout, member tables, launch-shape autotuning, CUDA-graph capture of the
+// solve (a WHILE conditional node repeats the iteration body until the device
+// stop tests clear it), the plain FP64 path and the mixed-precision path
+// (FP32 storage, FP64 iterative refinement).
+#include <algorithm>
+#include <cmath>
+#include <cstring>
+#include <map>
+#include <mutex>
+#include <tuple>
+#include <vector>
+
+#include "engine.cuh"
+#include "engine_api.h"
+
+namespace clowns {
+
+// ---------------------------------------------------------------------------
+// Mixed-path kernels (FP64 vectors, coefficients of type T)
+
+template <typename T>
+__device__ __forceinline__ bool tile_outer(const Eng<T>& E, int blk, int& m, long& row0, int& rows) {
+    m = E.blk_member[blk];
+    if (m < 0) return false;
+    rows = E.blk_rows[blk];
+    if (rows == 0) return false;
+    if (E.S[m].odone) return false;
+    row0 = (long)blk * kTile;
+    return true;
+}
+
+// r64 = W (b - A x64) with the caller's original FP64 matrix (refinement residual)
+template <typename T>
+__global__ void __launch_bounds__(kEngBlock) k_mx_residual(Eng<T> E) {
+    for (int blk = blockIdx.x; blk < E.nblk; blk += gridDim.x) {
+        int m, rows;
+        long row0;
+        if (!tile_outer(E, blk, m, row0, rows)) continue;
+        const MemberIn in = E.in[m];
+        const long off = E.mem_off[m];
+        for (int r = threadIdx.x; r < rows; r += blockDim.x) {
+            const long i = row0 + r;
+            const long li = i - off;
+            double s = in.d[li] * E.x64[i];
+            for (int k = 0; k < in.nl; k++) {
+                const int c = in.ll[k * (long)in.na + li];
+                if (c > 0 && c <= in.n) s += in.al[k * (long)in.na + li] * E.x64[off + c - 1];
+            }
+            E.r64[i] = E.W[i] * (in.b[li] - s);
+        }
+    }
+}
+
+// One LDUSUB sweep on FP64 vectors with the stored (type T) coefficients
+template <typename T>
+__global__ void __launch_bounds__(kEngBlock) k_mx_sweep(Eng<T> E, int k, const double* __restrict__ in,
+                                                       double* __restrict__ out) {
+    const long NV = E.NV;
+    const T* __restrict__ a = E.al + k * NV;
+    const int* __restrict__ c = E.ll + k * NV;
+    for (int blk = blockIdx.x; blk < E.nblk; blk += gridDim.x) {
+        int m, rows;
+        long row0;
+        if (!tile_outer(E, blk, m, row0, rows)) continue;
+        for (int r = threadIdx.x; r < rows; r += blockDim.x) {
+            const long i = row0 + r;
+            out[i] = in[i] - (double)a[i] * in[c[i]];
+        }
+    }
+}
+
+// Last sweep on FP64 vectors with the squared norm of the result per member.
+//   PHASE 0: BN64 = ||PM W b||^2
+//   PHASE 1: ERR64 = sqrt(||PM r||^2 / BN64); stop the member at the outer
+//            tolerance or sweep cap, else arm its inner solve (mode 1).
+template <typename T, int PHASE>
+__global__ void __launch_bounds__(kEngBlock) k_mx_sweep56(Eng<T> E, const double* __restrict__ in,
+                                                         double* __restrict__ out, double inner_tol,
+                                                         int inner_max) {
+    __shared__ double red[64];
+    const long NV = E.NV;
+    const T* __restrict__ a5 = E.al + 4 * NV;
+    const T* __restrict__ a6 = E.al + 5 * NV;
+    const int* __restrict__ c5 = E.ll + 4 * NV;
+    const int* __restrict__ c6 = E.ll + 5 * NV;
+    for (int blk = blockIdx.x; blk < E.nblk; blk += gridDim.x) {
+        int m, rows;
+        long row0;
+        if (!tile_outer(E, blk, m, row0, rows)) continue;
+        double acc = 0.0;
+        for (int r = threadIdx.x; r < rows; r += blockDim.x) {
+            const long i = row0 + r;
+            const double y = in[i] - (double)a5[i] * in[c5[i]] - (double)a6[i] * in[c6[i]];
+            out[i] = y;
+            acc += y * y;
+        }
+        double tot[2];
+        if (!member_reduce(E, blk, m, acc, 0.0, red, tot)) continue;
+        if (threadIdx.x == 0) {
+            MemberScalars* S = E.S + m;
+            E.ticket[m] = 0;
+            if (PHASE == 0) {
+                S->BN64 = tot[0];
+            } else {
+                const double err = sqrt(tot[0] / S->BN64);
+                S->ERR64 = err;
+                if (!isfinite(err)) {
+                    S->odone = 1;
+                    stop_member(S, CLOWNS_STOP_NONFINITE, CLOWNS_IER_NONFINITE);
+                } else if (err <= S->EPS64) {
+                    S->odone = 1;
+                    stop_member(S, CLOWNS_STOP_TOL, 0);
+                } else if (S->outer >= S->OITER) {
+                    S->odone = 1;
+                    stop_member(S, CLOWNS_STOP_MAXITER, CLOWNS_IER_MAXITER);
+                } else {
+                    S->outer += 1;
+                    S->SIGMA = sqrt(tot[0]);
+                    S->K = 0;
+                    S->ERRP = 0.0;
+                    S->done = 0;
+                    S->mode = 1;
+                    S->EPS = inner_tol;
+                    S->ITER = inner_max;
+                }
+            }
+        }
+        __syncthreads();
+    }
+}
+
+// Inner right-hand side: r = p = r0 = T(PM r64 / sigma), xi = 0; BN = C1 = ||r||^2
+template <typename T>
+__global__ void __launch_bounds__(kEngBlock) k_mx_normalize(Eng<T> E) {
+    __shared__ double red[64];
+    for (int blk = blockIdx.x; blk < E.nblk; blk += gridDim.x) {
+        int m, rows;
+        long row0;
+        if (!tile_outer(E, blk, m, row0, rows)) continue;
+        const double inv = 1.0 / E.S[m].SIGMA;
+        double acc = 0.0;
+        for (int r = threadIdx.x; r < rows; r += blockDim.x) {
+            const long i = row0 + r;
+            const T v = T(E.r64[i] * inv);
+            E.r[i] = v;
+            E.p[i] = v;
+            E.r0[i] = v;
+            E.xi[i] = T(0);
+            acc += (double)v * (double)v;
+        }
+        double tot[2];
+        if (!member_reduce(E, blk, m, acc, 0.0, red, tot)) continue;
+        if (threadIdx.x == 0) {
+            E.ticket[m] = 0;
+            E.S[m].BN = tot[0];
+            E.S[m].C1 = tot[0];
+        }
+        __syncthreads();
+    }
+}
+
+// x64 += sigma * xi (FP64 pressure accumulation)
+template <typename T>
+__global__ void __launch_bounds__(kEngBlock) k_mx_update(Eng<T> E) {
+    for (int blk = blockIdx.x; blk < E.nblk; blk += gridDim.x) {
+        int m, rows;
+        long row0;
+        if (!tile_outer(E, blk, m, row0, rows)) continue;
+        const double sg = E.S[m].SIGMA;
+        for (int r = threadIdx.x; r < rows; r += blockDim.x) {
+            const long i = row0 + r;
+            E.x64[i] += sg * (double)E.xi[i];
+        }
+    }
+}
+
+__global__ void k_mx_reset_ctrl(int* ctrl, int inner_max) {
+    if (threadIdx.x == 0 && blockIdx.x == 0) { ctrl[0] = 0; ctrl[1] = inner_max; }
+}
+
+template <typename T>
+__global__ void k_mx_copy_out(Eng<T> E) {
+    for (long i = (long)blockIdx.x * blockDim.x + threadIdx.x; i < E.NV; i += (long)gridDim.x * blockDim.x) {
+        const int m = E.blk_member[i / kTile];
+        if (m < 0) continue;
+        const long li = i - E.mem_off[m];
+        if (li < E.mem_n[m]) E.in[m].x[li] = E.x64[i];
+    }
+}
+
+__global__ void k_mixed_init_scalars(MemberScalars* S, int M, double eps, int oiter, int* ctrl) {
+    for (int m = threadIdx.x; m < M; m += blockDim.x) {
+        MemberScalars z;
+        memset(&z, 0, sizeof(z));
+        z.EPS64 = eps;
+        z.OITER = oiter;
+        z.mode = 1;
+        S[m] = z;
+    }
+    if (threadIdx.x == 0) { ctrl[0] = 0; ctrl[1] = 0; }
+}
+
+// Export of the scaled/sorted matrix (test hook), member 0 only.
+template <typename T>
+__global__ void k_eng_export(Eng<T> E, double* al_s, int* ll_s, double* d_s, double* b_s, int nl, long na_out) {
+    const int n = E.mem_n[0];
+    for (long i = (long)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (long)gridDim.x * blockDim.x) {
+        for (int k = 0; k < nl; k++) {
+            al_s[k * na_out + i] = (double)E.al[k * E.NV + i];
+            ll_s[k * na_out + i] = E.ll[k * E.NV + i];
+        }
+        d_s[i] = (double)E.d[i];
+        b_s[i] = (double)E.r[i];
+    }
+}
+
+// ---------------------------------------------------------------------------
+// Layout
+
+struct EngLayout {
+    long NV = 0;
+    int M = 0, nblk = 0, mixed = 0, tsize = 8;
+    size_t o_blk_member, o_blk_rows, o_mem_off, o_mem_n, o_mem_nblk, o_mem_blk0, o_ticket, o_ctrl;
+    size_t o_in, o_S, o_partials, o_al, o_ll, o_d, o_vec[8], o_W, o_x64, o_r64, o_s64, o_t64;
+    size_t total = 0;
+};
+
+static EngLayout eng_layout(int M, const int* n, int mixed) {
+    EngLayout L;
+    L.M = M;
+    L.mixed = mixed;
+    L.tsize = mixed ? 4 : 8;
+    long NV = 0;
+    for (int m = 0; m < M; m++) NV += (long)align_up((size_t)n[m] + 1, kTile);
+    L.NV = NV;
+    L.nblk = (int)(NV / kTile);
+    size_t o = 0;
+    auto take = [&](size_t bytes) { size_t at = o; o = align_up(o + (bytes ? bytes : 1), 256); return at; };
+    L.o_blk_member = take(sizeof(int) * L.nblk);
+    L.o_blk_rows = take(sizeof(int) * L.nblk);
+    L.o_mem_off = take(sizeof(int) * M);
+    L.o_mem_n = take(sizeof(int) * M);
+    L.o_mem_nblk = take(sizeof(int) * M);
+    L.o_mem_blk0 = take(sizeof(int) * M);
+    L.o_ticket = take(sizeof(unsigned) * M);
+    L.o_ctrl = take(sizeof(int) * 8);
+    L.o_in = take(sizeof(MemberIn) * M);
+    L.o_S = take(sizeof(MemberScalars) * M);
+    L.o_partials = take(sizeof(double) * 2 * L.nblk);
+    L.o_al = take((size_t)L.tsize * 6 * NV);
+    L.o_ll = take(sizeof(int) * 6 * NV);
+    L.o_d = take((size_t)L.tsize * NV);
+    for (int v = 0; v < 8; v++) L.o_vec[v] = take((size_t)L.tsize * NV);
+    if (mixed) {
+        L.o_W = take(sizeof(double) * NV);
+        L.o_x64 = take(sizeof(double) * NV);
+        L.o_r64 = take(sizeof(double) * NV);
+        L.o_s64 = take(sizeof(double) * NV);
+        L.o_t64 = take(sizeof(double) * NV);
+    } else {
+        L.o_W = L.o_x64 = L.o_r64 = L.o_s64 = L.o_t64 = 0;
+    }
+    L.total = o;
+    return L;
+}
+
+template <typename T>
+static Eng<T> eng_bind(void* work, const EngLayout& L) {
+    char* b = (char*)work;
+    Eng<T> E;
+    E.NV = L.NV;
+    E.M = L.M;
+    E.nblk = L.nblk;
+    E.blk_member = (const int*)(b + L.o_blk_member);
+    E.blk_rows = (const int*)(b + L.o_blk_rows);
+    E.mem_off = (const int*)(b + L.o_mem_off);
+    E.mem_n = (const int*)(b + L.o_mem_n);
+    E.mem_nblk = (const int*)(b + L.o_mem_nblk);
+    E.mem_blk0 = (const int*)(b + L.o_mem_blk0);
+    E.ticket = (unsigned*)(b + L.o_ticket);
+    E.ctrl = (int*)(b + L.o_ctrl);
+    E.in = (const MemberIn*)(b + L.o_in);
+    E.S = (MemberScalars*)(b + L.o_S);
+    E.partials = (double*)(b + L.o_partials);
+    E.al = (T*)(b + L.o_al);
+    E.ll = (int*)(b + L.o_ll);
+    E.d = (T*)(b + L.o_d);
+    T* v[8];
+    for (int i = 0; i < 8; i++) v[i] = (T*)(b + L.o_vec[i]);
+    E.r = v[0]; E.p = v[1]; E.r0 = v[2]; E.q = v[3]; E.e = v[4]; E.v = v[5]; E.t = v[6]; E.xi = v[7];
+    if (L.mixed) {
+        E.W = (double*)(b + L.o_W);
+        E.x64 = (double*)(b + L.o_x64);
+        E.r64 = (double*)(b + L.o_r64);
+        E.s64 = (double*)(b + L.o_s64);
+        E.t64 = (double*)(b + L.o_t64);
+    } else {
+        E.W = E.x64 = E.r64 = E.s64 = E.t64 = nullptr;
+    }
+    return E;
+}
+
+// Upload the member tables (static for a given layout) and the input table.
+static int eng_upload_tables(void* work, const EngLayout& L, const int* n, const MemberIn* ins,
+                             cudaStream_t s) {
+    const int M = L.M;
+    std::vector<int> blk_member(L.nblk, -1), blk_rows(L.nblk, 0), off(M), nn(M), nblk(M), blk0(M);
+    long o = 0;
+    for (int m = 0; m < M; m++) {
+        off[m] = (int)o;
+        nn[m] = n[m];
+        blk0[m] = (int)(o / kTile);
+        nblk[m] = (n[m] + kTile - 1) / kTile;
+        const long R = (long)align_up((size_t)n[m] + 1, kTile);
+        for (long b = o / kTile; b < (o + R) / kTile; b++) {
+            blk_member[b] = m;
+            long rows = n[m] - (b * kTile - o);
+            blk_rows[b] = (int)std::max(0L, std::min((long)kTile, rows));
+        }
+        o += R;
+    }
+    std::vector<unsigned> zeros(M, 0u);
+    char* b = (char*)work;
+    CLOWNS_CUDA_TRY(cudaMemcpyAsync(b + L.o_blk_member, blk_member.data(), sizeof(int) * L.nblk, cudaMemcpyHostToDevice, s));
+    CLOWNS_CUDA_TRY(cudaMemcpyAsync(b + L.o_blk_rows, blk_rows.data(), sizeof(int) * L.nblk, cudaMemcpyHostToDevice, s));
+    CLOWNS_CUDA_TRY(cudaMemcpyAsync(b + L.o_mem_off, off.data(), sizeof(int) * M, cudaMemcpyHostToDevice, s));
+    CLOWNS_CUDA_TRY(cudaMemcpyAsync(b + L.o_mem_n, nn.data(), sizeof(int) * M, cudaMemcpyHostToDevice, s));
+    CLOWNS_CUDA_TRY(cudaMemcpyAsync(b + L.o_mem_nblk, nblk.data(), sizeof(int) * M, cudaMemcpyHostToDevice, s));
+    CLOWNS_CUDA_TRY(cudaMemcpyAsync(b + L.o_mem_blk0, blk0.data(), sizeof(int) * M, cudaMemcpyHostToDevice, s));
+    CLOWNS_CUDA_TRY(cudaMemcpyAsync(b + L.o_ticket, zeros.data(), sizeof(unsigned) * M, cudaMemcpyHostToDevice, s));
+    CLOWNS_CUDA_TRY(cudaMemcpyAsync(b + L.o_in, ins, sizeof(MemberIn) * M, cudaMemcpyHostToDevice, s));
+    CLOWNS_CUDA_TRY(cudaStreamSynchronize(s));
+    return CLOWNS_OK;
+}
+
+// ---------------------------------------------------------------------------
+// Launch shapes (autotuned per row-space size and precision)
+
+struct Shape {
+    int block = kEngBlock;
+    int grid = 0;   // 0: one block per tile
+};
+
+static std::mutex g_shape_mu;
+static std::map<std::pair<long, int>, Shape> g_shapes;
+
+static int grid_of(const Shape& sh, int nblk) { return sh.grid > 0 ? std::min(sh.grid, nblk) : nblk; }
+
+template <typename T>
+static void launch_apply(const Eng<T>& E, const Shape& sh, const T* in, T* out, T* tmp, int mode,
+                         cudaStream_t s) {
+    const int g = grid_of(sh, E.nblk), b = sh.block;
+    k_eng_axsub<T><<<g, b, 0, s>>>(E, in, tmp);
+    k_eng_sweep<T><<<g, b, 0, s>>>(E, 0, tmp, out);
+    k_eng_sweep<T><<<g, b, 0, s>>>(E, 1, out, tmp);
+    k_eng_sweep<T><<<g, b, 0, s>>>(E, 2, tmp, out);
+    k_eng_sweep<T><<<g, b, 0, s>>>(E, 3, out, tmp);
+    if (mode == 0) k_eng_sweep56<T, 0><<<g, b, 0, s>>>(E, tmp, out);
+    if (mode == 1) k_eng_sweep56<T, 1><<<g, b, 0, s>>>(E, tmp, out);
+    if (mode == 2) k_eng_sweep56<T, 2><<<g, b, 0, s>>>(E, tmp, out);
+}
+
+template <typename T>
+static void launch_ldusub_inplace(const Eng<T>& E, const Shape& sh, T* vec, T* a, T* bb, cudaStream_t s) {
+    const int g = grid_of(sh, E.nblk), b = sh.block;
+    k_eng_sweep<T><<<g, b, 0, s>>>(E, 0, vec, a);
+    k_eng_sweep<T><<<g, b, 0, s>>>(E, 1, a, bb);
+    k_eng_sweep<T><<<g, b, 0, s>>>(E, 2, bb, a);
+    k_eng_sweep<T><<<g, b, 0, s>>>(E, 3, a, bb);
+    k_eng_sweep56<T, 0><<<g, b, 0, s>>>(E, bb, vec);
+}
+
+template <typename T>
+static void launch_iteration(const Eng<T>& E, const Shape& sh, cudaStream_t s) {
+    const int g = grid_of(sh, E.nblk), b = sh.block;
+    launch_apply(E, sh, E.p, E.q, E.t, 1, s);     // q = PM A p ; RQ ; ALP
+    k_eng_eupdate<T><<<g, b, 0, s>>>(E);          // e = r - ALP q
+    launch_apply(E, sh, E.e, E.v, E.t, 2, s);     // v = PM A e ; AMU
+    k_eng_xrupdate<T><<<g, b, 0, s>>>(E);         // x, r ; RN, C1 ; stop tests
+    k_eng_pupdate<T><<<g, b, 0, s>>>(E);          // p
+}
+
+// PM r64 in place (FP64 vectors), last sweep with the member norm phase
+template <typename T, int PHASE>
+static void launch_ldusub64(const Eng<T>& E, const Shape& sh, double inner_tol, int inner_max, cudaStream_t s) {
+    const int g = grid_of(sh, E.nblk), b = sh.block;
+    k_mx_sweep<T><<<g, b, 0, s>>>(E, 0, E.r64, E.s64);
+    k_mx_sweep<T><<<g, b, 0, s>>>(E, 1, E.s64, E.t64);
+    k_mx_sweep<T><<<g, b, 0, s>>>(E, 2, E.t64, E.s64);
+    k_mx_sweep<T><<<g, b, 0, s>>>(E, 3, E.s64, E.t64);
+    k_mx_sweep56<T, PHASE><<<g, b, 0, s>>>(E, E.t64, E.r64, inner_tol, inner_max);
+}
+
+// Time candidate shapes on one operator application; keep the fastest.
+template <typename T>
+static Shape autotune(const Eng<T>& E, long key_nv, int key_prec, cudaStream_t s) {
+    {
+        std::lock_guard<std::mutex> lk(g_shape_mu);
+        auto it = g_shapes.find({key_nv, key_prec});
+        if (it != g_shapes.end()) return it->second;
+    }
+    std::vector<Shape> cands;
+    for (int b : {128, 256})
+        for (int g : {0, kNumSMs * 4, kNumSMs * 8, kNumSMs * 16}) {
+            Shape sh;
+            sh.block = b;
+            sh.grid = g;
+            cands.push_back(sh);
+        }
+    cudaEvent_t e0, e1;
+    cudaEventCreate(&e0);
+    cudaEventCreate(&e1);
+    Shape best;
+    float best_ms = 1e30f;
+    for (const Shape& sh : cands) {
+        launch_apply(E, sh, E.p, E.q, E.t, 0, s);      // warm
+        cudaEventRecord(e0, s);
+        for (int rep = 0; rep < 3; rep++) launch_apply(E, sh, E.p, E.q, E.t, 0, s);
+        cudaEventRecord(e1, s);
+        cudaEventSynchronize(e1);
+        float ms = 0.f;
+        cudaEventElapsedTime(&ms, e0, e1);
+        if (ms < best_ms) { best_ms = ms; best = sh; }
+    }
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    std::lock_guard<std::mutex> lk(g_shape_mu);
+    g_shapes[{key_nv, key_prec}] = best;
+    return best;
+}
+
+// ---------------------------------------------------------------------------
+// Graph cache
+
+struct GraphKey {
+    const void* work;
+    long NV;
+    int M, mixed, nl, kind;
+    double P1, tol, imax;
+    bool operator<(const GraphKey& o) const {
+        return std::tie(work, NV, M, mixed, nl, kind, P1, tol, imax) <
+               std::tie(o.work, o.NV, o.M, o.mixed, o.nl, o.kind, o.P1, o.tol, o.imax);
+    }
+};
+static std::mutex g_graph_mu;
+static std::map<GraphKey, cudaGraphExec_t> g_graphs;
+static cudaStream_t g_cap0 = nullptr, g_cap1 = nullptr;
+
+void release_all_graphs() {
+    std::lock_guard<std::mutex> lk(g_graph_mu);
+    for (auto& kv : g_graphs) cudaGraphExecDestroy(kv.second);
+    g_graphs.clear();
+}
+
+void release_graphs_for(const void* work) {
+    std::lock_guard<std::mutex> lk(g_graph_mu);
+    for (auto it = g_graphs.begin(); it != g_graphs.end();) {
+        if (it->first.work == work) {
+            cudaGraphExecDestroy(it->second);
+            it = g_graphs.erase(it);
+        } else {
+            ++it;
+        }
+    }
+}
+
+// Capture: prefix(s) ; WHILE { body(s2) ; guard } ; suffix(s)
+template <typename Prefix, typename Body, typename Suffix>
+static int capture_loop_graph(Prefix prefix, Body body, Suffix suffix, MemberScalars* S, int M, int* ctrl,
+                              cudaGraphExec_t* out) {
+    if (!g_cap0) CLOWNS_CUDA_TRY(cudaStreamCreateWithFlags(&g_cap0, cudaStreamNonBlocking));
+    if (!g_cap1) CLOWNS_CUDA_TRY(cudaStreamCreateWithFlags(&g_cap1, cudaStreamNonBlocking));
+    cudaStream_t s = g_cap0, s2 = g_cap1;
+    CLOWNS_CUDA_TRY(cudaStreamBeginCapture(s, cudaStreamCaptureModeThreadLocal));
+    prefix(s);
+    cudaStreamCaptureStatus st;
+    cudaGraph_t cap;
+    const cudaGraphNode_t* deps = nullptr;
+    size_t ndeps = 0;
+    CLOWNS_CUDA_TRY(cudaStreamGetCaptureInfo(s, &st, nullptr, &cap, &deps, nullptr, &ndeps));
+    cudaGraphConditionalHandle h;
+    CLOWNS_CUDA_TRY(cudaGraphConditionalHandleCreate(&h, cap, 1, cudaGraphCondAssignDefault));
+    cudaGraphNodeParams cp = {cudaGraphNodeTypeConditional};
+    cp.conditional.handle = h;
+    cp.conditional.type = cudaGraphCondTypeWhile;
+    cp.conditional.size = 1;
+    cudaGraphNode_t cnode;
+    CLOWNS_CUDA_TRY(cudaGraphAddNode(&cnode, cap, deps, nullptr, ndeps, &cp));
+    CLOWNS_CUDA_TRY(cudaStreamUpdateCaptureDependencies(s, &cnode, nullptr, 1, cudaStreamSetCaptureDependencies));
+    cudaGraph_t bg = cp.conditional.phGraph_out[0];
+    CLOWNS_CUDA_TRY(cudaStreamBeginCaptureToGraph(s2, bg, nullptr, nullptr, 0, cudaStreamCaptureModeThreadLocal));
+    body(s2);
+    k_eng_guard<<<1, 256, 0, s2>>>(S, M, ctrl, h);
+    cudaGraph_t bout;
+    CLOWNS_CUDA_TRY(cudaStreamEndCapture(s2, &bout));
+    suffix(s);
+    cudaGraph_t g;
+    CLOWNS_CUDA_TRY(cudaStreamEndCapture(s, &g));
+    cudaGraphExec_t ex;
+    CLOWNS_CUDA_TRY(cudaGraphInstantiate(&ex, g, 0));
+    cudaGraphDestroy(g);
+    *out = ex;
+    return CLOWNS_OK;
+}
+
+static int cached_graph(const GraphKey& key, cudaGraphExec_t* out) {
+    auto it = g_graphs.find(key);
+    if (it == g_graphs.end()) return 0;
+    *out = it->second;
+    return 1;
+}
+
+static void store_graph(const GraphKey& key, cudaGraphExec_t ex) {
+    if (g_graphs.size() >= 64) {
+        cudaGraphExecDestroy(g_graphs.begin()->second);
+        g_graphs.erase(g_graphs.begin());
+    }
+    g_graphs[key] = ex;
+}
+
+// ---------------------------------------------------------------------------
+// Solves
+
+static void params(int n, double eps, double parm, int iter, double* eps_o, int* iter_o, double* P1, double* P2) {
+    if (eps <= kTiny) eps = kSmall;                                 // pcgpme_para.F90:51
+    if (iter <= 0) iter = (int)(10 * (std::sqrt((double)n) + 1));   // 52
+    const double p1 = parm < 1.0 ? 4.0 : parm;                      // 56-58
+    *eps_o = eps;
+    *iter_o = iter;
+    *P1 = p1;
+    *P2 = p1 + 1.0;
+}
+
+static int read_infos(void* work, const EngLayout& L, cudaStream_t s, clowns_solve_info* info, int mixed) {
+    std::vector<MemberScalars> h(L.M);
+    CLOWNS_CUDA_TRY(cudaMemcpyAsync(h.data(), (char*)work + L.o_S, sizeof(MemberScalars) * L.M,
+                                    cudaMemcpyDeviceToHost, s));
+    CLOWNS_CUDA_TRY(cudaStreamSynchronize(s));
+    if (!info) return CLOWNS_OK;
+    for (int m = 0; m < L.M; m++) {
+        clowns_solve_info& o = info[m];
+        o.eps = mixed ? h[m].ERR64 : h[m].ERR;
+        o.bn = mixed ? h[m].BN64 : h[m].BN;
+        o.iter = mixed ? h[m].total_iter : h[m].K;
+        o.ier = h[m].bad_index ? CLOWNS_IER_ARG : h[m].ier;
+        o.reason = h[m].reason;
+        o.outer = mixed ? h[m].outer : 0;
+    }
+    return CLOWNS_OK;
+}
+
+size_t engine_workspace_bytes(int M, const int* n, int mixed) {
+    if (M < 1) return 0;
+    for (int m = 0; m < M; m++)
+        if (n[m] < 1) return 0;
+    return eng_layout(M, n, mixed).total;
+}
+
+static int check_members(int M, const MemberIn* ins, std::vector<int>& n, int* nl_out) {
+    n.resize(M);
+    int nl = -1;
+    for (int m = 0; m < M; m++) {
+        const MemberIn& in = ins[m];
+        if (!in.al || !in.ll || !in.d || !in.b || !in.x || in.n < 1 || in.na < in.n || (in.nl != 6 && in.nl != 4)) {
+            set_last_error_msg("pcgpme: invalid member arguments");
+            return CLOWNS_ERR_ARG;
+        }
+        if (nl >= 0 && in.nl != nl) {
+            set_last_error_msg("pcgpme: all members must share nl");
+            return CLOWNS_ERR_ARG;
+        }
+        nl = in.nl;
+        n[m] = in.n;
+    }
+    long tot = 0;
+    for (int m = 0; m < M; m++) tot += (long)align_up((size_t)n[m] + 1, kTile);
+    if (tot >= (1L << 31) - kTile) {
+        set_last_error_msg("pcgpme: total rows exceed the 32-bit index range");
+        return CLOWNS_ERR_LIMIT;
+    }
+    *nl_out = nl;
+    return CLOWNS_OK;
+}
+
+// Plain FP64 (reference method and stop tests) over M members.
+int engine_solve_plain(int M, const MemberIn* ins, double eps, double parm, int iter, void* work,
+                       size_t work_bytes, cudaStream_t s, clowns_solve_info* info) {
+    std::vector<int> n;
+    int nl = 6;
+    int rc = check_members(M, ins, n, &nl);
+    if (rc) return rc;
+    EngLayout L = eng_layout(M, n.data(), 0);
+    if (!work || work_bytes < L.total) {
+        set_last_error_msg("pcgpme: workspace too small");
+        return CLOWNS_ERR_WORKSPACE;
+    }
+    int maxn = *std::max_element(n.begin(), n.end());
+    double eps_r, P1, P2;
+    int iter_r;
+    params(maxn, eps, parm, iter, &eps_r, &iter_r, &P1, &P2);
+    rc = eng_upload_tables(work, L, n.data(), ins, s);
+    if (rc) return rc;
+    Eng<double> E = eng_bind<double>(work, L);
+    k_eng_init_scalars<<<1, 256, 0, s>>>(E.S, M, eps_r, iter_r, 0, E.ctrl);
+    CLOWNS_CUDA_TRY(cudaGetLastError());
+    std::lock_guard<std::mutex> lk(g_graph_mu);
+    GraphKey key{work, L.NV, M, 0, nl, 0, P1, 0.0, 0.0};
+    cudaGraphExec_t ex;
+    if (!cached_graph(key, &ex)) {
+        const int gs = std::min(L.nblk * 4, kEngMaxGrid * 4);
+        if (nl == 6) k_eng_setup<double, 6><<<gs, kEngBlock, 0, s>>>(E, P1, P2, 0);
+        else k_eng_setup<double, 4><<<gs, kEngBlock, 0, s>>>(E, P1, P2, 0);
+        Shape sh = autotune(E, L.NV, 0, s);
+        rc = capture_loop_graph(
+            [&](cudaStream_t cs) {
+                if (nl == 6) k_eng_setup<double, 6><<<gs, kEngBlock, 0, cs>>>(E, P1, P2, 0);
+                else k_eng_setup<double, 4><<<gs, kEngBlock, 0, cs>>>(E, P1, P2, 0);
+                launch_ldusub_inplace(E, sh, E.p, E.t, E.q, cs);     // b^ = PM W b
+                launch_apply(E, sh, E.xi, E.q, E.t, 0, cs);           // q = PM A x0
+                k_eng_initres<double><<<grid_of(sh, E.nblk), sh.block, 0, cs>>>(E);
+            },
+            [&](cudaStream_t cs) { launch_iteration(E, sh, cs); },
+            [&](cudaStream_t cs) { k_eng_copy_out<double><<<gs, kEngBlock, 0, cs>>>(E); },
+            E.S, M, E.ctrl, &ex);
+        if (rc) return rc;
+        store_graph(key, ex);
+        // the autotuning runs wrote the vectors; re-initialise the scalars
+        k_eng_init_scalars<<<1, 256, 0, s>>>(E.S, M, eps_r, iter_r, 0, E.ctrl);
+    }
+    CLOWNS_CUDA_TRY(cudaGraphLaunch(ex, s));
+    return read_infos(work, L, s, info, 0);
+}
+
+// Mixed precision: FP32 coefficients and Krylov vectors in the inner BiCGSTAB,
+// FP64 refinement residual r = W (b - A x), FP64 norms and FP64 x accumulation.
+int engine_solve_mixed(int M, const MemberIn* ins, double eps, double parm, double inner_tol,
+                       int inner_max, int max_outer, void* work, size_t work_bytes, cudaStream_t s,
+                       clowns_solve_info* info) {
+    std::vector<int> n;
+    int nl = 6;
+    int rc = check_members(M, ins, n, &nl);
+    if (rc) return rc;
+    EngLayout L = eng_layout(M, n.data(), 1);
+    if (!work || work_bytes < L.total) {
+        set_last_error_msg("pcgpme_mixed: workspace too small");
+        return CLOWNS_ERR_WORKSPACE;
+    }
+    int maxn = *std::max_element(n.begin(), n.end());
+    double eps_r, P1, P2;
+    int iter_r;
+    params(maxn, eps, parm, 0, &eps_r, &iter_r, &P1, &P2);
+    if (inner_tol <= 0) inner_tol = 1e-4;
+    if (inner_max <= 0) inner_max = 2000;
+    if (max_outer <= 0) max_outer = 30;
+    rc = eng_upload_tables(work, L, n.data(), ins, s);
+    if (rc) return rc;
+    Eng<float> E = eng_bind<float>(work, L);
+    k_mixed_init_scalars<<<1, 256, 0, s>>>(E.S, M, eps_r, max_outer, E.ctrl);
+    const int gs = std::min(L.nblk * 4, kEngMaxGrid * 4);
+    if (nl == 6) k_eng_setup<float, 6><<<gs, kEngBlock, 0, s>>>(E, P1, P2, 1);
+    else k_eng_setup<float, 4><<<gs, kEngBlock, 0, s>>>(E, P1, P2, 1);
+    CLOWNS_CUDA_TRY(cudaGetLastError());
+    std::lock_guard<std::mutex> lk(g_graph_mu);
+    Shape sh = autotune(E, L.NV, 1, s);
+    // BN64 = ||PM W b||^2 (r64 holds W b after the setup)
+    launch_ldusub64<float, 0>(E, sh, inner_tol, inner_max, s);
+    GraphKey key{work, L.NV, M, 1, nl, 1, P1, inner_tol, (double)inner_max};
+    cudaGraphExec_t ex;
+    if (!cached_graph(key, &ex)) {
+        rc = capture_loop_graph(
+            [&](cudaStream_t cs) {
+                k_mx_reset_ctrl<<<1, 32, 0, cs>>>(E.ctrl, inner_max);
+                k_mx_residual<float><<<grid_of(sh, E.nblk), sh.block, 0, cs>>>(E);
+                launch_ldusub64<float, 1>(E, sh, inner_tol, inner_max, cs);
+                k_mx_normalize<float><<<grid_of(sh, E.nblk), sh.block, 0, cs>>>(E);
+            },
+            [&](cudaStream_t cs) { launch_iteration(E, sh, cs); },
+            [&](cudaStream_t cs) { k_mx_update<float><<<grid_of(sh, E.nblk), sh.block, 0, cs>>>(E); },
+            E.S, M, E.ctrl, &ex);
+        if (rc) return rc;
+        store_graph(key, ex);
+    }
+    std::vector<MemberScalars> h(M);
+    for (int sweep = 0; sweep <= max_outer + 1; sweep++) {
+        CLOWNS_CUDA_TRY(cudaGraphLaunch(ex, s));
+        CLOWNS_CUDA_TRY(cudaMemcpyAsync(h.data(), E.S, sizeof(MemberScalars) * M, cudaMemcpyDeviceToHost, s));
+        CLOWNS_CUDA_TRY(cudaStreamSynchronize(s));
+        bool all = true;
+        for (int m = 0; m < M; m++) all = all && h[m].odone;
+        if (all) break;
+    }
+    k_mx_copy_out<float><<<gs, kEngBlock, 0, s>>>(E);
+    CLOWNS_CUDA_TRY(cudaGetLastError());
+    return read_infos(work, L, s, info, 1);
+}
+
+// Test hooks -------------------------------------------------------------------
+
+int engine_setup_export(const MemberIn& in, double parm, double* al_s, int* ll_s, double* d_s, double* b_s,
+                        int na_out, void* work, size_t work_bytes, cudaStream_t s) {
+    std::vector<int> n;
+    int nl;
+    int rc = check_members(1, &in, n, &nl);
+    if (rc) return rc;
+    EngLayout L = eng_layout(1, n.data(), 0);
+    if (!work || work_bytes < L.total) {
+        set_last_error_msg("setup: workspace too small");
+        return CLOWNS_ERR_WORKSPACE;
+    }
+    double e, P1, P2;
+    int it;
+    params(in.n, 0.0, parm, 0, &e, &it, &P1, &P2);
+    rc = eng_upload_tables(work, L, n.data(), &in, s);
+    if (rc) return rc;
+    Eng<double> E = eng_bind<double>(work, L);
+    k_eng_init_scalars<<<1, 32, 0, s>>>(E.S, 1, 1e-10, 1, 0, E.ctrl);
+    if (nl == 6) k_eng_setup<double, 6><<<std::min(L.nblk * 4, 4096), kEngBlock, 0, s>>>(E, P1, P2, 0);
+    else k_eng_setup<double, 4><<<std::min(L.nblk * 4, 4096), kEngBlock, 0, s>>>(E, P1, P2, 0);
+    k_eng_export<double><<<std::min(L.nblk * 4, 4096), kEngBlock, 0, s>>>(E, al_s, ll_s, d_s, b_s, nl, na_out);
+    CLOWNS_CUDA_TRY(cudaGetLastError());
+    CLOWNS_CUDA_TRY(cudaStreamSynchronize(s));
+    return CLOWNS_OK;
+}
+
+__global__ void k_hook_load_x(Eng<double> E, const double* x, int n) {
+    for (long i = (long)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (long)gridDim.x * blockDim.x) E.xi[i] = x[i];
+}
+__global__ void k_hook_store_y(Eng<double> E, double* y, int n) {
+    for (long i = (long)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (long)gridDim.x * blockDim.x) y[i] = E.q[i];
+}
+
+int engine_apply_pm_a(const MemberIn& in, double parm, const double* x, double* y, void* work, size_t work_bytes,
+                      cudaStream_t s) {
+    std::vector<int> n;
+    int nl;
+    int rc = check_members(1, &in, n, &nl);
+    if (rc) return rc;
+    EngLayout L = eng_layout(1, n.data(), 0);
+    if (!work || work_bytes < L.total) {
+        set_last_error_msg("apply: workspace too small");
+        return CLOWNS_ERR_WORKSPACE;
+    }
+    double e, P1, P2;
+    int it;
+    params(in.n, 0.0, parm, 0, &e, &it, &P1, &P2);
+    rc = eng_upload_tables(work, L, n.data(), &in, s);
+    if (rc) return rc;
+    Eng<double> E = eng_bind<double>(work, L);
+    k_eng_init_scalars<<<1, 32, 0, s>>>(E.S, 1, 1e-10, 1, 0, E.ctrl);
+    const int gs = std::min(L.nblk * 4, 4096);
+    if (nl == 6) k_eng_setup<double, 6><<<gs, kEngBlock, 0, s>>>(E, P1, P2, 0);
+    else k_eng_setup<double, 4><<<gs, kEngBlock, 0, s>>>(E, P1, P2, 0);
+    k_hook_load_x<<<gs, kEngBlock, 0, s>>>(E, x, in.n);
+    Shape sh;
+    launch_apply(E, sh, E.xi, E.q, E.t, 0, s);
+    k_hook_store_y<<<gs, kEngBlock, 0, s>>>(E, y, in.n);
+    CLOWNS_CUDA_TRY(cudaGetLastError());
+    CLOWNS_CUDA_TRY(cudaStreamSynchronize(s));
+    return CLOWNS_OK;
+}
+
+}  // namespace clowns

@@ -1,0 +1,25 @@
+// engine_api.h -- host-side entry points of the batched BiCGSTAB engine.
+#pragma once
+
+#include <cuda_runtime.h>
+
+#include "clowns_gpu.h"
+
+namespace clowns {
+
+struct MemberIn;
+
+size_t engine_workspace_bytes(int M, const int* n, int mixed);
+int engine_solve_plain(int M, const MemberIn* ins, double eps, double parm, int iter, void* work,
+                       size_t work_bytes, cudaStream_t s, clowns_solve_info* info);
+int engine_solve_mixed(int M, const MemberIn* ins, double eps, double parm, double inner_tol,
+                       int inner_max, int max_outer, void* work, size_t work_bytes, cudaStream_t s,
+                       clowns_solve_info* info);
+int engine_setup_export(const MemberIn& in, double parm, double* al_s, int* ll_s, double* d_s,
+                        double* b_s, int na_out, void* work, size_t work_bytes, cudaStream_t s);
+int engine_apply_pm_a(const MemberIn& in, double parm, const double* x, double* y, void* work,
+                      size_t work_bytes, cudaStream_t s);
+void release_all_graphs();
+void release_graphs_for(const void* work);
+
+}  // namespace clowns

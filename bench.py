@@ -163,47 +163,119 @@ def run_reference(args, world, rank):
     print(json.dumps(line), flush=True)
 
 
+def bytes_solve_mixed(n: int, inner_iters: int, outer: int) -> float:
+    """Algorithmic bytes of one mixed solve: N [96 + sum_outer(248 + 272 it_j) + 100 outer]
+    = N [96 + 248 outer + 272 iters + 100 outer] (FP32 words of 4 B, FP64 refinement)."""
+    return float(n) * (96 + 248 * outer + 272 * inner_iters + 100 * outer)
+
+
+def time_device(fn, steps, stream):
+    import torch
+    ev0 = torch.cuda.Event(enable_timing=True)
+    ev1 = torch.cuda.Event(enable_timing=True)
+    ev0.record(stream)
+    out = [fn() for _ in range(steps)]
+    ev1.record(stream)
+    torch.cuda.synchronize()
+    return ev0.elapsed_time(ev1), out
+
+
+def workload_case(pkg, name):
+    wl = pkg.workload
+    if name == "beach_256x256x96":
+        return wl.beach_256x256x96(seed=1)
+    if name == "beach_512x384x128":
+        return wl.beach_512x384x128()
+    if name == "beach_192x192x64":
+        return wl.beach_192x192x64()
+    if name == "tank_64x64x32":
+        return wl.tank_64x64x32()
+    if name.startswith("beach_"):
+        nx, ny, nz = (int(v) for v in name.split("_")[1].split("x"))
+        return wl.beach_case(nx, ny, nz, seed=1)
+    raise SystemExit(f"unknown workload {name}")
+
+
 def run_gpu(args, world, rank, local):
     import torch
     torch.cuda.set_device(local)
     pkg = ge.load_package()
     pkg.build()
-    case = pkg.workload.beach_256x256x96(seed=1)
+    case = workload_case(pkg, args.workload)
     dc, ds = pkg.prepare_dev(case)
     n = ds.mnoe
     solver = pkg.Solver(n)
     x = torch.zeros(ds.mm2, dtype=torch.float64, device="cuda")
     stream = torch.cuda.current_stream()
-    # warm-up (builds and caches the solve graph)
-    info = None
+
+    def plain_step():
+        x.zero_()                       # xe = 0 before every solve (1sub-momentum.F90:269)
+        return solver.solve(ds.alu, ds.llu, ds.de, ds.b, x, eps=case.eps0)
+
     for _ in range(args.warmup):
-        info = solver.solve(ds.alu, ds.llu, ds.de, ds.b, x, eps=case.eps0)
-    # ---- device-resident timing
+        plain_step()
+    # ---- device-resident timing (plain FP64: the headline value)
     clocks = Clocks(local)
+    clocks.start()
+    time.sleep(0.5)
     barrier(world)
     torch.cuda.synchronize()
-    clocks.start()
-    ev0 = torch.cuda.Event(enable_timing=True)
-    ev1 = torch.cuda.Event(enable_timing=True)
-    ev0.record(stream)
-    iters = []
-    for _ in range(args.steps):
-        info = solver.solve(ds.alu, ds.llu, ds.de, ds.b, x, eps=case.eps0)
-        iters.append(info.iter)
-    ev1.record(stream)
+    ms, infos = time_device(plain_step, args.steps, stream)
     torch.cuda.synchronize()
     barrier(world)
     clk = clocks.stop()
-    ms = ev0.elapsed_time(ev1)
     ms = max_over_ranks(ms, world)
+    info = infos[-1]
+    it = int(round(statistics.mean(i.iter for i in infos)))
     per_solve_s = ms / 1000.0 / args.steps
     value = world * args.steps / (ms / 1000.0)
-    it = int(round(statistics.mean(iters)))
     peak, peak_kind = measured_peaks()
     alg = bytes_solve_fp64(n, it)
     achieved = alg / per_solve_s / 1e9
+    x_plain = x[:n].cpu().numpy().copy()
 
-    # ---- end-to-end through the host-array drop-in (Fortran call shape)
+    legs = set(args.legs.split(","))
+    minfo = None
+    m_value = ms_m = m_alg = None
+    x_mixed = None
+    # ---- mixed precision on the same system (FP32 storage + FP64 refinement)
+    if "mixed" in legs:
+        m_value, ms_m, minfo, m_alg, x_mixed = run_mixed(pkg, args, ds, case, world, stream)
+    e2e_value = None
+    if "e2e" in legs:
+        e2e_value = run_e2e(pkg, args, ds, case, world)
+    h2d = n * 6 * 8 + n * 6 * 4 + 3 * n * 8
+    d2h = n * 8
+    _report(pkg, args, world, rank, case, n, ms, infos, info, it, value, alg, achieved, peak, peak_kind,
+            clk, x_plain, legs, m_value, ms_m, minfo, m_alg, x_mixed, e2e_value, h2d, d2h)
+
+
+def run_mixed(pkg, args, ds, case, world, stream):
+    import torch
+    n = ds.mnoe
+    msolver = pkg.MixedSolver(n)
+    xm = torch.zeros(ds.mm2, dtype=torch.float64, device="cuda")
+
+    def mixed_step():
+        xm.zero_()
+        return msolver.solve(ds.alu, ds.llu, ds.de, ds.b, xm, eps=case.eps0)
+
+    for _ in range(args.warmup):
+        mixed_step()
+    torch.cuda.synchronize()
+    ms_m, minfos = time_device(mixed_step, args.steps, stream)
+    ms_m = max_over_ranks(ms_m, world)
+    minfo = minfos[-1]
+    m_value = world * args.steps / (ms_m / 1000.0)
+    m_alg = bytes_solve_mixed(n, minfo.iter, minfo.outer)
+    x_mixed = xm[:n].cpu().numpy().copy()
+    return m_value, ms_m, minfo, m_alg, x_mixed
+
+
+def run_e2e(pkg, args, ds, case, world):
+    """Same solve through the host-array drop-in (Fortran call shape)."""
+    import torch
+    n = ds.mnoe
     al = ds.alu.cpu().numpy()
     ll = ds.llu.cpu().numpy()
     de = ds.de.cpu().numpy()
@@ -213,7 +285,6 @@ def run_gpu(args, world, rank, local):
         xh[:] = 0.0
         pkg.pcgpme(al, ll, de, b, xh, n, eps=case.eps0)
     barrier(world)
-    torch.cuda.synchronize()
     e2e_times = []
     for _ in range(args.steps):
         xh[:] = 0.0
@@ -222,41 +293,55 @@ def run_gpu(args, world, rank, local):
         e2e_times.append(time.perf_counter() - t0)
     barrier(world)
     e2e_s = max_over_ranks(sum(e2e_times), world)
-    e2e_value = world * args.steps / e2e_s
-    h2d = n * 6 * 8 + n * 6 * 4 + 3 * n * 8
-    d2h = n * 8
+    return world * args.steps / e2e_s
 
+
+def _report(pkg, args, world, rank, case, n, ms, infos, info, it, value, alg, achieved, peak, peak_kind,
+            clk, x_plain, legs, m_value, ms_m, minfo, m_alg, x_mixed, e2e_value, h2d, d2h):
     # ---- CPU baseline: the oracle on the host cores (rank 0, N=1 only)
     cpu = None
-    if rank == 0 and world == 1 and not args.no_cpu:
+    err_plain = err_mixed = None
+    if rank == 0 and world == 1 and not args.no_cpu and "cpu" in legs:
         ora = ge.load_oracle()
         ora.build()
         cls, sm, sy = ora.prepare(case)
         threads = os.cpu_count() or 1
         t, r = cpu_reference_solve(ora, sy, case.eps0, threads)
         cpu = {"value": 1.0 / t, "unit": "solves/s", "cores": threads, "kind": "port",
-               "sample": f"one full solve of {WORKLOAD} (N={sy.mnoe}, {r.iters} iterations), OpenMP "
+               "sample": f"one full solve of {args.workload} (N={sy.mnoe}, {r.iters} iterations), OpenMP "
                          f"restatement of pcgpme_para.F90 on {threads} threads"}
+        nrm = np.linalg.norm(r.x)
+        err_plain = float(np.linalg.norm(x_plain - r.x) / nrm)
+        if x_mixed is not None:
+            err_mixed = float(np.linalg.norm(x_mixed - r.x) / nrm)
 
     if rank == 0:
+        launches_per_solve = 17 + 16 * it
         line = {
             "metric": "pressure solves/s", "value": value, "unit": "solves/s", "n_gpus": world,
             "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms / args.steps,
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
             "data": "synthetic (seeded generator)",
-            "config": {"workload": WORKLOAD, "rows": n, "tol": case.eps0, "iters": it,
+            "config": {"workload": args.workload, "rows": n, "tol": case.eps0, "iters": it,
                        "stop": pkg.STOP_NAMES.get(info.reason), "eps": info.eps,
+                       "rel_l2_vs_oracle": err_plain,
                        "l2": "inputs larger than L2 (matrix %.0f MB)" % (n * 80 / 1e6),
                        "path": "plain FP64", "parallelism": f"replicas x{world}"},
-            "roofline": {"bound": "hbm", "kernel": "pcgpme solve (one graph launch)",
+            "roofline": {"bound": "hbm", "kernel": "pcgpme FP64 solve (one graph launch)",
                          "achieved": achieved, "peak": peak, "peak_kind": peak_kind, "unit": "GB/s",
                          "frac": achieved / peak, "traffic": None,
                          "algorithmic_bytes_per_solve": alg},
             "e2e": {"value": e2e_value, "unit": "solves/s", "h2d_bytes_per_step": h2d,
                     "d2h_bytes_per_step": d2h},
-            "gpu_launches": args.steps * (3 + 17 + 16 * it),
+            "gpu_launches": args.steps * launches_per_solve,
             "clocks": clk,
         }
+        if minfo is not None:
+            line["mixed"] = {"value": m_value, "unit": "solves/s", "speedup_vs_fp64": m_value / value,
+                             "inner_iters": minfo.iter, "outer": minfo.outer, "eps": minfo.eps,
+                             "rel_l2_vs_oracle": err_mixed, "ms_per_solve": ms_m / args.steps,
+                             "achieved_gbs": m_alg / (ms_m / 1000.0 / args.steps) / 1e9,
+                             "algorithmic_bytes_per_solve": m_alg}
         if cpu:
             line["cpu_baseline"] = cpu
         print(json.dumps(line), flush=True)
@@ -269,6 +354,11 @@ def main():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="gpu", choices=["gpu", "reference"])
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline leg")
+    ap.add_argument("--legs", default="plain,mixed,e2e,cpu",
+                    help="measurement legs to run (the plain FP64 leg always runs)")
+    ap.add_argument("--workload", default=WORKLOAD,
+                    help="beach_256x256x96 (default), beach_512x384x128, beach_192x192x64, "
+                         "tank_64x64x32 or beach_NXxNYxNZ")
     args = ap.parse_args()
     world, rank, local = dist_init()
     if args.impl == "reference":

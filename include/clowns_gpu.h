@@ -115,21 +115,67 @@ int clowns_pcgpme_dev(const double* al, int nl, int na, const int* ll, const dou
                       const double* b, double* x, double eps, double parm, int iter,
                       void* work, size_t work_bytes, void* stream, clowns_solve_info* info);
 
-/* Test hooks of the solve's building blocks (device pointers, workspace laid out
- * as for clowns_pcgpme_dev).  clowns_pcgpme_setup_dev performs only the scaling
- * and per-row sort of pcgpme_para.F90:77-112 and copies the scaled, sorted
- * matrix out: al_s/ll_s (na_out, nl) column-major, 0-based ll_s with every empty
- * slot pointing at row n (a zero pad row); d_s, b_s length n. */
+/* ========================================================================== */
+/* Mixed precision and batched ensembles (no reference counterpart: new       */
+/* capabilities of the same PCGPME method)                                    */
+/* ========================================================================== */
+
+/* Precision selectors */
+#define CLOWNS_PREC_FP64 0   /* plain FP64, the reference's arithmetic and stop tests  */
+#define CLOWNS_PREC_MIXED 1  /* FP32 coefficients/Krylov vectors + FP64 refinement     */
+
+/* Mixed-precision solve of the same system as clowns_pcgpme_dev.  The row scaling
+ * and per-row sort are computed in FP64 exactly as the reference does; the scaled,
+ * sorted coefficients and the Krylov vectors of an inner BiCGSTAB are stored in
+ * FP32.  An FP64 outer loop forms r = W (b - A x) from the caller's original FP64
+ * matrix, measures ERR = ||PM r|| / ||PM W b|| (the reference's EPS definition)
+ * in FP64, solves PM W A d = PM r / ||PM r|| in FP32 to inner_tol (<= 0: 1e-4),
+ * and accumulates x += ||PM r|| d in FP64, until ERR <= eps.  info->iter counts
+ * inner iterations, info->outer the refinement sweeps; IER = 3000 after
+ * max_outer sweeps (<= 0: 30).  inner_max <= 0: 2000. */
+size_t clowns_pcgpme_mixed_workspace_bytes(int n, int nl);
+int clowns_pcgpme_mixed_dev(const double* al, int nl, int na, const int* ll, const double* d, int n,
+                            const double* b, double* x, double eps, double parm, double inner_tol,
+                            int inner_max, int max_outer, void* work, size_t work_bytes,
+                            void* stream, clowns_solve_info* info);
+
+/* One independent system of an ensemble (device pointers, layouts as for
+ * clowns_pcgpme_dev).  x: initial guess in, solution out. */
+typedef struct clowns_member {
+    const double* al;
+    const int* ll;
+    const double* d;
+    const double* b;
+    double* x;
+    int na, n, nl, pad;
+} clowns_member;
+
+/* Batched ensemble: m independent systems of different sizes solved together in
+ * one CUDA-graph launch per solve (FP64) or per refinement sweep (mixed).  Rows of
+ * all members share one tile-aligned row space; every kernel serves all members
+ * and skips members whose stop test fired (per-member convergence masks);
+ * dot products reduce per member.  members: HOST array of m descriptors;
+ * infos: HOST array of m results.  Each member gets exactly the single-system
+ * semantics of its precision. */
+size_t clowns_pcgpme_batched_workspace_bytes(int m, const int* n, int precision);
+int clowns_pcgpme_batched_dev(int m, const clowns_member* members, int precision, double eps,
+                              double parm, int iter, double inner_tol, int inner_max, int max_outer,
+                              void* work, size_t work_bytes, void* stream, clowns_solve_info* infos);
+
+/* Test hooks of the solve's building blocks (device pointers; workspace sized by
+ * clowns_pcgpme_workspace_bytes(n, nl)).  clowns_pcgpme_setup_dev performs only
+ * the row scaling and per-row sort of pcgpme_para.F90:77-112 and copies the
+ * scaled, sorted matrix out: al_s/ll_s (na_out, nl) column-major, 0-based ll_s
+ * with every empty slot pointing at row n (a zero pad row); d_s, b_s length n. */
 int clowns_pcgpme_setup_dev(const double* al, int nl, int na, const int* ll, const double* d,
                             int n, const double* b, double parm, double* al_s, int* ll_s,
                             double* d_s, double* b_s, int na_out, void* work,
                             size_t work_bytes, void* stream);
-/* y = PM * A * x with a scaled/sorted matrix as produced above (AXSUB then
- * LDUSUB, pcgpme_para.F90:263-352).  x, y: device, length n. */
-int clowns_apply_pm_a_dev(const double* al_s, const int* ll_s, const double* d_s, int nl,
-                          int na_s, int n, const double* x, double* y, void* work,
-                          size_t work_bytes, void* stream);
-
+/* y = PM * (W A) * x: the scaled/sorted operator of the setup above applied with
+ * AXSUB then LDUSUB (pcgpme_para.F90:263-352).  x, y: device, length n. */
+int clowns_apply_pm_a_dev(const double* al, int nl, int na, const int* ll, const double* d, int n,
+                          double parm, const double* x, double* y, void* work, size_t work_bytes,
+                          void* stream);
 
 /* ========================================================================== */
 /* Classification, static coefficients, rows, right-hand side, assembly       */
@@ -191,6 +237,32 @@ int clowns_correct_dev(const int* dims, int inne, int mx2, const int* mn, const 
                        const double* a, const double* dx, double dt, int mnoe,
                        const int* mno2mn, const int* mno, const double* xe0, double* p,
                        double* un, void* stream);
+
+/* ========================================================================== */
+/* Discrete adjoint (no reference counterpart)                                */
+/* ========================================================================== */
+
+/* Explicit transpose of an assembled ELL matrix: row i of (alt, llt, det) holds
+ * column i of A; the coefficient of row j toward its neighbour i in direction d
+ * lands in row i at the opposite direction slot (x- <-> x+, ...).  n rows,
+ * leading dimension na, 1-based llu (0 = none).  *bad (device int) is set if an
+ * index lies outside 1..n.  The adjoint solve then runs clowns_pcgpme_dev (or
+ * the mixed / batched variants) on (alt, llt, det): the reference's PCGPME
+ * method applied to A^T, with its own row scaling and sort. */
+int clowns_transpose_dev(int n, int na, const double* alu, const int* llu, const double* de,
+                         double* alt, int* llt, double* det, int* bad, void* stream);
+
+/* Face-coefficient gradient dJ/da(l, owner) = -lambda^T (dA/da) x for the face
+ * area fractions a(0:2, 0:inne2+1) that enter A through ALU_C
+ * (1sub-matrix.F90:49-61): x solves A x = b, lambda solves A^T lambda = dJ/dx.
+ * Faces of surface rows (whose coefficients do not depend on a) and faces
+ * cancelled by the Neumann fix (1sub-momentum.F90:502-509) get zero.  grad has
+ * the layout of a and is overwritten.  The right-hand side is an independent
+ * input; its gradient is lambda itself. */
+int clowns_face_grad_dev(const int* dims, int inne, int inne2, int ifln, const int* fln,
+                         const int* in_, const int* jn, const int* kn, const int* nf,
+                         const int* mno, const double* alu_c, const int* ll_c, const double* a,
+                         const double* x, const double* lambda, double* grad, void* stream);
 
 #ifdef __cplusplus
 }

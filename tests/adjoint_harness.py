@@ -1,0 +1,91 @@
+"""Check harness for the discrete adjoint: a torch.autograd.Function whose
+forward assembles the pressure matrix from the face area fractions ``a`` and
+solves it on the GPU, and whose backward runs the adjoint solve on the explicit
+transpose plus the face-gradient kernel.  Used only by the tests."""
+import numpy as np
+import torch
+
+import __graft_entry__ as ge
+
+pkg = ge.load_package()
+
+
+class PressureSystem:
+    """Classification fixed, matrix rebuilt from ``a`` on every forward."""
+
+    def __init__(self, case):
+        self.case = case
+        self.dc, self.sy = pkg.prepare_dev(case)
+        self.n = self.sy.mnoe
+        self.b0 = self.sy.b.clone()          # right-hand side held fixed (independent input)
+        self.solver = pkg.Solver(self.n)
+
+    def assemble(self, a_dev):
+        """init_matrix + cal_matrix_element for face fractions a_dev (inne2+2, 3)."""
+        self.dc.a.copy_(a_dev)
+        mp, alu_c, ll_c, de_c = pkg.init_matrix_dev(self.dc)
+        r = pkg.rows_rhs_assemble_dev(self.dc, self.sy.fln, self.sy.ifln, mp, alu_c, ll_c, de_c, mm2=self.sy.mm2)
+        self.sy.alu, self.sy.llu, self.sy.de = r["alu"], r["llu"], r["de"]
+        self.sy.alu_c, self.sy.ll_c = alu_c, ll_c
+        self.sy.mno = r["mno"]
+        return self.sy
+
+    def solve(self, b, x0=None, eps=1e-13):
+        x = torch.zeros(self.sy.mm2, dtype=torch.float64, device="cuda")
+        if x0 is not None:
+            x[:self.n] = x0[:self.n]
+        info = self.solver.solve(self.sy.alu, self.sy.llu, self.sy.de, b, x, eps=eps)
+        return x[:self.n].clone(), info
+
+
+class PressureSolve(torch.autograd.Function):
+    @staticmethod
+    def forward(ctx, a, b, system: PressureSystem):
+        system.assemble(a.detach())
+        bb = torch.zeros(system.sy.mm2, dtype=torch.float64, device="cuda")
+        bb[:system.n] = b.detach()
+        x, info = system.solve(bb)
+        ctx.system = system
+        ctx.save_for_backward(x)
+        return x
+
+    @staticmethod
+    def backward(ctx, gx):
+        system = ctx.system
+        (x,) = ctx.saved_tensors
+        lam, grad_a, info = pkg.adjoint_dev(system.dc, system.sy, x, gx.contiguous(), eps=1e-13,
+                                            solver=system.solver)
+        return grad_a, lam, None
+
+
+def gauges(n, count=16, seed=4):
+    rng = np.random.default_rng(seed)
+    rows = rng.choice(n, size=count, replace=False)
+    w = rng.uniform(0.5, 1.5, size=count)
+    return rows, w
+
+
+def fd_faces(system: PressureSystem, count=200, seed=5):
+    """Seeded faces (l, owner) whose coefficient enters a fluid row of A."""
+    sy = system.sy
+    dc = system.dc
+    rng = np.random.default_rng(seed)
+    nf = dc.nf.cpu().numpy()
+    a = dc.a.cpu().numpy()
+    ll_c = sy.ll_c.cpu().numpy()
+    mno2mn = sy.mno2mn.cpu().numpy()[:system.n]
+    cand = []
+    for c in mno2mn[rng.permutation(len(mno2mn))[:20 * count]]:
+        if nf[c] != 1:
+            continue
+        for ll in range(6):
+            lc = ll_c[ll, c - 1]
+            if lc == 0:
+                continue
+            owner = lc if ll % 2 else c
+            l = ll // 2
+            if a[owner, l] > 0 and nf[lc] == 1:
+                cand.append((int(owner), l))
+        if len(set(cand)) >= count:
+            break
+    return sorted(set(cand))[:count]

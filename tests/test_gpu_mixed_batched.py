@@ -1,0 +1,112 @@
+"""Mixed precision (FP32 storage + FP64 refinement) and batched ensembles.
+
+Tolerances: the mixed path must reach the reference's ERR <= 1e-10 (measured in
+FP64) and give a pressure within 1e-9 relative L2 of the FP64 oracle; a batched
+member must match its single-system solve within 1e-10 relative L2 when both
+solve to 1e-13."""
+import numpy as np
+import pytest
+
+from cases import small_cases
+
+pytestmark = pytest.mark.gpu
+
+CASES = small_cases()
+
+
+@pytest.fixture(scope="module")
+def systems(gpu, ora):
+    import torch
+    out = []
+    for label, case in CASES:
+        cls, sm, sy = ora.prepare(case)
+        dc, ds = gpu.prepare_dev(case)
+        torch.cuda.synchronize()
+        out.append((label, case, sy, ds))
+    return out
+
+
+def _x(ds):
+    import torch
+    return torch.zeros(ds.mm2, dtype=torch.float64, device="cuda")
+
+
+@pytest.mark.parametrize("idx", range(len(CASES)), ids=[c[0] for c in CASES])
+def test_mixed_matches_fp64_oracle(gpu, ora, systems, idx):
+    label, case, sy, ds = systems[idx]
+    n = sy.mnoe
+    ref = ora.pcgpme(sy.alu, sy.llu, sy.de[1:], sy.b[1:], n, eps=1e-13)
+    solver = gpu.MixedSolver(n)
+    for eps, bound in ((1e-10, 100 * 1e-10), (1e-12, 1e-9)):
+        # at ERR <= 1e-10 the pressure error is the system's conditioning times
+        # 1e-10 (the plain FP64 path carries the same); 1e-9 holds from 1e-12 on
+        x = _x(ds)
+        info = solver.solve(ds.alu, ds.llu, ds.de, ds.b, x, eps=eps)
+        xg = x.cpu().numpy()[:n]
+        rel = np.linalg.norm(xg - ref.x) / np.linalg.norm(ref.x)
+        assert info.ier == 0 and info.eps <= eps, info.as_dict()
+        assert info.outer >= 1
+        assert rel <= bound, (label, eps, rel, info.as_dict())
+
+
+def test_mixed_true_residual(gpu, ora, systems):
+    """Unpreconditioned true residual of the mixed solution is at the FP64 level."""
+    label, case, sy, ds = systems[1]
+    n = sy.mnoe
+    x = _x(ds)
+    gpu.MixedSolver(n).solve(ds.alu, ds.llu, ds.de, ds.b, x, eps=1e-12)
+    A = ora.to_csr(sy)
+    b = sy.b[1:n + 1]
+    xg = x.cpu().numpy()[:n]
+    assert np.linalg.norm(b - A @ xg) <= 1e-10 * np.linalg.norm(b)
+
+
+def test_batched_fp64_matches_single(gpu, systems):
+    import torch
+    sys_list = [(ds.alu, ds.llu, ds.de, ds.b) for (_, _, _, ds) in systems]
+    sizes = [ds.mnoe for (_, _, _, ds) in systems]
+    xs = [_x(ds) for (_, _, _, ds) in systems]
+    infos = gpu.BatchedSolver(sizes, gpu.PREC_FP64).solve(sys_list, xs, eps=1e-13)
+    for (label, case, sy, ds), x, info in zip(systems, xs, infos):
+        xs1 = _x(ds)
+        i1 = gpu.Solver(ds.mnoe).solve(ds.alu, ds.llu, ds.de, ds.b, xs1, eps=1e-13)
+        a = x.cpu().numpy()[:ds.mnoe]
+        b = xs1.cpu().numpy()[:ds.mnoe]
+        assert info.ier == 0 and i1.ier == 0
+        assert np.linalg.norm(a - b) <= 1e-10 * np.linalg.norm(b), label
+        assert abs(info.iter - i1.iter) <= max(5, i1.iter // 4)
+    torch.cuda.synchronize()
+
+
+def test_batched_mixed_converges_per_member(gpu, ora, systems):
+    sys_list = [(ds.alu, ds.llu, ds.de, ds.b) for (_, _, _, ds) in systems]
+    sizes = [ds.mnoe for (_, _, _, ds) in systems]
+    xs = [_x(ds) for (_, _, _, ds) in systems]
+    infos = gpu.BatchedSolver(sizes, gpu.PREC_MIXED).solve(sys_list, xs, eps=1e-12)
+    for (label, case, sy, ds), x, info in zip(systems, xs, infos):
+        n = sy.mnoe
+        ref = ora.pcgpme(sy.alu, sy.llu, sy.de[1:], sy.b[1:], n, eps=1e-13)
+        xg = x.cpu().numpy()[:n]
+        assert info.ier == 0 and info.eps <= 1e-12, (label, info.as_dict())
+        assert np.linalg.norm(xg - ref.x) <= 1e-9 * np.linalg.norm(ref.x), label
+
+
+def test_batched_member_fault_is_isolated(gpu, systems):
+    """A NaN right-hand side (injected on the host) stops only its own member."""
+    import torch
+    sys_list = []
+    for k, (_, _, _, ds) in enumerate(systems):
+        b = ds.b.clone()
+        if k == 2:
+            b[ds.mnoe // 3] = float("nan")
+        sys_list.append((ds.alu, ds.llu, ds.de, b))
+    sizes = [ds.mnoe for (_, _, _, ds) in systems]
+    for prec in (gpu.PREC_FP64, gpu.PREC_MIXED):
+        xs = [_x(ds) for (_, _, _, ds) in systems]
+        infos = gpu.BatchedSolver(sizes, prec).solve(sys_list, xs, eps=1e-10)
+        for k, info in enumerate(infos):
+            if k == 2:
+                assert info.ier == gpu.IER_NONFINITE, info.as_dict()
+            else:
+                assert info.ier == 0 and info.eps <= 1e-10, (k, info.as_dict())
+    torch.cuda.synchronize()
