@@ -90,6 +90,9 @@ _SIGS = {
                             + [C.c_size_t, C.c_void_p]),
     "clowns_assemble_dev": (C.c_int, [C.c_void_p, C.c_int, C.c_int, C.c_int] + [C.c_void_p] * 8
                             + [C.c_int] + [C.c_void_p] * 5 + [C.c_int] + [C.c_void_p] * 5),
+    "clowns_pcgpme_static_dev": (C.c_int, [C.c_void_p, C.c_int, C.c_int, C.c_void_p, C.c_void_p, C.c_int,
+                                           C.c_void_p, C.c_void_p, C.c_double, C.c_double, C.c_int,
+                                           C.c_void_p, C.c_void_p]),
     "clowns_transpose_dev": (C.c_int, [C.c_int, C.c_int] + [C.c_void_p] * 8),
     "clowns_face_grad_dev": (C.c_int, [C.c_void_p, C.c_int, C.c_int, C.c_int] + [C.c_void_p] * 13),
     "clowns_correct_dev": (C.c_int, [C.c_void_p, C.c_int, C.c_int] + [C.c_void_p] * 8

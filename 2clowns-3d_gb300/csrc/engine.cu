@@ -761,3 +761,145 @@ int engine_apply_pm_a(const MemberIn& in, double parm, const double* x, double* 
 }
 
 }  // namespace clowns
+
+// ---------------------------------------------------------------------------
+// Allocation-free FP64 solve.
+//
+// For callers that cannot allocate device memory: a Fortran time loop whose
+// device memory is owned by another runtime or a fixed memory budget, or a
+// library that must not grow the process's allocations while a solve runs.
+// The scratch space of the solve lives in one file-scope device array of fixed
+// size, loaded with the library; the entry point itself calls no allocator and
+// builds no CUDA graph -- it launches the same kernels as clowns_pcgpme_dev and
+// polls the device stop flag every eight iterations.  The array is shared by
+// every call on a device: calls that overlap on the GPU (different streams or
+// host threads) race on it.  Every call re-initialises all scratch it reads.
+
+namespace clowns {
+
+constexpr int kStaticMaxRows = CLOWNS_STATIC_MAX_ROWS;
+constexpr long kStaticNV = ((long)(kStaticMaxRows + 1) + kTile - 1) / kTile * kTile;
+constexpr int kStaticMaxBlk = (int)(kStaticNV / kTile);
+// matrix (6 T + 6 int + 1 T) + 8 Krylov vectors, plus tables and alignment slack
+constexpr size_t kStaticBytes = (size_t)kStaticNV * (6 * 8 + 6 * 4 + 8 + 8 * 8) + 64 * 1024;
+constexpr int kStaticMaxDevices = 64;
+
+static __device__ __align__(256) unsigned char g_static_scratch[kStaticBytes];
+static void* g_static_addr[kStaticMaxDevices];
+static std::mutex g_static_mu;
+
+// Device address of the scratch array for the current device, resolved once
+// per device on the first call (the host-side name is only a stand-in).
+static int static_scratch(void** out) {
+    int dev = 0;
+    CLOWNS_CUDA_TRY(cudaGetDevice(&dev));
+    if (dev < 0 || dev >= kStaticMaxDevices) {
+        set_last_error_msg("pcgpme_static: device ordinal beyond the supported 64");
+        return CLOWNS_ERR_LIMIT;
+    }
+    std::lock_guard<std::mutex> lk(g_static_mu);
+    if (!g_static_addr[dev]) {
+        void* p = nullptr;
+        cudaError_t e = cudaGetSymbolAddress(&p, g_static_scratch);
+        if (e != cudaSuccess || !p) {
+            set_last_error(e, "cudaGetSymbolAddress(g_static_scratch)", __FILE__, __LINE__);
+            return CLOWNS_ERR_CUDA;
+        }
+        g_static_addr[dev] = p;
+    }
+    *out = g_static_addr[dev];
+    return CLOWNS_OK;
+}
+
+// Member tables of a single system from stack arrays (no allocation).
+static int static_upload_tables(void* work, const EngLayout& L, int n, const MemberIn& in, cudaStream_t s) {
+    int blk_member[kStaticMaxBlk], blk_rows[kStaticMaxBlk];
+    for (int b = 0; b < L.nblk; b++) {
+        blk_member[b] = 0;
+        long rows = (long)n - (long)b * kTile;
+        blk_rows[b] = (int)std::max(0L, std::min((long)kTile, rows));
+    }
+    const int off = 0, nblk = (n + kTile - 1) / kTile, blk0 = 0;
+    const unsigned zero = 0u;
+    char* b = (char*)work;
+    CLOWNS_CUDA_TRY(cudaMemcpyAsync(b + L.o_blk_member, blk_member, sizeof(int) * L.nblk, cudaMemcpyHostToDevice, s));
+    CLOWNS_CUDA_TRY(cudaMemcpyAsync(b + L.o_blk_rows, blk_rows, sizeof(int) * L.nblk, cudaMemcpyHostToDevice, s));
+    CLOWNS_CUDA_TRY(cudaMemcpyAsync(b + L.o_mem_off, &off, sizeof(int), cudaMemcpyHostToDevice, s));
+    CLOWNS_CUDA_TRY(cudaMemcpyAsync(b + L.o_mem_n, &n, sizeof(int), cudaMemcpyHostToDevice, s));
+    CLOWNS_CUDA_TRY(cudaMemcpyAsync(b + L.o_mem_nblk, &nblk, sizeof(int), cudaMemcpyHostToDevice, s));
+    CLOWNS_CUDA_TRY(cudaMemcpyAsync(b + L.o_mem_blk0, &blk0, sizeof(int), cudaMemcpyHostToDevice, s));
+    CLOWNS_CUDA_TRY(cudaMemcpyAsync(b + L.o_ticket, &zero, sizeof(unsigned), cudaMemcpyHostToDevice, s));
+    CLOWNS_CUDA_TRY(cudaMemcpyAsync(b + L.o_in, &in, sizeof(MemberIn), cudaMemcpyHostToDevice, s));
+    CLOWNS_CUDA_TRY(cudaStreamSynchronize(s));   // stack sources must outlive the copies
+    return CLOWNS_OK;
+}
+
+}  // namespace clowns
+
+extern "C" int clowns_pcgpme_static_dev(const double* al, int nl, int na, const int* ll, const double* d, int n,
+                                        const double* b, double* x, double eps, double parm, int iter, void* stream,
+                                        clowns_solve_info* info) {
+    using namespace clowns;
+    if (n > kStaticMaxRows) {
+        set_last_error_msg("pcgpme_static: n exceeds CLOWNS_STATIC_MAX_ROWS (32768 rows)");
+        return CLOWNS_ERR_LIMIT;
+    }
+    if (!al || !ll || !d || !b || !x || n < 1 || na < n || (nl != 6 && nl != 4)) {
+        set_last_error_msg("pcgpme_static: invalid arguments");
+        return CLOWNS_ERR_ARG;
+    }
+    cudaStream_t s = (cudaStream_t)stream;
+    void* work = nullptr;
+    int rc = static_scratch(&work);
+    if (rc) return rc;
+    EngLayout L = eng_layout(1, &n, 0);
+    if (L.total > kStaticBytes || L.nblk > kStaticMaxBlk) {
+        set_last_error_msg("pcgpme_static: layout exceeds the static scratch");
+        return CLOWNS_ERR_LIMIT;
+    }
+    MemberIn in;
+    in.al = al; in.ll = ll; in.d = d; in.b = b; in.x = x;
+    in.na = na; in.n = n; in.nl = nl; in.pad = 0;
+    double eps_r, P1, P2;
+    int iter_r;
+    params(n, eps, parm, iter, &eps_r, &iter_r, &P1, &P2);
+    std::lock_guard<std::mutex> lk(g_static_mu);
+    rc = static_upload_tables(work, L, n, in, s);
+    if (rc) return rc;
+    Eng<double> E = eng_bind<double>(work, L);
+    const Shape sh;                                 // one 256-thread block per tile
+    const int g = grid_of(sh, E.nblk);
+    k_eng_init_scalars<<<1, 256, 0, s>>>(E.S, 1, eps_r, iter_r, 0, E.ctrl);
+    if (nl == 6) k_eng_setup<double, 6><<<4 * L.nblk, kEngBlock, 0, s>>>(E, P1, P2, 0);
+    else k_eng_setup<double, 4><<<4 * L.nblk, kEngBlock, 0, s>>>(E, P1, P2, 0);
+    launch_ldusub_inplace(E, sh, E.p, E.t, E.q, s);       // b^ = PM W b
+    launch_apply(E, sh, E.xi, E.q, E.t, 0, s);             // q = PM A x0
+    k_eng_initres<double><<<g, sh.block, 0, s>>>(E);
+    CLOWNS_CUDA_TRY(cudaGetLastError());
+    // Iterations: kernels of a stopped member return at once, so batches of
+    // eight between polls are exact; the stop tests cap the count at ITER.
+    int done = 0;
+    for (long launched = 0; !done; launched += 8) {
+        for (int k = 0; k < 8; k++) launch_iteration(E, sh, s);
+        CLOWNS_CUDA_TRY(cudaGetLastError());
+        CLOWNS_CUDA_TRY(cudaMemcpyAsync(&done, &E.S->done, sizeof(int), cudaMemcpyDeviceToHost, s));
+        CLOWNS_CUDA_TRY(cudaStreamSynchronize(s));
+        if (!done && launched > (long)iter_r + 16) {
+            set_last_error_msg("pcgpme_static: stop flag not raised after ITER iterations");
+            return CLOWNS_ERR_NOCONV;
+        }
+    }
+    k_eng_copy_out<double><<<4 * L.nblk, kEngBlock, 0, s>>>(E);
+    MemberScalars h;
+    CLOWNS_CUDA_TRY(cudaMemcpyAsync(&h, E.S, sizeof(MemberScalars), cudaMemcpyDeviceToHost, s));
+    CLOWNS_CUDA_TRY(cudaStreamSynchronize(s));
+    if (info) {
+        info->eps = h.ERR;
+        info->bn = h.BN;
+        info->iter = h.K;
+        info->ier = h.bad_index ? CLOWNS_IER_ARG : h.ier;
+        info->reason = h.reason;
+        info->outer = 0;
+    }
+    return CLOWNS_OK;
+}

@@ -264,6 +264,29 @@ int clowns_face_grad_dev(const int* dims, int inne, int inne2, int ifln, const i
                          const int* mno, const double* alu_c, const int* ll_c, const double* a,
                          const double* x, const double* lambda, double* grad, void* stream);
 
+/* ========================================================================== */
+/* Allocation-free FP64 solve (no counterpart in the reference)               */
+/* ========================================================================== */
+
+/* Largest system the allocation-free solve accepts. */
+#define CLOWNS_STATIC_MAX_ROWS 32768
+
+/* The FP64 solve of clowns_pcgpme_dev for callers that cannot allocate device
+ * memory -- a host model whose device memory belongs to another runtime or to
+ * a fixed budget, which therefore can neither cudaMalloc a workspace nor hand
+ * one over.  Inputs and outputs are the caller's device arrays as for
+ * clowns_pcgpme_dev; all scratch space lives in one static device array of
+ * about 5 MB that every GPU loading the library holds until the process exits.
+ * The call allocates nothing (no cudaMalloc/cudaFree, no allocating library
+ * routine) and returns CLOWNS_ERR_LIMIT for n > CLOWNS_STATIC_MAX_ROWS.  The
+ * first call on a device looks up the array's device address (once per device,
+ * with that device current); make that first call before any stream capture.
+ * Every call shares the array and re-initialises what it reads, so calls that
+ * overlap on the GPU (other streams or host threads) race on it. */
+int clowns_pcgpme_static_dev(const double* al, int nl, int na, const int* ll, const double* d,
+                             int n, const double* b, double* x, double eps, double parm, int iter,
+                             void* stream, clowns_solve_info* info);
+
 #ifdef __cplusplus
 }
 #endif
