@@ -235,6 +235,8 @@ def run_gpu(args, world, rank, local):
     x_plain = x[:n].cpu().numpy().copy()
 
     legs = set(args.legs.split(","))
+    if "apply" in legs:
+        run_apply_profile(pkg, args, ds, stream)
     minfo = None
     m_value = ms_m = m_alg = None
     x_mixed = None
@@ -248,6 +250,18 @@ def run_gpu(args, world, rank, local):
     d2h = n * 8
     _report(pkg, args, world, rank, case, n, ms, infos, info, it, value, alg, achieved, peak, peak_kind,
             clk, x_plain, legs, m_value, ms_m, minfo, m_alg, x_mixed, e2e_value, h2d, d2h)
+
+
+def run_apply_profile(pkg, args, ds, stream):
+    """Operator application y = PM (W A) x through the test hook (row scaling,
+    sort, AXSUB and the five LDUSUB sweeps as plain launches, so that a profiler
+    can attribute them kernel by kernel)."""
+    import torch
+    n = ds.mnoe
+    xv = torch.ones(n, dtype=torch.float64, device="cuda")
+    for _ in range(max(1, args.steps)):
+        pkg.apply_pm_a_dev(ds.alu, ds.llu, ds.de, n, xv)
+    torch.cuda.synchronize()
 
 
 def run_mixed(pkg, args, ds, case, world, stream):

@@ -37,6 +37,18 @@ class PressureSystem:
         info = self.solver.solve(self.sy.alu, self.sy.llu, self.sy.de, b, x, eps=eps)
         return x[:self.n].clone(), info
 
+    def solve_refined(self, b, x0):
+        """Warm-started solve driven to the FP64 floor by iterative refinement on
+        the true residual (used for finite differences: the perturbation of x is
+        resolved to ~1e-10 of itself, which a tolerance-stopped solve does not)."""
+        if not hasattr(self, "msolver"):
+            self.msolver = pkg.MixedSolver(self.n)
+        x = torch.zeros(self.sy.mm2, dtype=torch.float64, device="cuda")
+        x[:self.n] = x0[:self.n]
+        info = self.msolver.solve(self.sy.alu, self.sy.llu, self.sy.de, b, x, eps=2e-15, inner_tol=1e-5,
+                                  max_outer=12)
+        return x[:self.n].clone(), info
+
 
 class PressureSolve(torch.autograd.Function):
     @staticmethod

@@ -101,8 +101,8 @@ def test_adjoint_matches_cpu_transposed_solve(gpu, ora, bore):
 def test_adjoint_matches_finite_differences(gpu, bore):
     """Central differences with relative step 1e-6 on 40 seeded face fractions,
     through the autograd wrapper.  The perturbed solves start from the
-    unperturbed pressure and stop at ERR <= 1e-14 (a tolerance <= 1e-15 would
-    be replaced by 1e-9 under the reference's rule, pcgpme_para.F90:51)."""
+    unperturbed pressure and are refined on the true FP64 residual down to the
+    FP64 floor; J(+) - J(-) is formed as w.(x+ - x-) to avoid cancellation."""
     import torch
     from adjoint_harness import PressureSolve, PressureSystem, fd_faces, gauges
     system = PressureSystem(bore)
@@ -123,14 +123,14 @@ def test_adjoint_matches_finite_differences(gpu, bore):
     fd, ad = [], []
     for owner, l in faces:
         h = 1e-6 * float(a0[owner, l])
-        vals = []
+        xs = []
         for sgn in (1.0, -1.0):
             ap = a0.clone()
             ap[owner, l] += sgn * h
             system.assemble(ap)
-            xs, info = system.solve(system.b0, x0=x0, eps=1e-14)
-            vals.append(float((wt * xs).sum()))
-        fd.append((vals[0] - vals[1]) / (2 * h))
+            xsol, info = system.solve_refined(system.b0, x0)
+            xs.append(xsol)
+        fd.append(float((wt * (xs[0] - xs[1])).sum()) / (2 * h))
         ad.append(ga[owner, l])
     fd, ad = np.array(fd), np.array(ad)
     assert np.linalg.norm(ad - fd) <= 1e-6 * np.linalg.norm(fd), (np.abs(ad - fd) / np.abs(fd)).max()
@@ -143,8 +143,8 @@ def test_adjoint_matches_finite_differences(gpu, bore):
     bp[:n] += hb * v
     bm = system.b0.clone()
     bm[:n] -= hb * v
-    xp, _ = system.solve(bp, x0=x0, eps=1e-14)
-    xm, _ = system.solve(bm, x0=x0, eps=1e-14)
+    xp, _ = system.solve_refined(bp, x0)
+    xm, _ = system.solve_refined(bm, x0)
     fdb = float((wt * (xp - xm)).sum()) / (2 * hb)
     adb = float((b.grad * v).sum())
     assert abs(fdb - adb) <= 1e-6 * abs(adb)
