@@ -93,6 +93,14 @@ _SIGS = {
     "clowns_pcgpme_static_dev": (C.c_int, [C.c_void_p, C.c_int, C.c_int, C.c_void_p, C.c_void_p, C.c_int,
                                            C.c_void_p, C.c_void_p, C.c_double, C.c_double, C.c_int,
                                            C.c_void_p, C.c_void_p]),
+    "clowns_tuned_shape": (C.c_int, [C.c_int, C.c_void_p, C.c_int, C.c_void_p, C.c_void_p, C.c_void_p]),
+    "clowns_session_create": (C.c_int, [C.c_void_p, C.c_void_p, C.c_int, C.c_int, C.c_int] + [C.c_void_p] * 7),
+    "clowns_session_set_fields": (C.c_int, [C.c_void_p] * 9),
+    "clowns_session_classify": (C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p]),
+    "clowns_session_pressure_loop": (C.c_int, [C.c_void_p, C.c_double, C.c_double, C.c_double, C.c_int]
+                                     + [C.c_void_p] * 5),
+    "clowns_session_get_fields": (C.c_int, [C.c_void_p] * 7),
+    "clowns_session_destroy": (C.c_int, [C.c_void_p]),
     "clowns_transpose_dev": (C.c_int, [C.c_int, C.c_int] + [C.c_void_p] * 8),
     "clowns_face_grad_dev": (C.c_int, [C.c_void_p, C.c_int, C.c_int, C.c_int] + [C.c_void_p] * 13),
     "clowns_correct_dev": (C.c_int, [C.c_void_p, C.c_int, C.c_int] + [C.c_void_p] * 8
@@ -325,6 +333,16 @@ PREC_FP64 = 0
 PREC_MIXED = 1
 
 
+def tuned_shape(sizes, precision=0):
+    """(block, grid, registers) the autotuner chose for this row space, or None."""
+    L = lib()
+    arr = (C.c_int * len(sizes))(*[int(v) for v in sizes])
+    b, g, r = C.c_int(0), C.c_int(0), C.c_int(0)
+    if L.clowns_tuned_shape(len(sizes), arr, precision, C.byref(b), C.byref(g), C.byref(r)) != 0:
+        return None
+    return {"block": b.value, "grid": g.value, "registers": r.value}
+
+
 class Member(C.Structure):
     """clowns_member: one system of an ensemble (device pointers)."""
     _fields_ = [("al", C.c_void_p), ("ll", C.c_void_p), ("d", C.c_void_p), ("b", C.c_void_p),
@@ -497,3 +515,59 @@ def adjoint_dev(dc: DeviceCase, sy: DeviceSystem, x, djdx, eps: float = 1e-12, s
     info = solver.solve(alt, llt, det, rhs, lam, eps=eps)
     grad_a = face_grad_dev(dc, sy, x, lam)
     return lam[:n], grad_a, info
+
+
+# ---------------------------------------------------------------------------
+# Device-resident ik loop
+
+class Session:
+    """The pressure-correction ik loop of one domain with its arrays in HBM."""
+
+    def __init__(self, case):
+        L = lib()
+        self.case = case
+        self.h = C.c_void_p()
+        c = case
+        self._keep = [np.ascontiguousarray(v) for v in (c.dims, c.mn, c.in_, c.jn, c.kn, c.x, c.dx, c.objno)]
+        d, mn, in_, jn, kn, x, dx, ob = self._keep
+        _check(L.clowns_session_create(C.byref(self.h), d.ctypes.data, c.inne, c.inne2, c.mx2, mn.ctypes.data,
+                                       in_.ctypes.data, jn.ctypes.data, kn.ctypes.data, x.ctypes.data,
+                                       dx.ctypes.data, ob.ctypes.data), "session_create")
+
+    def set_fields(self, nf, nfb, f, fb, a, un, sp, p):
+        arrs = [np.ascontiguousarray(v) for v in (nf, nfb, f, fb, a, un, sp, p)]
+        _check(lib().clowns_session_set_fields(self.h, *[v.ctypes.data for v in arrs]), "session_set_fields")
+
+    def classify(self):
+        ifln, isfn = C.c_int(0), C.c_int(0)
+        _check(lib().clowns_session_classify(self.h, C.byref(ifln), C.byref(isfn)), "session_classify")
+        return ifln.value, isfn.value
+
+    def pressure_loop(self, dt, d0=1e-5, eps0=1e-10, precision=PREC_FP64):
+        ik, dmax, it, err, icon = C.c_int(0), C.c_double(0), C.c_int(0), C.c_double(0), C.c_int(0)
+        _check(lib().clowns_session_pressure_loop(self.h, dt, d0, eps0, precision, C.byref(ik), C.byref(dmax),
+                                                  C.byref(it), C.byref(err), C.byref(icon)), "pressure_loop")
+        return {"ik": ik.value, "dmax": dmax.value, "iter": it.value, "err": err.value, "icon": icon.value}
+
+    def fields(self):
+        nc = self.case.inne2 + 2
+        nf = np.zeros(nc, np.int32)
+        nfb = np.zeros(nc, np.int32)
+        f = np.zeros(nc)
+        p = np.zeros(nc)
+        un = np.zeros((nc, 3))
+        mnoe = C.c_int(0)
+        _check(lib().clowns_session_get_fields(self.h, nf.ctypes.data, nfb.ctypes.data, f.ctypes.data,
+                                               p.ctypes.data, un.ctypes.data, C.byref(mnoe)), "get_fields")
+        return {"nf": nf, "nfb": nfb, "f": f, "p": p, "un": un, "mnoe": mnoe.value}
+
+    def close(self):
+        if self.h:
+            lib().clowns_session_destroy(self.h)
+            self.h = C.c_void_p()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass

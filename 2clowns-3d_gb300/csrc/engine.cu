@@ -222,7 +222,7 @@ struct EngLayout {
     long NV = 0;
     int M = 0, nblk = 0, mixed = 0, tsize = 8;
     size_t o_blk_member, o_blk_rows, o_mem_off, o_mem_n, o_mem_nblk, o_mem_blk0, o_ticket, o_ctrl;
-    size_t o_in, o_S, o_partials, o_al, o_ll, o_d, o_vec[8], o_W, o_x64, o_r64, o_s64, o_t64;
+    size_t o_in, o_S, o_partials, o_bar, o_al, o_ll, o_d, o_vec[8], o_W, o_x64, o_r64, o_s64, o_t64;
     size_t total = 0;
 };
 
@@ -248,6 +248,7 @@ static EngLayout eng_layout(int M, const int* n, int mixed) {
     L.o_in = take(sizeof(MemberIn) * M);
     L.o_S = take(sizeof(MemberScalars) * M);
     L.o_partials = take(sizeof(double) * 2 * L.nblk);
+    L.o_bar = take(sizeof(GridBar));
     L.o_al = take((size_t)L.tsize * 6 * NV);
     L.o_ll = take(sizeof(int) * 6 * NV);
     L.o_d = take((size_t)L.tsize * NV);
@@ -338,7 +339,7 @@ static int eng_upload_tables(void* work, const EngLayout& L, const int* n, const
 // Launch shapes (autotuned per row-space size and precision)
 
 struct Shape {
-    int block = kEngBlock;
+    int block = kStepBlock;
     int grid = 0;   // 0: one block per tile
 };
 
@@ -431,93 +432,119 @@ static Shape autotune(const Eng<T>& E, long key_nv, int key_prec, cudaStream_t s
 }
 
 // ---------------------------------------------------------------------------
-// Graph cache
+// Persistent loop launch (cooperative: all blocks co-resident)
 
-struct GraphKey {
-    const void* work;
-    long NV;
-    int M, mixed, nl, kind;
-    double P1, tol, imax;
-    bool operator<(const GraphKey& o) const {
-        return std::tie(work, NV, M, mixed, nl, kind, P1, tol, imax) <
-               std::tie(o.work, o.NV, o.M, o.mixed, o.nl, o.kind, o.P1, o.tol, o.imax);
-    }
+struct LoopShape {
+    int block = kStepBlock;
+    int grid = 0;
+    int minb = 8;     // register budget of the loop kernel: 8 -> 32, 4 -> 64 registers
 };
-static std::mutex g_graph_mu;
-static std::map<GraphKey, cudaGraphExec_t> g_graphs;
-static cudaStream_t g_cap0 = nullptr, g_cap1 = nullptr;
 
-void release_all_graphs() {
-    std::lock_guard<std::mutex> lk(g_graph_mu);
-    for (auto& kv : g_graphs) cudaGraphExecDestroy(kv.second);
-    g_graphs.clear();
+template <typename T>
+static const void* loop_fn(int minb) {
+    return minb == 4 ? (const void*)k_eng_loop<T, 4> : (const void*)k_eng_loop<T, 8>;
 }
 
-void release_graphs_for(const void* work) {
-    std::lock_guard<std::mutex> lk(g_graph_mu);
-    for (auto it = g_graphs.begin(); it != g_graphs.end();) {
-        if (it->first.work == work) {
-            cudaGraphExecDestroy(it->second);
-            it = g_graphs.erase(it);
-        } else {
-            ++it;
-        }
-    }
-}
+static std::mutex g_loop_mu;
+static std::map<std::pair<long, int>, LoopShape> g_loop_shapes;
 
-// Capture: prefix(s) ; WHILE { body(s2) ; guard } ; suffix(s)
-template <typename Prefix, typename Body, typename Suffix>
-static int capture_loop_graph(Prefix prefix, Body body, Suffix suffix, MemberScalars* S, int M, int* ctrl,
-                              cudaGraphExec_t* out) {
-    if (!g_cap0) CLOWNS_CUDA_TRY(cudaStreamCreateWithFlags(&g_cap0, cudaStreamNonBlocking));
-    if (!g_cap1) CLOWNS_CUDA_TRY(cudaStreamCreateWithFlags(&g_cap1, cudaStreamNonBlocking));
-    cudaStream_t s = g_cap0, s2 = g_cap1;
-    CLOWNS_CUDA_TRY(cudaStreamBeginCapture(s, cudaStreamCaptureModeThreadLocal));
-    prefix(s);
-    cudaStreamCaptureStatus st;
-    cudaGraph_t cap;
-    const cudaGraphNode_t* deps = nullptr;
-    size_t ndeps = 0;
-    CLOWNS_CUDA_TRY(cudaStreamGetCaptureInfo(s, &st, nullptr, &cap, &deps, nullptr, &ndeps));
-    cudaGraphConditionalHandle h;
-    CLOWNS_CUDA_TRY(cudaGraphConditionalHandleCreate(&h, cap, 1, cudaGraphCondAssignDefault));
-    cudaGraphNodeParams cp = {cudaGraphNodeTypeConditional};
-    cp.conditional.handle = h;
-    cp.conditional.type = cudaGraphCondTypeWhile;
-    cp.conditional.size = 1;
-    cudaGraphNode_t cnode;
-    CLOWNS_CUDA_TRY(cudaGraphAddNode(&cnode, cap, deps, nullptr, ndeps, &cp));
-    CLOWNS_CUDA_TRY(cudaStreamUpdateCaptureDependencies(s, &cnode, nullptr, 1, cudaStreamSetCaptureDependencies));
-    cudaGraph_t bg = cp.conditional.phGraph_out[0];
-    CLOWNS_CUDA_TRY(cudaStreamBeginCaptureToGraph(s2, bg, nullptr, nullptr, 0, cudaStreamCaptureModeThreadLocal));
-    body(s2);
-    k_eng_guard<<<1, 256, 0, s2>>>(S, M, ctrl, h);
-    cudaGraph_t bout;
-    CLOWNS_CUDA_TRY(cudaStreamEndCapture(s2, &bout));
-    suffix(s);
-    cudaGraph_t g;
-    CLOWNS_CUDA_TRY(cudaStreamEndCapture(s, &g));
-    cudaGraphExec_t ex;
-    CLOWNS_CUDA_TRY(cudaGraphInstantiate(&ex, g, 0));
-    cudaGraphDestroy(g);
-    *out = ex;
+template <typename T>
+static int loop_max_grid(int block, int minb, int* out) {
+    int per_sm = 0, dev = 0, sms = 0;
+    CLOWNS_CUDA_TRY(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, loop_fn<T>(minb), block, 0));
+    CLOWNS_CUDA_TRY(cudaGetDevice(&dev));
+    CLOWNS_CUDA_TRY(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
+    *out = per_sm * sms;
     return CLOWNS_OK;
 }
 
-static int cached_graph(const GraphKey& key, cudaGraphExec_t* out) {
-    auto it = g_graphs.find(key);
-    if (it == g_graphs.end()) return 0;
-    *out = it->second;
-    return 1;
+template <typename T>
+static int launch_loop(Eng<T> E, GridBar* gb, int init, const LoopShape& sh, cudaStream_t s) {
+    int grid = std::max(1, std::min(sh.grid, E.nblk));
+    CLOWNS_CUDA_TRY(cudaMemsetAsync(gb, 0, sizeof(GridBar), s));
+    void* args[] = {(void*)&E, (void*)&gb, (void*)&init};
+    CLOWNS_CUDA_TRY(cudaLaunchCooperativeKernel(loop_fn<T>(sh.minb), dim3(grid), dim3(sh.block), args, 0, s));
+    return CLOWNS_OK;
 }
 
-static void store_graph(const GraphKey& key, cudaGraphExec_t ex) {
-    if (g_graphs.size() >= 64) {
-        cudaGraphExecDestroy(g_graphs.begin()->second);
-        g_graphs.erase(g_graphs.begin());
+static int check_abort(GridBar* gb, cudaStream_t s) {
+    int abort = 0;
+    CLOWNS_CUDA_TRY(cudaMemcpyAsync(&abort, &gb->abort, sizeof(int), cudaMemcpyDeviceToHost, s));
+    CLOWNS_CUDA_TRY(cudaStreamSynchronize(s));
+    if (abort) {
+        set_last_error_msg("pcgpme: a grid barrier timed out; the solve was abandoned");
+        return CLOWNS_ERR_NOCONV;
     }
-    g_graphs[key] = ex;
+    return CLOWNS_OK;
 }
+
+// Autotuner: time a few iterations of the persistent loop for candidate block
+// and grid sizes on the actual row space; the fastest shape is cached per
+// (row-space size, precision).  `prime` re-creates the state a loop starts from.
+template <typename T, typename Prime>
+static int tune_loop(Eng<T> E, GridBar* gb, long key_nv, int key_prec, int init, Prime prime, cudaStream_t s,
+                     LoopShape* out) {
+    {
+        std::lock_guard<std::mutex> lk(g_loop_mu);
+        auto it = g_loop_shapes.find({key_nv, key_prec});
+        if (it != g_loop_shapes.end()) { *out = it->second; return CLOWNS_OK; }
+    }
+    std::vector<LoopShape> cands;
+    for (int minb : {8, 4})
+        for (int b : {kStepBlock}) {
+            int gmax = 0;
+            int rc = loop_max_grid<T>(b, minb, &gmax);
+            if (rc) return rc;
+            for (int frac : {4, 3, 2}) {
+                LoopShape sh;
+                sh.block = b;
+                sh.minb = minb;
+                sh.grid = std::max(1, gmax * frac / 4);
+                cands.push_back(sh);
+            }
+        }
+    cudaEvent_t e0, e1;
+    CLOWNS_CUDA_TRY(cudaEventCreate(&e0));
+    CLOWNS_CUDA_TRY(cudaEventCreate(&e1));
+    LoopShape best = cands[0];
+    float best_ms = 1e30f;
+    for (const LoopShape& sh : cands) {
+        float ms = 0.f;
+        for (int rep = 0; rep < 2; rep++) {
+            prime(s);
+            CLOWNS_CUDA_TRY(cudaEventRecord(e0, s));
+            int rc = launch_loop(E, gb, init, sh, s);
+            if (rc) return rc;
+            CLOWNS_CUDA_TRY(cudaEventRecord(e1, s));
+            CLOWNS_CUDA_TRY(cudaEventSynchronize(e1));
+            CLOWNS_CUDA_TRY(cudaEventElapsedTime(&ms, e0, e1));
+            int rc2 = check_abort(gb, s);
+            if (rc2) return rc2;
+        }
+        if (ms < best_ms) { best_ms = ms; best = sh; }
+    }
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    std::lock_guard<std::mutex> lk(g_loop_mu);
+    g_loop_shapes[{key_nv, key_prec}] = best;
+    *out = best;
+    return CLOWNS_OK;
+}
+
+int engine_tuned_shape(long nv, int prec, int* block, int* grid, int* minb) {
+    std::lock_guard<std::mutex> lk(g_loop_mu);
+    auto it = g_loop_shapes.find({nv, prec});
+    if (it == g_loop_shapes.end()) return CLOWNS_ERR_ARG;
+    *block = it->second.block;
+    *grid = it->second.grid;
+    *minb = it->second.minb;
+    return CLOWNS_OK;
+}
+
+long engine_row_space(int M, const int* n, int mixed) { return eng_layout(M, n, mixed).NV; }
+
+void release_all_graphs() {}
+void release_graphs_for(const void*) {}
 
 // ---------------------------------------------------------------------------
 // Solves
@@ -583,7 +610,8 @@ static int check_members(int M, const MemberIn* ins, std::vector<int>& n, int* n
     return CLOWNS_OK;
 }
 
-// Plain FP64 (reference method and stop tests) over M members.
+// Plain FP64 (reference method and stop tests) over M members: setup kernel,
+// one persistent launch for PCGPME's start and its whole iteration loop, copy-out.
 int engine_solve_plain(int M, const MemberIn* ins, double eps, double parm, int iter, void* work,
                        size_t work_bytes, cudaStream_t s, clowns_solve_info* info) {
     std::vector<int> n;
@@ -602,33 +630,25 @@ int engine_solve_plain(int M, const MemberIn* ins, double eps, double parm, int 
     rc = eng_upload_tables(work, L, n.data(), ins, s);
     if (rc) return rc;
     Eng<double> E = eng_bind<double>(work, L);
-    k_eng_init_scalars<<<1, 256, 0, s>>>(E.S, M, eps_r, iter_r, 0, E.ctrl);
+    GridBar* gb = (GridBar*)((char*)work + L.o_bar);
+    const int gs = std::min(L.nblk * 2, kEngMaxGrid * 4);
+    auto prime = [&](cudaStream_t cs, double e, int it) {
+        k_eng_init_scalars<<<1, 256, 0, cs>>>(E.S, M, e, it, 0, E.ctrl);
+        if (nl == 6) k_eng_setup<double, 6><<<gs, kEngBlock, 0, cs>>>(E, P1, P2, 0);
+        else k_eng_setup<double, 4><<<gs, kEngBlock, 0, cs>>>(E, P1, P2, 0);
+    };
+    LoopShape sh;
+    // tuning runs: eight iterations from the real start
+    rc = tune_loop(E, gb, L.NV, 0, 1, [&](cudaStream_t cs) { prime(cs, 1e-300, 8); }, s, &sh);
+    if (rc) return rc;
+    prime(s, eps_r, iter_r);
     CLOWNS_CUDA_TRY(cudaGetLastError());
-    std::lock_guard<std::mutex> lk(g_graph_mu);
-    GraphKey key{work, L.NV, M, 0, nl, 0, P1, 0.0, 0.0};
-    cudaGraphExec_t ex;
-    if (!cached_graph(key, &ex)) {
-        const int gs = std::min(L.nblk * 4, kEngMaxGrid * 4);
-        if (nl == 6) k_eng_setup<double, 6><<<gs, kEngBlock, 0, s>>>(E, P1, P2, 0);
-        else k_eng_setup<double, 4><<<gs, kEngBlock, 0, s>>>(E, P1, P2, 0);
-        Shape sh = autotune(E, L.NV, 0, s);
-        rc = capture_loop_graph(
-            [&](cudaStream_t cs) {
-                if (nl == 6) k_eng_setup<double, 6><<<gs, kEngBlock, 0, cs>>>(E, P1, P2, 0);
-                else k_eng_setup<double, 4><<<gs, kEngBlock, 0, cs>>>(E, P1, P2, 0);
-                launch_ldusub_inplace(E, sh, E.p, E.t, E.q, cs);     // b^ = PM W b
-                launch_apply(E, sh, E.xi, E.q, E.t, 0, cs);           // q = PM A x0
-                k_eng_initres<double><<<grid_of(sh, E.nblk), sh.block, 0, cs>>>(E);
-            },
-            [&](cudaStream_t cs) { launch_iteration(E, sh, cs); },
-            [&](cudaStream_t cs) { k_eng_copy_out<double><<<gs, kEngBlock, 0, cs>>>(E); },
-            E.S, M, E.ctrl, &ex);
-        if (rc) return rc;
-        store_graph(key, ex);
-        // the autotuning runs wrote the vectors; re-initialise the scalars
-        k_eng_init_scalars<<<1, 256, 0, s>>>(E.S, M, eps_r, iter_r, 0, E.ctrl);
-    }
-    CLOWNS_CUDA_TRY(cudaGraphLaunch(ex, s));
+    rc = launch_loop(E, gb, 1, sh, s);
+    if (rc) return rc;
+    k_eng_copy_out<double><<<gs, kEngBlock, 0, s>>>(E);
+    CLOWNS_CUDA_TRY(cudaGetLastError());
+    rc = check_abort(gb, s);
+    if (rc) return rc;
     return read_infos(work, L, s, info, 0);
 }
 
@@ -656,39 +676,42 @@ int engine_solve_mixed(int M, const MemberIn* ins, double eps, double parm, doub
     rc = eng_upload_tables(work, L, n.data(), ins, s);
     if (rc) return rc;
     Eng<float> E = eng_bind<float>(work, L);
-    k_mixed_init_scalars<<<1, 256, 0, s>>>(E.S, M, eps_r, max_outer, E.ctrl);
-    const int gs = std::min(L.nblk * 4, kEngMaxGrid * 4);
-    if (nl == 6) k_eng_setup<float, 6><<<gs, kEngBlock, 0, s>>>(E, P1, P2, 1);
-    else k_eng_setup<float, 4><<<gs, kEngBlock, 0, s>>>(E, P1, P2, 1);
+    GridBar* gb = (GridBar*)((char*)work + L.o_bar);
+    const int gs = std::min(L.nblk * 2, kEngMaxGrid * 4);
+    const Shape ksh;                               // standalone FP64 refinement kernels
+    const int kg = grid_of(ksh, E.nblk);
+    auto setup = [&](cudaStream_t cs) {
+        k_mixed_init_scalars<<<1, 256, 0, cs>>>(E.S, M, eps_r, max_outer, E.ctrl);
+        if (nl == 6) k_eng_setup<float, 6><<<gs, kEngBlock, 0, cs>>>(E, P1, P2, 1);
+        else k_eng_setup<float, 4><<<gs, kEngBlock, 0, cs>>>(E, P1, P2, 1);
+        launch_ldusub64<float, 0>(E, ksh, inner_tol, inner_max, cs);   // BN64 = ||PM W b||^2
+    };
+    // one refinement sweep up to the inner loop: residual, PM r, ERR test, inner RHS
+    auto sweep_head = [&](cudaStream_t cs, double itol, int imax) {
+        k_mx_reset_ctrl<<<1, 32, 0, cs>>>(E.ctrl, imax);
+        k_mx_residual<float><<<kg, ksh.block, 0, cs>>>(E);
+        launch_ldusub64<float, 1>(E, ksh, itol, imax, cs);
+        k_mx_normalize<float><<<kg, ksh.block, 0, cs>>>(E);
+    };
+    LoopShape sh;
+    rc = tune_loop(E, gb, L.NV, 1, 0, [&](cudaStream_t cs) { setup(cs); sweep_head(cs, 1e-30, 8); }, s, &sh);
+    if (rc) return rc;
+    setup(s);
     CLOWNS_CUDA_TRY(cudaGetLastError());
-    std::lock_guard<std::mutex> lk(g_graph_mu);
-    Shape sh = autotune(E, L.NV, 1, s);
-    // BN64 = ||PM W b||^2 (r64 holds W b after the setup)
-    launch_ldusub64<float, 0>(E, sh, inner_tol, inner_max, s);
-    GraphKey key{work, L.NV, M, 1, nl, 1, P1, inner_tol, (double)inner_max};
-    cudaGraphExec_t ex;
-    if (!cached_graph(key, &ex)) {
-        rc = capture_loop_graph(
-            [&](cudaStream_t cs) {
-                k_mx_reset_ctrl<<<1, 32, 0, cs>>>(E.ctrl, inner_max);
-                k_mx_residual<float><<<grid_of(sh, E.nblk), sh.block, 0, cs>>>(E);
-                launch_ldusub64<float, 1>(E, sh, inner_tol, inner_max, cs);
-                k_mx_normalize<float><<<grid_of(sh, E.nblk), sh.block, 0, cs>>>(E);
-            },
-            [&](cudaStream_t cs) { launch_iteration(E, sh, cs); },
-            [&](cudaStream_t cs) { k_mx_update<float><<<grid_of(sh, E.nblk), sh.block, 0, cs>>>(E); },
-            E.S, M, E.ctrl, &ex);
-        if (rc) return rc;
-        store_graph(key, ex);
-    }
     std::vector<MemberScalars> h(M);
     for (int sweep = 0; sweep <= max_outer + 1; sweep++) {
-        CLOWNS_CUDA_TRY(cudaGraphLaunch(ex, s));
+        sweep_head(s, inner_tol, inner_max);
         CLOWNS_CUDA_TRY(cudaMemcpyAsync(h.data(), E.S, sizeof(MemberScalars) * M, cudaMemcpyDeviceToHost, s));
         CLOWNS_CUDA_TRY(cudaStreamSynchronize(s));
         bool all = true;
         for (int m = 0; m < M; m++) all = all && h[m].odone;
         if (all) break;
+        rc = launch_loop(E, gb, 0, sh, s);
+        if (rc) return rc;
+        k_mx_update<float><<<kg, ksh.block, 0, s>>>(E);
+        CLOWNS_CUDA_TRY(cudaGetLastError());
+        rc = check_abort(gb, s);
+        if (rc) return rc;
     }
     k_mx_copy_out<float><<<gs, kEngBlock, 0, s>>>(E);
     CLOWNS_CUDA_TRY(cudaGetLastError());

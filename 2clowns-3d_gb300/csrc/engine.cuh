@@ -15,8 +15,10 @@
 
 namespace clowns {
 
-constexpr int kTile = 2048;          // rows per tile (multiple of kEngBlock)
+constexpr int kTile = 512;           // rows per tile (multiple of kEngBlock)
 constexpr int kEngBlock = 256;
+constexpr int kRowsPerThread = 4;   // rows a thread handles per step (explicit ILP)
+constexpr int kStepBlock = kTile / kRowsPerThread;   // threads covering one tile in one step
 constexpr int kEngMaxGrid = kNumSMs * 8;
 
 // Per-member scalars; names follow pcgpme_para.F90:47.
@@ -77,6 +79,20 @@ struct Eng {
 };
 
 // ---------------------------------------------------------------------------
+// Loads of data other blocks wrote.  Vectors are read with plain loads: every
+// phase that reads a vector is separated from the phase that wrote it by a
+// kernel boundary or by grid_sync, whose gpu-scope fence orders the block's
+// later loads after the other blocks' stores (the L1 is not a source of stale
+// lines across it).  Scalars and reduction partials, which can be written by
+// the last block of a member within the same phase, are read through L2
+// (ld.global.cg).
+
+template <typename V>
+__device__ __forceinline__ V ldg2(const V* p) { return *p; }
+__device__ __forceinline__ double sld(const double* p) { return __ldcg(p); }
+__device__ __forceinline__ int sld(const int* p) { return __ldcg(p); }
+
+// ---------------------------------------------------------------------------
 // Tile walk helpers
 
 template <typename T>
@@ -85,7 +101,7 @@ __device__ __forceinline__ bool tile_active(const Eng<T>& E, int blk, int& m, lo
     if (m < 0) return false;
     rows = E.blk_rows[blk];
     if (rows == 0) return false;
-    if (E.S[m].done) return false;
+    if (sld(&E.S[m].done)) return false;
     row0 = (long)blk * kTile;
     return true;
 }
@@ -111,17 +127,19 @@ __device__ __forceinline__ bool member_reduce(const Eng<T>& E, int blk, int m, d
     __syncthreads();
     if (!last) return false;
     __threadfence();
-    if (threadIdx.x < 32) {
+    {
+        // the member's blocks are contiguous; every thread sums a fixed stride,
+        // then a fixed-order block reduction: deterministic for a given layout
         const int b0 = E.mem_blk0[m];
         const int nb = E.mem_nblk[m];
-        double s0 = 0.0, s1 = 0.0;
-        // blocks of a member are contiguous; pad-only blocks contribute zero records
-        for (int b = threadIdx.x; b < nb; b += 32) {
-            s0 += __ldcg(E.partials + 2L * (b0 + b) + 0);
-            s1 += __ldcg(E.partials + 2L * (b0 + b) + 1);
+        double s2[2] = {0.0, 0.0};
+        for (int b = threadIdx.x; b < nb; b += blockDim.x) {
+            s2[0] += __ldcg(E.partials + 2L * (b0 + b) + 0);
+            s2[1] += __ldcg(E.partials + 2L * (b0 + b) + 1);
         }
-        tot[0] = warp_sum(s0);
-        tot[1] = warp_sum(s1);
+        block_sum<2>(s2, red);
+        tot[0] = s2[0];
+        tot[1] = s2[1];
     }
     return true;
 }
@@ -224,35 +242,55 @@ static __global__ void k_eng_init_scalars(MemberScalars* S, int M, double eps, i
 }
 
 // ---------------------------------------------------------------------------
-// Operator pieces.  MEMBER-AWARE: every kernel skips tiles of stopped members.
+// Operator pieces as phase functions: a phase walks the tiles
+// blockIdx.x, blockIdx.x + gridDim.x, ... so the same code runs as a
+// standalone kernel (one block per tile) and inside the persistent kernel
+// (a co-resident grid, phases separated by grid barriers).  MEMBER-AWARE:
+// tiles of stopped members are skipped.
 
 // out = D in + sum_k AL_k in[LL_k]   (AXSUB, pcgpme_para.F90:323-352)
 template <typename T>
-__global__ void __launch_bounds__(kEngBlock) k_eng_axsub(Eng<T> E, const T* __restrict__ in,
-                                                        T* __restrict__ out) {
+__device__ __forceinline__ void ph_axsub(const Eng<T>& E, const T* __restrict__ in, T* __restrict__ out) {
+    constexpr int R = kRowsPerThread;
     const long NV = E.NV;
     for (int blk = blockIdx.x; blk < E.nblk; blk += gridDim.x) {
         int m, rows;
         long row0;
         if (!tile_active(E, blk, m, row0, rows)) continue;
-        for (int r = threadIdx.x; r < rows; r += blockDim.x) {
-            const long i = row0 + r;
-            T s = in[i] * ld_stream(E.d + i);
+        for (int base = threadIdx.x; base < rows; base += blockDim.x * R) {
+            T s[R];
+            bool ok[R];
+#pragma unroll
+            for (int u = 0; u < R; u++) {
+                const int r = base + u * blockDim.x;
+                ok[u] = r < rows;
+                const long i = row0 + (ok[u] ? r : 0);
+                s[u] = ldg2(in + i) * ld_stream(E.d + i);
+            }
 #pragma unroll
             for (int k = 0; k < 6; k++) {
-                const T a = ld_stream(E.al + k * NV + i);
-                const int c = ld_stream(E.ll + k * NV + i);
-                s += a * in[c];
+                T a[R];
+                int c[R];
+#pragma unroll
+                for (int u = 0; u < R; u++) {
+                    const long i = row0 + (ok[u] ? base + u * blockDim.x : 0);
+                    a[u] = ld_stream(E.al + k * NV + i);
+                    c[u] = ld_stream(E.ll + k * NV + i);
+                }
+#pragma unroll
+                for (int u = 0; u < R; u++) s[u] += a[u] * ldg2(in + c[u]);
             }
-            out[i] = s;
+#pragma unroll
+            for (int u = 0; u < R; u++)
+                if (ok[u]) out[row0 + base + u * blockDim.x] = s[u];
         }
     }
 }
 
 // One single-neighbour sweep of LDUSUB: out = in - AL_k in[LL_k]  (263-304)
 template <typename T>
-__global__ void __launch_bounds__(kEngBlock) k_eng_sweep(Eng<T> E, int k, const T* __restrict__ in,
-                                                        T* __restrict__ out) {
+__device__ __forceinline__ void ph_sweep(const Eng<T>& E, int k, const T* __restrict__ in, T* __restrict__ out) {
+    constexpr int R = kRowsPerThread;
     const long NV = E.NV;
     const T* __restrict__ a = E.al + k * NV;
     const int* __restrict__ c = E.ll + k * NV;
@@ -260,9 +298,24 @@ __global__ void __launch_bounds__(kEngBlock) k_eng_sweep(Eng<T> E, int k, const 
         int m, rows;
         long row0;
         if (!tile_active(E, blk, m, row0, rows)) continue;
-        for (int r = threadIdx.x; r < rows; r += blockDim.x) {
-            const long i = row0 + r;
-            out[i] = in[i] - ld_stream(a + i) * in[ld_stream(c + i)];
+        for (int base = threadIdx.x; base < rows; base += blockDim.x * R) {
+            T av[R], xv[R], gv[R];
+            int cv[R];
+            bool ok[R];
+#pragma unroll
+            for (int u = 0; u < R; u++) {
+                const int r = base + u * blockDim.x;
+                ok[u] = r < rows;
+                const long i = row0 + (ok[u] ? r : 0);
+                av[u] = ld_stream(a + i);
+                cv[u] = ld_stream(c + i);
+                xv[u] = ldg2(in + i);
+            }
+#pragma unroll
+            for (int u = 0; u < R; u++) gv[u] = ldg2(in + cv[u]);
+#pragma unroll
+            for (int u = 0; u < R; u++)
+                if (ok[u]) out[row0 + base + u * blockDim.x] = xv[u] - av[u] * gv[u];
         }
     }
 }
@@ -270,8 +323,7 @@ __global__ void __launch_bounds__(kEngBlock) k_eng_sweep(Eng<T> E, int k, const 
 // Last sweep (J=5,6, 306-318) with an optional fused per-member reduction:
 //   MODE 0 none; 1: RQ = (r0,out) -> ALP = C1/RQ; 2: AMU = (e,out)/(out,out)
 template <typename T, int MODE>
-__global__ void __launch_bounds__(kEngBlock) k_eng_sweep56(Eng<T> E, const T* __restrict__ in,
-                                                          T* __restrict__ out) {
+__device__ __forceinline__ void ph_sweep56(const Eng<T>& E, const T* __restrict__ in, T* __restrict__ out) {
     __shared__ double red[64];
     const long NV = E.NV;
     const T* __restrict__ a5 = E.al + 4 * NV;
@@ -282,13 +334,37 @@ __global__ void __launch_bounds__(kEngBlock) k_eng_sweep56(Eng<T> E, const T* __
         int m, rows;
         long row0;
         if (!tile_active(E, blk, m, row0, rows)) continue;
+        constexpr int R = kRowsPerThread;
         T acc0 = T(0), acc1 = T(0);
-        for (int r = threadIdx.x; r < rows; r += blockDim.x) {
-            const long i = row0 + r;
-            const T y = in[i] - ld_stream(a5 + i) * in[ld_stream(c5 + i)] - ld_stream(a6 + i) * in[ld_stream(c6 + i)];
-            out[i] = y;
-            if (MODE == 1) acc0 += E.r0[i] * y;
-            if (MODE == 2) { acc0 += E.e[i] * y; acc1 += y * y; }
+        for (int base = threadIdx.x; base < rows; base += blockDim.x * R) {
+            T a5v[R], a6v[R], xv[R], g5[R], g6[R];
+            int c5v[R], c6v[R];
+            bool ok[R];
+#pragma unroll
+            for (int u = 0; u < R; u++) {
+                const int r = base + u * blockDim.x;
+                ok[u] = r < rows;
+                const long i = row0 + (ok[u] ? r : 0);
+                a5v[u] = ld_stream(a5 + i);
+                a6v[u] = ld_stream(a6 + i);
+                c5v[u] = ld_stream(c5 + i);
+                c6v[u] = ld_stream(c6 + i);
+                xv[u] = ldg2(in + i);
+            }
+#pragma unroll
+            for (int u = 0; u < R; u++) {
+                g5[u] = ldg2(in + c5v[u]);
+                g6[u] = ldg2(in + c6v[u]);
+            }
+#pragma unroll
+            for (int u = 0; u < R; u++) {
+                if (!ok[u]) continue;
+                const long i = row0 + base + u * blockDim.x;
+                const T y = xv[u] - a5v[u] * g5[u] - a6v[u] * g6[u];
+                out[i] = y;
+                if (MODE == 1) acc0 += ldg2(E.r0 + i) * y;
+                if (MODE == 2) { acc0 += ldg2(E.e + i) * y; acc1 += y * y; }
+            }
         }
         if (MODE == 0) continue;
         double tot[2];
@@ -297,20 +373,24 @@ __global__ void __launch_bounds__(kEngBlock) k_eng_sweep56(Eng<T> E, const T* __
             MemberScalars* S = E.S + m;
             E.ticket[m] = 0;
             if (MODE == 1) {
+                const double C1 = sld(&S->C1);
                 S->RQ = tot[0];
-                S->ALP = S->C1 / tot[0];                               // 167
-                if (!isfinite(tot[0]) || !isfinite(S->ALP)) {
-                    S->K += 1;
-                    stop_member(S, CLOWNS_STOP_NONFINITE, S->mode == 0 ? CLOWNS_IER_NONFINITE : 0);
+                const double ALP = C1 / tot[0];                         // 167
+                S->ALP = ALP;
+                if (!isfinite(tot[0]) || !isfinite(ALP)) {
+                    S->K = sld(&S->K) + 1;
+                    stop_member(S, CLOWNS_STOP_NONFINITE, sld(&S->mode) == 0 ? CLOWNS_IER_NONFINITE : 0);
                 }
             } else {
                 S->SS = tot[1];
-                S->AMU = tot[0] / tot[1];                              // 197
-                if (!isfinite(tot[1]) || !isfinite(S->AMU)) {
-                    S->K += 1;
-                    stop_member(S, CLOWNS_STOP_NONFINITE, S->mode == 0 ? CLOWNS_IER_NONFINITE : 0);
+                const double AMU = tot[0] / tot[1];                     // 197
+                S->AMU = AMU;
+                if (!isfinite(tot[1]) || !isfinite(AMU)) {
+                    S->K = sld(&S->K) + 1;
+                    stop_member(S, CLOWNS_STOP_NONFINITE, sld(&S->mode) == 0 ? CLOWNS_IER_NONFINITE : 0);
                 }
             }
+            __threadfence();
         }
         __syncthreads();
     }
@@ -318,15 +398,27 @@ __global__ void __launch_bounds__(kEngBlock) k_eng_sweep56(Eng<T> E, const T* __
 
 // E = R - ALP Q  (171-175)
 template <typename T>
-__global__ void __launch_bounds__(kEngBlock) k_eng_eupdate(Eng<T> E) {
+__device__ __forceinline__ void ph_eupdate(const Eng<T>& E) {
     for (int blk = blockIdx.x; blk < E.nblk; blk += gridDim.x) {
         int m, rows;
         long row0;
         if (!tile_active(E, blk, m, row0, rows)) continue;
-        const T ALP = T(E.S[m].ALP);
-        for (int r = threadIdx.x; r < rows; r += blockDim.x) {
-            const long i = row0 + r;
-            E.e[i] = E.r[i] - ALP * E.q[i];
+        const T ALP = T(sld(&E.S[m].ALP));
+        constexpr int R = kRowsPerThread;
+        for (int base = threadIdx.x; base < rows; base += blockDim.x * R) {
+            T rv[R], qv[R];
+#pragma unroll
+            for (int u = 0; u < R; u++) {
+                const int r = base + u * blockDim.x;
+                const long i = row0 + (r < rows ? r : 0);
+                rv[u] = ldg2(E.r + i);
+                qv[u] = ldg2(E.q + i);
+            }
+#pragma unroll
+            for (int u = 0; u < R; u++) {
+                const int r = base + u * blockDim.x;
+                if (r < rows) E.e[row0 + r] = rv[u] - ALP * qv[u];
+            }
         }
     }
 }
@@ -334,22 +426,38 @@ __global__ void __launch_bounds__(kEngBlock) k_eng_eupdate(Eng<T> E) {
 // X += ALP P + AMU E ; R = E - AMU V ; RN = (R,R) ; C1 = (R0,R)  (199-213),
 // then ERR and the stop tests (215-241).
 template <typename T>
-__global__ void __launch_bounds__(kEngBlock) k_eng_xrupdate(Eng<T> E) {
+__device__ __forceinline__ void ph_xrupdate(const Eng<T>& E) {
     __shared__ double red[64];
     for (int blk = blockIdx.x; blk < E.nblk; blk += gridDim.x) {
         int m, rows;
         long row0;
         if (!tile_active(E, blk, m, row0, rows)) continue;
-        const T ALP = T(E.S[m].ALP), AMU = T(E.S[m].AMU);
+        const T ALP = T(sld(&E.S[m].ALP)), AMU = T(sld(&E.S[m].AMU));
         T acc0 = T(0), acc1 = T(0);
-        for (int r = threadIdx.x; r < rows; r += blockDim.x) {
-            const long i = row0 + r;
-            const T temp = E.e[i];
-            E.xi[i] = E.xi[i] + ALP * E.p[i] + AMU * temp;
-            const T rn = temp - AMU * E.v[i];
-            E.r[i] = rn;
-            acc0 += rn * rn;
-            acc1 += rn * E.r0[i];
+        constexpr int R = kRowsPerThread;
+        for (int base = threadIdx.x; base < rows; base += blockDim.x * R) {
+            T ev[R], xv[R], pv[R], vv[R], r0v[R];
+#pragma unroll
+            for (int u = 0; u < R; u++) {
+                const int r = base + u * blockDim.x;
+                const long i = row0 + (r < rows ? r : 0);
+                ev[u] = ldg2(E.e + i);
+                xv[u] = ldg2(E.xi + i);
+                pv[u] = ldg2(E.p + i);
+                vv[u] = ldg2(E.v + i);
+                r0v[u] = ldg2(E.r0 + i);
+            }
+#pragma unroll
+            for (int u = 0; u < R; u++) {
+                const int r = base + u * blockDim.x;
+                if (r >= rows) continue;
+                const long i = row0 + r;
+                E.xi[i] = xv[u] + ALP * pv[u] + AMU * ev[u];
+                const T rn = ev[u] - AMU * vv[u];
+                E.r[i] = rn;
+                acc0 += rn * rn;
+                acc1 += rn * r0v[u];
+            }
         }
         double tot[2];
         if (!member_reduce(E, blk, m, (double)acc0, (double)acc1, red, tot)) continue;
@@ -357,37 +465,41 @@ __global__ void __launch_bounds__(kEngBlock) k_eng_xrupdate(Eng<T> E) {
             MemberScalars* S = E.S + m;
             E.ticket[m] = 0;
             const double RN = tot[0], C1 = tot[1];
+            const double AMUs = sld(&S->AMU), RQ = sld(&S->RQ), BN = sld(&S->BN);
+            const double ERRP = sld(&S->ERRP), EPS = sld(&S->EPS);
+            const int mode = sld(&S->mode), ITER = sld(&S->ITER);
             S->RN = RN;
             S->C1 = C1;
-            S->K += 1;
-            S->total_iter += 1;
-            const int K = S->K;
-            const double ERR = sqrt(RN / S->BN);                        // 215
+            const int K = sld(&S->K) + 1;
+            S->K = K;
+            S->total_iter = sld(&S->total_iter) + 1;
+            const double ERR = sqrt(RN / BN);                            // 215
             S->ERR = ERR;
             if (!isfinite(RN) || !isfinite(C1)) {
-                stop_member(S, CLOWNS_STOP_NONFINITE, S->mode == 0 ? CLOWNS_IER_NONFINITE : 0);
-            } else if (K >= 10 && fabs(ERR - S->ERRP) <= ERR * 1.0e-6) {  // 228
+                stop_member(S, CLOWNS_STOP_NONFINITE, mode == 0 ? CLOWNS_IER_NONFINITE : 0);
+            } else if (K >= 10 && fabs(ERR - ERRP) <= ERR * 1.0e-6) {    // 228
                 stop_member(S, CLOWNS_STOP_STAGNATION, 0);
-            } else if (ERR <= S->EPS) {                                  // 232
+            } else if (ERR <= EPS) {                                     // 232
                 stop_member(S, CLOWNS_STOP_TOL, 0);
             } else {
                 S->ERRP = ERR;
-                if (S->AMU == 0.0) {                                     // 234
+                if (AMUs == 0.0) {                                       // 234
                     stop_member(S, CLOWNS_STOP_AMU_ZERO, 0);
                 } else if (C1 == 0.0) {                                  // 240
                     stop_member(S, CLOWNS_STOP_C1_ZERO, 0);
                 } else {
-                    S->BETA = C1 / S->AMU / S->RQ;                       // 241
-                    if (K >= S->ITER) {                                  // 250-254
-                        if (S->mode == 0) {
+                    S->BETA = C1 / AMUs / RQ;                            // 241
+                    if (K >= ITER) {                                     // 250-254
+                        if (mode == 0) {
                             stop_member(S, CLOWNS_STOP_MAXITER, CLOWNS_IER_MAXITER);
-                            S->K = S->ITER + 1;
+                            S->K = ITER + 1;
                         } else {
                             stop_member(S, CLOWNS_STOP_MAXITER, 0);
                         }
                     }
                 }
             }
+            __threadfence();
         }
         __syncthreads();
     }
@@ -395,15 +507,28 @@ __global__ void __launch_bounds__(kEngBlock) k_eng_xrupdate(Eng<T> E) {
 
 // P = R + BETA (P - AMU Q)  (242-246)
 template <typename T>
-__global__ void __launch_bounds__(kEngBlock) k_eng_pupdate(Eng<T> E) {
+__device__ __forceinline__ void ph_pupdate(const Eng<T>& E) {
     for (int blk = blockIdx.x; blk < E.nblk; blk += gridDim.x) {
         int m, rows;
         long row0;
         if (!tile_active(E, blk, m, row0, rows)) continue;
-        const T BETA = T(E.S[m].BETA), AMU = T(E.S[m].AMU);
-        for (int r = threadIdx.x; r < rows; r += blockDim.x) {
-            const long i = row0 + r;
-            E.p[i] = E.r[i] + BETA * (E.p[i] - AMU * E.q[i]);
+        const T BETA = T(sld(&E.S[m].BETA)), AMU = T(sld(&E.S[m].AMU));
+        constexpr int R = kRowsPerThread;
+        for (int base = threadIdx.x; base < rows; base += blockDim.x * R) {
+            T rv[R], pv[R], qv[R];
+#pragma unroll
+            for (int u = 0; u < R; u++) {
+                const int r = base + u * blockDim.x;
+                const long i = row0 + (r < rows ? r : 0);
+                rv[u] = ldg2(E.r + i);
+                pv[u] = ldg2(E.p + i);
+                qv[u] = ldg2(E.q + i);
+            }
+#pragma unroll
+            for (int u = 0; u < R; u++) {
+                const int r = base + u * blockDim.x;
+                if (r < rows) E.p[row0 + r] = rv[u] + BETA * (pv[u] - AMU * qv[u]);
+            }
         }
     }
 }
@@ -411,7 +536,7 @@ __global__ void __launch_bounds__(kEngBlock) k_eng_pupdate(Eng<T> E) {
 // BN = (b^,b^); R = b^ - q; C1 = (R,R); P = R0 = R  (129-145).  p holds b^ = PM W b
 // and q holds PM A x0 on entry.
 template <typename T>
-__global__ void __launch_bounds__(kEngBlock) k_eng_initres(Eng<T> E) {
+__device__ __forceinline__ void ph_initres(const Eng<T>& E) {
     __shared__ double red[64];
     for (int blk = blockIdx.x; blk < E.nblk; blk += gridDim.x) {
         int m, rows;
@@ -420,9 +545,9 @@ __global__ void __launch_bounds__(kEngBlock) k_eng_initres(Eng<T> E) {
         T acc0 = T(0), acc1 = T(0);
         for (int r = threadIdx.x; r < rows; r += blockDim.x) {
             const long i = row0 + r;
-            T temp = E.p[i];
+            T temp = ldg2(E.p + i);
             acc0 += temp * temp;
-            temp = temp - E.q[i];
+            temp = temp - ldg2(E.q + i);
             E.r[i] = temp;
             acc1 += temp * temp;
             E.p[i] = temp;
@@ -434,30 +559,144 @@ __global__ void __launch_bounds__(kEngBlock) k_eng_initres(Eng<T> E) {
             E.ticket[m] = 0;
             E.S[m].BN = tot[0];
             E.S[m].C1 = tot[1];
+            __threadfence();
         }
         __syncthreads();
     }
 }
 
-// Loop guard: the only writer of the WHILE condition.  Continue while any
-// member is still iterating; as a backstop no correct run reaches, stop after
-// max ITER + 2 body executions.
-static __global__ void k_eng_guard(MemberScalars* S, int M, int* ctrl, cudaGraphConditionalHandle h) {
-    __shared__ int any;
-    if (threadIdx.x == 0) any = 0;
-    __syncthreads();
-    for (int m = threadIdx.x; m < M; m += blockDim.x)
-        if (!S[m].done) atomicOr(&any, 1);
+// Standalone kernels (one block per tile): the same phases.
+template <typename T>
+__global__ void __launch_bounds__(kEngBlock) k_eng_axsub(Eng<T> E, const T* __restrict__ in, T* __restrict__ out) {
+    ph_axsub(E, in, out);
+}
+template <typename T>
+__global__ void __launch_bounds__(kEngBlock) k_eng_sweep(Eng<T> E, int k, const T* __restrict__ in,
+                                                        T* __restrict__ out) {
+    ph_sweep(E, k, in, out);
+}
+template <typename T, int MODE>
+__global__ void __launch_bounds__(kEngBlock) k_eng_sweep56(Eng<T> E, const T* __restrict__ in, T* __restrict__ out) {
+    ph_sweep56<T, MODE>(E, in, out);
+}
+template <typename T>
+__global__ void __launch_bounds__(kEngBlock) k_eng_eupdate(Eng<T> E) { ph_eupdate(E); }
+template <typename T>
+__global__ void __launch_bounds__(kEngBlock) k_eng_xrupdate(Eng<T> E) { ph_xrupdate(E); }
+template <typename T>
+__global__ void __launch_bounds__(kEngBlock) k_eng_pupdate(Eng<T> E) { ph_pupdate(E); }
+template <typename T>
+__global__ void __launch_bounds__(kEngBlock) k_eng_initres(Eng<T> E) { ph_initres(E); }
+
+// ---------------------------------------------------------------------------
+// Persistent iteration loop.
+//
+// One cooperative launch runs the whole BiCGSTAB loop of every member: the 16
+// phases of an iteration are separated by grid barriers instead of kernel
+// boundaries.  Every barrier wait is bounded: a block that waits longer than
+// kBarSpinLimit polls (seconds) raises the abort flag, and every block leaves
+// the kernel at its next barrier; the host then reports CLOWNS_IER_DEVICE.  No
+// correct run comes near the bound (a phase lasts microseconds to milliseconds).
+
+struct GridBar {
+    unsigned count;
+    unsigned gen;
+    int abort;
+    int pad[29];
+};
+
+constexpr long kBarSpinLimit = 1L << 24;
+
+__device__ __forceinline__ bool grid_sync(GridBar* gb) {
+    __shared__ int s_ok;
     __syncthreads();
     if (threadIdx.x == 0) {
-        ctrl[0] += 1;
-        int go = any;
-        if (go && ctrl[0] > ctrl[1] + 1) {
-            go = 0;
-            for (int m = 0; m < M; m++)
-                if (!S[m].done) stop_member(S + m, CLOWNS_STOP_MAXITER, S[m].mode == 0 ? CLOWNS_IER_MAXITER : 0);
+        volatile unsigned* genp = &gb->gen;
+        volatile int* abortp = &gb->abort;
+        const unsigned g0 = *genp;
+        __threadfence();
+        const unsigned arrived = atomicAdd(&gb->count, 1u);
+        if (arrived == gridDim.x - 1) {
+            gb->count = 0;                 // nobody arrives again before gen moves
+            __threadfence();
+            atomicAdd(&gb->gen, 1u);
+        } else {
+            long spins = 0;
+            while (*genp == g0) {
+                if (*abortp) break;
+                if (++spins > kBarSpinLimit) {
+                    atomicExch(&gb->abort, 1);
+                    break;
+                }
+                __nanosleep(64);
+            }
         }
-        cudaGraphSetConditional(h, go ? 1u : 0u);
+        __threadfence();
+        s_ok = (*abortp == 0);
+    }
+    __syncthreads();
+    return s_ok != 0;
+}
+
+template <typename T>
+__device__ __forceinline__ bool ph_apply(const Eng<T>& E, GridBar* gb, const T* in, T* out, T* tmp, int mode) {
+    ph_axsub(E, in, tmp);
+    if (!grid_sync(gb)) return false;
+    ph_sweep(E, 0, tmp, out);
+    if (!grid_sync(gb)) return false;
+    ph_sweep(E, 1, out, tmp);
+    if (!grid_sync(gb)) return false;
+    ph_sweep(E, 2, tmp, out);
+    if (!grid_sync(gb)) return false;
+    ph_sweep(E, 3, out, tmp);
+    if (!grid_sync(gb)) return false;
+    if (mode == 0) ph_sweep56<T, 0>(E, tmp, out);
+    if (mode == 1) ph_sweep56<T, 1>(E, tmp, out);
+    if (mode == 2) ph_sweep56<T, 2>(E, tmp, out);
+    return grid_sync(gb);
+}
+
+// init != 0: also run the start of PCGPME (b^ = PM W b, q = PM A x0, residuals)
+template <typename T, int MINB>
+__global__ void __launch_bounds__(kEngBlock, MINB) k_eng_loop(Eng<T> E, GridBar* gb, int init) {
+    if (init) {
+        // b^ = PM W b in place on p (sweeps p->t->q->t->q->p)
+        ph_sweep(E, 0, E.p, E.t);
+        if (!grid_sync(gb)) return;
+        ph_sweep(E, 1, E.t, E.q);
+        if (!grid_sync(gb)) return;
+        ph_sweep(E, 2, E.q, E.t);
+        if (!grid_sync(gb)) return;
+        ph_sweep(E, 3, E.t, E.q);
+        if (!grid_sync(gb)) return;
+        ph_sweep56<T, 0>(E, E.q, E.p);
+        if (!grid_sync(gb)) return;
+        if (!ph_apply(E, gb, E.xi, E.q, E.t, 0)) return;      // q = PM A x0
+        ph_initres(E);
+        if (!grid_sync(gb)) return;
+    }
+    const int cap = sld(E.ctrl + 1) + 2;
+    for (int body = 0;; body++) {
+        // every block reads the same flags: their last writers finished before
+        // the barrier that ended the previous iteration
+        int any = 0;
+        for (int m = 0; m < E.M; m++) any |= !sld(&E.S[m].done);
+        if (!any) break;
+        if (body >= cap) {                       // backstop: ITER bounds every member
+            if (blockIdx.x == 0 && threadIdx.x == 0)
+                for (int m = 0; m < E.M; m++)
+                    if (!sld(&E.S[m].done))
+                        stop_member(E.S + m, CLOWNS_STOP_MAXITER, sld(&E.S[m].mode) == 0 ? CLOWNS_IER_MAXITER : 0);
+            break;
+        }
+        if (!ph_apply(E, gb, E.p, E.q, E.t, 1)) return;       // q = PM A p ; ALP
+        ph_eupdate(E);                                        // e = r - ALP q
+        if (!grid_sync(gb)) return;
+        if (!ph_apply(E, gb, E.e, E.v, E.t, 2)) return;       // v = PM A e ; AMU
+        ph_xrupdate(E);                                       // x, r ; stop tests
+        if (!grid_sync(gb)) return;
+        ph_pupdate(E);                                        // p
+        if (!grid_sync(gb)) return;
     }
 }
 

@@ -94,3 +94,19 @@ extern "C" int clowns_apply_pm_a_dev(const double* al, int nl, int na, const int
     MemberIn in = member(al, nl, na, ll, d, n, x, const_cast<double*>(x));
     return engine_apply_pm_a(in, parm, x, y, work, work_bytes, (cudaStream_t)stream);
 }
+
+extern "C" int clowns_tuned_shape(int m, const int* n, int precision, int* block, int* grid, int* regs) {
+    if (m < 1 || !n || !block || !grid || !regs) {
+        set_last_error_msg("tuned_shape: invalid arguments");
+        return CLOWNS_ERR_ARG;
+    }
+    const int mixed = precision == CLOWNS_PREC_MIXED;
+    int minb = 0;
+    int rc = engine_tuned_shape(engine_row_space(m, n, mixed), mixed, block, grid, &minb);
+    if (rc) {
+        set_last_error_msg("tuned_shape: no solve of this size has run yet");
+        return rc;
+    }
+    *regs = minb == 4 ? 64 : 32;
+    return CLOWNS_OK;
+}

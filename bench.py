@@ -115,11 +115,13 @@ def barrier(world):
 
 
 def max_over_ranks(v: float, world: int) -> float:
+    """Slowest rank's time (the job's time).  CPU tensor under gloo."""
     if world <= 1:
         return v
     import torch
     import torch.distributed as dist
-    t = torch.tensor([v], dtype=torch.float64, device="cuda")
+    dev = "cpu" if dist.get_backend() == "gloo" else "cuda"
+    t = torch.tensor([v], dtype=torch.float64, device=dev)
     dist.all_reduce(t, op=dist.ReduceOp.MAX)
     return float(t.item())
 
@@ -194,6 +196,111 @@ def workload_case(pkg, name):
         nx, ny, nz = (int(v) for v in name.split("_")[1].split("x"))
         return wl.beach_case(nx, ny, nz, seed=1)
     raise SystemExit(f"unknown workload {name}")
+
+
+def run_ensemble(args):
+    """Batched ensemble (64 members, grids U[96,256] x U[96,192] x U[48,80], slopes
+    U(1/30,1/10), 0-40 obstacles, amplitudes U(0.01,0.1)): one batched mixed solve
+    and one batched FP64 solve against serial per-member launches of the plain
+    FP64 and mixed paths.  Prints one JSON line."""
+    import torch
+    pkg = ge.load_package()
+    pkg.build()
+    specs = pkg.workload.ensemble_members(n=args.members, seed=3, scale=args.member_scale)
+    systems, xs, sizes = [], [], []
+    t0 = time.perf_counter()
+    for sp in specs:
+        case = pkg.workload.ensemble_case(sp)
+        dc, ds = pkg.prepare_dev(case)
+        del dc
+        systems.append((ds.alu, ds.llu, ds.de, ds.b))
+        xs.append(torch.zeros(ds.mm2, dtype=torch.float64, device="cuda"))
+        sizes.append(ds.mnoe)
+    torch.cuda.synchronize()
+    t_gen = time.perf_counter() - t0
+    stream = torch.cuda.current_stream()
+    eps = 1e-10
+
+    def zero():
+        for x in xs:
+            x.zero_()
+
+    def serial(kind):
+        solvers = [pkg.Solver(n) if kind == "fp64" else pkg.MixedSolver(n) for n in sizes]
+
+        def run():
+            zero()
+            return [sv.solve(*sy, x, eps=eps) for sv, sy, x in zip(solvers, systems, xs)]
+        return run
+
+    def batched(prec):
+        bs = pkg.BatchedSolver(sizes, prec)
+
+        def run():
+            zero()
+            return bs.solve(systems, xs, eps=eps)
+        return run
+
+    out = {}
+    for name, fn in (("serial_fp64", serial("fp64")), ("serial_mixed", serial("mixed")),
+                     ("batched_fp64", batched(pkg.PREC_FP64)), ("batched_mixed", batched(pkg.PREC_MIXED))):
+        for _ in range(max(1, args.warmup)):
+            fn()
+        ms, res = time_device(fn, args.steps, stream)
+        infos = res[-1]
+        out[name] = {"ms_per_ensemble": ms / args.steps, "solves_per_s": len(sizes) * args.steps / (ms / 1000.0),
+                     "iters_total": int(sum(i.iter for i in infos)), "max_eps": max(i.eps for i in infos),
+                     "ier": sorted(set(int(i.ier) for i in infos))}
+    line = {"metric": "ensemble pressure solves/s", "unit": "solves/s", "members": len(sizes),
+            "rows_total": int(sum(sizes)), "rows_min": int(min(sizes)), "rows_max": int(max(sizes)),
+            "tol": eps, "generation_s": t_gen, "legs": out,
+            "batched_mixed_vs_serial_fp64": out["batched_mixed"]["solves_per_s"] / out["serial_fp64"]["solves_per_s"],
+            "batched_mixed_vs_serial_mixed": out["batched_mixed"]["solves_per_s"] / out["serial_mixed"]["solves_per_s"],
+            "batched_fp64_vs_serial_fp64": out["batched_fp64"]["solves_per_s"] / out["serial_fp64"]["solves_per_s"]}
+    print(json.dumps(line), flush=True)
+
+
+def run_adjoint(args):
+    """Adjoint on the 192x192x64 beach: J = sum of 16 seeded gauge pressures with
+    weights U(0.5,1.5); dJ/da for 200 seeded face fractions against central
+    differences at relative step 1e-6 (evaluated through the exact difference
+    identity) and dJ/db = lambda.  Prints one JSON line."""
+    import torch
+    sys.path.insert(0, str(ROOT / "tests"))
+    from adjoint_harness import PressureSolve, PressureSystem, central_difference, fd_faces, gauges
+    pkg = ge.load_package()
+    pkg.build()
+    case = pkg.workload.beach_192x192x64()
+    system = PressureSystem(case)
+    n = system.n
+    rows, w = gauges(n)
+    wt = torch.zeros(n, dtype=torch.float64, device="cuda")
+    wt[torch.from_numpy(rows).cuda()] = torch.from_numpy(w).cuda()
+    a0 = system.dc.a.clone()
+    a = a0.clone().requires_grad_(True)
+    b = system.b0[:n].clone().requires_grad_(True)
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    x = PressureSolve.apply(a, b, system)
+    J = (wt * x).sum()
+    J.backward()
+    torch.cuda.synchronize()
+    t_fwd_adj = time.perf_counter() - t0
+    ga = a.grad.cpu().numpy()
+    faces = fd_faces(system, count=args.faces)
+    fd, ad = [], []
+    t0 = time.perf_counter()
+    for owner, l in faces:
+        fd.append(central_difference(system, wt, a0, owner, l, x.detach()))
+        ad.append(ga[owner, l])
+    t_fd = time.perf_counter() - t0
+    fd, ad = np.array(fd), np.array(ad)
+    line = {"metric": "adjoint gradient vs central differences", "workload": "beach_192x192x64", "rows": n,
+            "faces": len(faces), "fd_step_rel": 1e-6,
+            "rel_l2_error": float(np.linalg.norm(ad - fd) / np.linalg.norm(fd)),
+            "max_rel_error_face": float(np.max(np.abs(ad - fd) / np.maximum(np.abs(fd), 1e-300))),
+            "forward_plus_adjoint_s": t_fwd_adj, "fd_s": t_fd}
+    print(json.dumps(line), flush=True)
 
 
 def run_gpu(args, world, rank, local):
@@ -330,7 +437,7 @@ def _report(pkg, args, world, rank, case, n, ms, infos, info, it, value, alg, ac
             err_mixed = float(np.linalg.norm(x_mixed - r.x) / nrm)
 
     if rank == 0:
-        launches_per_solve = 17 + 16 * it
+        launches_per_solve = 4          # init scalars, setup, persistent loop, copy-out
         line = {
             "metric": "pressure solves/s", "value": value, "unit": "solves/s", "n_gpus": world,
             "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms / args.steps,
@@ -348,6 +455,7 @@ def _report(pkg, args, world, rank, case, n, ms, infos, info, it, value, alg, ac
             "e2e": {"value": e2e_value, "unit": "solves/s", "h2d_bytes_per_step": h2d,
                     "d2h_bytes_per_step": d2h},
             "gpu_launches": args.steps * launches_per_solve,
+            "tuned_shape": {"fp64": pkg.tuned_shape([n], 0), "mixed": pkg.tuned_shape([n], 1)},
             "clocks": clk,
         }
         if minfo is not None:
@@ -370,11 +478,26 @@ def main():
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline leg")
     ap.add_argument("--legs", default="plain,mixed,e2e,cpu",
                     help="measurement legs to run (the plain FP64 leg always runs)")
+    ap.add_argument("--ensemble", action="store_true", help="batched ensemble measurement instead")
+    ap.add_argument("--members", type=int, default=64)
+    ap.add_argument("--member-scale", type=float, default=1.0)
+    ap.add_argument("--adjoint", action="store_true", help="adjoint vs finite differences instead")
+    ap.add_argument("--faces", type=int, default=200)
     ap.add_argument("--workload", default=WORKLOAD,
                     help="beach_256x256x96 (default), beach_512x384x128, beach_192x192x64, "
                          "tank_64x64x32 or beach_NXxNYxNZ")
     args = ap.parse_args()
     world, rank, local = dist_init()
+    if args.ensemble:
+        import torch
+        torch.cuda.set_device(local)
+        run_ensemble(args)
+        return
+    if args.adjoint:
+        import torch
+        torch.cuda.set_device(local)
+        run_adjoint(args)
+        return
     if args.impl == "reference":
         run_reference(args, world, rank)
     else:

@@ -162,6 +162,12 @@ int clowns_pcgpme_batched_dev(int m, const clowns_member* members, int precision
                               double parm, int iter, double inner_tol, int inner_max, int max_outer,
                               void* work, size_t work_bytes, void* stream, clowns_solve_info* infos);
 
+/* Launch shape the autotuner chose for the persistent iteration kernel of a row
+ * space (m systems of sizes n[], precision as above): threads per block, blocks
+ * (all co-resident) and the register budget per thread.  CLOWNS_ERR_ARG until a
+ * solve of that size has run. */
+int clowns_tuned_shape(int m, const int* n, int precision, int* block, int* grid, int* regs);
+
 /* Test hooks of the solve's building blocks (device pointers; workspace sized by
  * clowns_pcgpme_workspace_bytes(n, nl)).  clowns_pcgpme_setup_dev performs only
  * the row scaling and per-row sort of pcgpme_para.F90:77-112 and copies the
@@ -286,6 +292,39 @@ int clowns_face_grad_dev(const int* dims, int inne, int inne2, int ifln, const i
 int clowns_pcgpme_static_dev(const double* al, int nl, int na, const int* ll, const double* d,
                              int n, const double* b, double* x, double eps, double parm, int iter,
                              void* stream, clowns_solve_info* info);
+
+/* ========================================================================== */
+/* Device-resident pressure-correction loop of one domain                     */
+/* ========================================================================== */
+
+/* The ik loop of cal_momentum (src2LOWNS/1sub-momentum.F90:41-60) with the
+ * domain's module arrays kept in HBM: cal_err_of_continuity, check_dmax,
+ * cal_matrix_element, cal_poisson_equation, p -= xe and estimate_velocity2, with
+ * one host read-back of dmax per ik.  Host arrays in the reference layouts; the
+ * session owns its device memory. */
+typedef struct clowns_session clowns_session;
+
+/* Static grid: dims, mn, in/jn/kn, x, dx, objno (uploaded once). */
+int clowns_session_create(clowns_session** s, const int* dims, int inne, int inne2, int mx2,
+                          const int* mn, const int* in_, const int* jn, const int* kn,
+                          const double* x, const double* dx, const int* objno);
+/* Fields of the current step: nff%f, nff%b, f, fb, a, un, sp, p. */
+int clowns_session_set_fields(clowns_session* s, const int* nf, const int* nfb, const double* f,
+                              const double* fb, const double* a, const double* un,
+                              const double* sp, const double* p);
+/* set_nflag (every step) and, on the first call, init_matrix; sizes the
+ * matrix rows to ifln + 5000 as the reference does. */
+int clowns_session_classify(clowns_session* s, int* ifln, int* isfn);
+/* The ik loop until dmax < d0 or ik > 1000 or a solver failure.  Returns ik and
+ * dmax at exit, the last solve's iteration count and ERR, and icon as the
+ * reference's caller sets it (0, 12, 96, 911 or 1030). */
+int clowns_session_pressure_loop(clowns_session* s, double dt, double d0, double eps0,
+                                 int precision, int* ik, double* dmax, int* iter, double* err,
+                                 int* icon);
+/* Read back nff%f, nff%b, f, p, un (any may be NULL) and mnoe. */
+int clowns_session_get_fields(clowns_session* s, int* nf, int* nfb, double* f, double* p,
+                              double* un, int* mnoe);
+int clowns_session_destroy(clowns_session* s);
 
 #ifdef __cplusplus
 }

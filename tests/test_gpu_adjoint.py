@@ -100,11 +100,13 @@ def test_adjoint_matches_cpu_transposed_solve(gpu, ora, bore):
 
 def test_adjoint_matches_finite_differences(gpu, bore):
     """Central differences with relative step 1e-6 on 40 seeded face fractions,
-    through the autograd wrapper.  The perturbed solves start from the
-    unperturbed pressure and are refined on the true FP64 residual down to the
-    FP64 floor; J(+) - J(-) is formed as w.(x+ - x-) to avoid cancellation."""
+    through the autograd wrapper.  The difference quotient is evaluated through
+    the exact identity x(a+h) - x(a-h) = -A(a+h)^-1 [A(a+h) - A(a-h)] x(a-h)
+    (see adjoint_harness.central_difference): two perturbed assemblies, a solve
+    at a-h refined to the FP64 floor and a solve for the difference.  Also a
+    plain two-solve difference, which FP64 resolution limits to ~1e-5."""
     import torch
-    from adjoint_harness import PressureSolve, PressureSystem, fd_faces, gauges
+    from adjoint_harness import PressureSolve, PressureSystem, central_difference, fd_faces, gauges
     system = PressureSystem(bore)
     n = system.n
     rows, w = gauges(n)
@@ -120,8 +122,9 @@ def test_adjoint_matches_finite_differences(gpu, bore):
     faces = fd_faces(system, count=40)
     assert len(faces) >= 20
     x0 = x.detach()
-    fd, ad = [], []
+    fd, fd2, ad = [], [], []
     for owner, l in faces:
+        fd.append(central_difference(system, wt, a0, owner, l, x0))
         h = 1e-6 * float(a0[owner, l])
         xs = []
         for sgn in (1.0, -1.0):
@@ -130,21 +133,16 @@ def test_adjoint_matches_finite_differences(gpu, bore):
             system.assemble(ap)
             xsol, info = system.solve_refined(system.b0, x0)
             xs.append(xsol)
-        fd.append(float((wt * (xs[0] - xs[1])).sum()) / (2 * h))
+        fd2.append(float((wt * (xs[0] - xs[1])).sum()) / (2 * h))
         ad.append(ga[owner, l])
-    fd, ad = np.array(fd), np.array(ad)
-    assert np.linalg.norm(ad - fd) <= 1e-6 * np.linalg.norm(fd), (np.abs(ad - fd) / np.abs(fd)).max()
-    # dJ/db = lambda: one directional check
+    fd, fd2, ad = np.array(fd), np.array(fd2), np.array(ad)
+    assert np.linalg.norm(ad - fd) <= 1e-6 * np.linalg.norm(fd), np.linalg.norm(ad - fd) / np.linalg.norm(fd)
+    assert np.linalg.norm(ad - fd2) <= 1e-4 * np.linalg.norm(fd2)
+    # dJ/db = lambda along a random direction: x(b+hv) - x(b-hv) = A^-1 (2 h v) exactly
+    system.assemble(a0)
     rng = np.random.default_rng(2)
     v = torch.from_numpy(rng.standard_normal(n)).cuda()
-    system.assemble(a0)
-    hb = 1e-6 * float(system.b0[:n].abs().max())
-    bp = system.b0.clone()
-    bp[:n] += hb * v
-    bm = system.b0.clone()
-    bm[:n] -= hb * v
-    xp, _ = system.solve_refined(bp, x0)
-    xm, _ = system.solve_refined(bm, x0)
-    fdb = float((wt * (xp - xm)).sum()) / (2 * hb)
-    adb = float((b.grad * v).sum())
-    assert abs(fdb - adb) <= 1e-6 * abs(adb)
+    rhs = torch.zeros(system.sy.mm2, dtype=torch.float64, device="cuda")
+    rhs[:n] = v
+    dxv, _ = system.solve(rhs, eps=1e-13)
+    assert abs(float((wt * dxv).sum()) - float((b.grad * v).sum())) <= 1e-8 * abs(float((b.grad * v).sum()))
