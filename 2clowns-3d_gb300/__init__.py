@@ -94,6 +94,7 @@ _SIGS = {
                                            C.c_void_p, C.c_void_p, C.c_double, C.c_double, C.c_int,
                                            C.c_void_p, C.c_void_p]),
     "clowns_tuned_shape": (C.c_int, [C.c_int, C.c_void_p, C.c_int, C.c_void_p, C.c_void_p, C.c_void_p]),
+    "clowns_last_kernel_launches": (C.c_long, []),
     "clowns_session_create": (C.c_int, [C.c_void_p, C.c_void_p, C.c_int, C.c_int, C.c_int] + [C.c_void_p] * 7),
     "clowns_session_set_fields": (C.c_int, [C.c_void_p] * 9),
     "clowns_session_classify": (C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p]),
@@ -340,7 +341,15 @@ def tuned_shape(sizes, precision=0):
     b, g, r = C.c_int(0), C.c_int(0), C.c_int(0)
     if L.clowns_tuned_shape(len(sizes), arr, precision, C.byref(b), C.byref(g), C.byref(r)) != 0:
         return None
-    return {"block": b.value, "grid": g.value, "registers": r.value}
+    if g.value == 0:
+        return {"mode": "graph", "block": b.value}
+    return {"mode": "persistent", "block": b.value, "grid": g.value, "registers": r.value}
+
+
+def last_kernel_launches():
+    """Kernels the calling thread's last solve launched (host launches plus the
+    kernel nodes executed inside loop graphs)."""
+    return int(lib().clowns_last_kernel_launches())
 
 
 class Member(C.Structure):

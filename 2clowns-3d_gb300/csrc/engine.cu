@@ -5,6 +5,7 @@
 // (FP32 storage, FP64 iterative refinement).
 #include <algorithm>
 #include <cmath>
+#include <cstdlib>
 #include <cstring>
 #include <map>
 #include <mutex>
@@ -175,8 +176,9 @@ __global__ void __launch_bounds__(kEngBlock) k_mx_update(Eng<T> E) {
     }
 }
 
+// ctrl[2] accumulates the loop bodies of earlier sweeps.
 __global__ void k_mx_reset_ctrl(int* ctrl, int inner_max) {
-    if (threadIdx.x == 0 && blockIdx.x == 0) { ctrl[0] = 0; ctrl[1] = inner_max; }
+    if (threadIdx.x == 0 && blockIdx.x == 0) { ctrl[2] += ctrl[0]; ctrl[0] = 0; ctrl[1] = inner_max; }
 }
 
 template <typename T>
@@ -198,7 +200,7 @@ __global__ void k_mixed_init_scalars(MemberScalars* S, int M, double eps, int oi
         z.mode = 1;
         S[m] = z;
     }
-    if (threadIdx.x == 0) { ctrl[0] = 0; ctrl[1] = 0; }
+    if (threadIdx.x == 0) { ctrl[0] = 0; ctrl[1] = 0; ctrl[2] = 0; }
 }
 
 // Export of the scaled/sorted matrix (test hook), member 0 only.
@@ -218,10 +220,17 @@ __global__ void k_eng_export(Eng<T> E, double* al_s, int* ll_s, double* d_s, dou
 // ---------------------------------------------------------------------------
 // Layout
 
+// Reduction groups of a member of n rows: kGroupTiles consecutive tiles each.
+static inline int member_groups(int n) {
+    const int nblk = (n + kTile - 1) / kTile;
+    return (nblk + kGroupTiles - 1) / kGroupTiles;
+}
+
 struct EngLayout {
     long NV = 0;
-    int M = 0, nblk = 0, mixed = 0, tsize = 8;
+    int M = 0, nblk = 0, ngrp = 0, mixed = 0, tsize = 8;
     size_t o_blk_member, o_blk_rows, o_mem_off, o_mem_n, o_mem_nblk, o_mem_blk0, o_ticket, o_ctrl;
+    size_t o_blk_group, o_grp_blk0, o_grp_nblk, o_mem_grp0, o_mem_ngrp, o_gticket, o_gpartials;
     size_t o_in, o_S, o_partials, o_bar, o_al, o_ll, o_d, o_vec[8], o_W, o_x64, o_r64, o_s64, o_t64;
     size_t total = 0;
 };
@@ -232,9 +241,14 @@ static EngLayout eng_layout(int M, const int* n, int mixed) {
     L.mixed = mixed;
     L.tsize = mixed ? 4 : 8;
     long NV = 0;
-    for (int m = 0; m < M; m++) NV += (long)align_up((size_t)n[m] + 1, kTile);
+    int ngrp = 0;
+    for (int m = 0; m < M; m++) {
+        NV += (long)align_up((size_t)n[m] + 1, kTile);
+        ngrp += member_groups(n[m]);
+    }
     L.NV = NV;
     L.nblk = (int)(NV / kTile);
+    L.ngrp = ngrp;
     size_t o = 0;
     auto take = [&](size_t bytes) { size_t at = o; o = align_up(o + (bytes ? bytes : 1), 256); return at; };
     L.o_blk_member = take(sizeof(int) * L.nblk);
@@ -244,6 +258,13 @@ static EngLayout eng_layout(int M, const int* n, int mixed) {
     L.o_mem_nblk = take(sizeof(int) * M);
     L.o_mem_blk0 = take(sizeof(int) * M);
     L.o_ticket = take(sizeof(unsigned) * M);
+    L.o_blk_group = take(sizeof(int) * L.nblk);
+    L.o_grp_blk0 = take(sizeof(int) * ngrp);
+    L.o_grp_nblk = take(sizeof(int) * ngrp);
+    L.o_mem_grp0 = take(sizeof(int) * M);
+    L.o_mem_ngrp = take(sizeof(int) * M);
+    L.o_gticket = take(sizeof(unsigned) * ngrp);
+    L.o_gpartials = take(sizeof(double) * 2 * ngrp);
     L.o_ctrl = take(sizeof(int) * 8);
     L.o_in = take(sizeof(MemberIn) * M);
     L.o_S = take(sizeof(MemberScalars) * M);
@@ -280,6 +301,13 @@ static Eng<T> eng_bind(void* work, const EngLayout& L) {
     E.mem_nblk = (const int*)(b + L.o_mem_nblk);
     E.mem_blk0 = (const int*)(b + L.o_mem_blk0);
     E.ticket = (unsigned*)(b + L.o_ticket);
+    E.blk_group = (const int*)(b + L.o_blk_group);
+    E.grp_blk0 = (const int*)(b + L.o_grp_blk0);
+    E.grp_nblk = (const int*)(b + L.o_grp_nblk);
+    E.mem_grp0 = (const int*)(b + L.o_mem_grp0);
+    E.mem_ngrp = (const int*)(b + L.o_mem_ngrp);
+    E.gticket = (unsigned*)(b + L.o_gticket);
+    E.gpartials = (double*)(b + L.o_gpartials);
     E.ctrl = (int*)(b + L.o_ctrl);
     E.in = (const MemberIn*)(b + L.o_in);
     E.S = (MemberScalars*)(b + L.o_S);
@@ -302,6 +330,24 @@ static Eng<T> eng_bind(void* work, const EngLayout& L) {
     return E;
 }
 
+// Reduction-group tables: group q of member m covers its real tiles
+// blk0 + q*kGroupTiles .. (at most kGroupTiles of them).  Callers size the
+// arrays: blk_group[nblk] (pre-filled with -1), grp_blk0/grp_nblk[ngrp],
+// mem_grp0/mem_ngrp[M].
+static void fill_groups(int M, const int* blk0, const int* nblk, int* blk_group, int* grp_blk0, int* grp_nblk,
+                        int* mem_grp0, int* mem_ngrp) {
+    int g = 0;
+    for (int m = 0; m < M; m++) {
+        mem_grp0[m] = g;
+        mem_ngrp[m] = (nblk[m] + kGroupTiles - 1) / kGroupTiles;
+        for (int q = 0; q < mem_ngrp[m]; q++, g++) {
+            grp_blk0[g] = blk0[m] + q * kGroupTiles;
+            grp_nblk[g] = std::min(kGroupTiles, nblk[m] - q * kGroupTiles);
+            for (int t = 0; t < grp_nblk[g]; t++) blk_group[grp_blk0[g] + t] = g;
+        }
+    }
+}
+
 // Upload the member tables (static for a given layout) and the input table.
 static int eng_upload_tables(void* work, const EngLayout& L, const int* n, const MemberIn* ins,
                              cudaStream_t s) {
@@ -321,7 +367,10 @@ static int eng_upload_tables(void* work, const EngLayout& L, const int* n, const
         }
         o += R;
     }
-    std::vector<unsigned> zeros(M, 0u);
+    std::vector<int> blk_group(L.nblk, -1), grp_blk0(L.ngrp), grp_nblk(L.ngrp), mem_grp0(M), mem_ngrp(M);
+    fill_groups(M, blk0.data(), nblk.data(), blk_group.data(), grp_blk0.data(), grp_nblk.data(), mem_grp0.data(),
+                mem_ngrp.data());
+    std::vector<unsigned> zeros(std::max(M, L.ngrp), 0u);
     char* b = (char*)work;
     CLOWNS_CUDA_TRY(cudaMemcpyAsync(b + L.o_blk_member, blk_member.data(), sizeof(int) * L.nblk, cudaMemcpyHostToDevice, s));
     CLOWNS_CUDA_TRY(cudaMemcpyAsync(b + L.o_blk_rows, blk_rows.data(), sizeof(int) * L.nblk, cudaMemcpyHostToDevice, s));
@@ -330,6 +379,12 @@ static int eng_upload_tables(void* work, const EngLayout& L, const int* n, const
     CLOWNS_CUDA_TRY(cudaMemcpyAsync(b + L.o_mem_nblk, nblk.data(), sizeof(int) * M, cudaMemcpyHostToDevice, s));
     CLOWNS_CUDA_TRY(cudaMemcpyAsync(b + L.o_mem_blk0, blk0.data(), sizeof(int) * M, cudaMemcpyHostToDevice, s));
     CLOWNS_CUDA_TRY(cudaMemcpyAsync(b + L.o_ticket, zeros.data(), sizeof(unsigned) * M, cudaMemcpyHostToDevice, s));
+    CLOWNS_CUDA_TRY(cudaMemcpyAsync(b + L.o_blk_group, blk_group.data(), sizeof(int) * L.nblk, cudaMemcpyHostToDevice, s));
+    CLOWNS_CUDA_TRY(cudaMemcpyAsync(b + L.o_grp_blk0, grp_blk0.data(), sizeof(int) * L.ngrp, cudaMemcpyHostToDevice, s));
+    CLOWNS_CUDA_TRY(cudaMemcpyAsync(b + L.o_grp_nblk, grp_nblk.data(), sizeof(int) * L.ngrp, cudaMemcpyHostToDevice, s));
+    CLOWNS_CUDA_TRY(cudaMemcpyAsync(b + L.o_mem_grp0, mem_grp0.data(), sizeof(int) * M, cudaMemcpyHostToDevice, s));
+    CLOWNS_CUDA_TRY(cudaMemcpyAsync(b + L.o_mem_ngrp, mem_ngrp.data(), sizeof(int) * M, cudaMemcpyHostToDevice, s));
+    CLOWNS_CUDA_TRY(cudaMemcpyAsync(b + L.o_gticket, zeros.data(), sizeof(unsigned) * L.ngrp, cudaMemcpyHostToDevice, s));
     CLOWNS_CUDA_TRY(cudaMemcpyAsync(b + L.o_in, ins, sizeof(MemberIn) * M, cudaMemcpyHostToDevice, s));
     CLOWNS_CUDA_TRY(cudaStreamSynchronize(s));
     return CLOWNS_OK;
@@ -432,13 +487,34 @@ static Shape autotune(const Eng<T>& E, long key_nv, int key_prec, cudaStream_t s
 }
 
 // ---------------------------------------------------------------------------
-// Persistent loop launch (cooperative: all blocks co-resident)
+// The iteration loop, executed one of two ways (the autotuner times both on the
+// actual row space and keeps the faster):
+//   persistent: one cooperative launch of k_eng_loop; phases separated by grid
+//               barriers (no launch gaps, static tile assignment);
+//   graph:      a CUDA graph whose WHILE node repeats the iteration's kernels,
+//               chained by programmatic dependent launch (dynamic scheduling,
+//               full occupancy, launch latency overlapped with the previous
+//               kernel's tail).
 
 struct LoopShape {
     int block = kStepBlock;
     int grid = 0;
     int minb = 8;     // register budget of the loop kernel: 8 -> 32, 4 -> 64 registers
+    int graph = 0;    // 1: run the loop as a CUDA graph; 2: host-launched kernels
 };
+
+// CLOWNS_LOOP_MODE=graph|persistent|launch forces one execution of the loop
+// ("launch": the iteration's kernels launched from the host, eight iterations
+// between polls of the stop flags -- the same kernels, visible one by one to a
+// profiler); unset or "auto": the autotuner decides.
+static int forced_loop_mode() {
+    const char* v = getenv("CLOWNS_LOOP_MODE");
+    if (!v || !*v || !strcmp(v, "auto")) return -1;
+    if (!strcmp(v, "persistent")) return 0;
+    if (!strcmp(v, "graph")) return 1;
+    if (!strcmp(v, "launch")) return 2;
+    return -1;
+}
 
 template <typename T>
 static const void* loop_fn(int minb) {
@@ -458,12 +534,189 @@ static int loop_max_grid(int block, int minb, int* out) {
     return CLOWNS_OK;
 }
 
+// Kernel launch with optional programmatic serialization (captured as a
+// programmatic edge inside a graph).
+template <typename... KArgs, typename... Args>
+static void klaunch(bool pdl, void (*kern)(KArgs...), int grid, int block, cudaStream_t s, Args... args) {
+    cudaLaunchConfig_t cfg = {};
+    cfg.gridDim = dim3(grid);
+    cfg.blockDim = dim3(block);
+    cfg.dynamicSmemBytes = 0;
+    cfg.stream = s;
+    cudaLaunchAttribute at[1];
+    if (pdl) {
+        at[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
+        at[0].val.programmaticStreamSerializationAllowed = 1;
+        cfg.attrs = at;
+        cfg.numAttrs = 1;
+    }
+    cudaLaunchKernelEx(&cfg, kern, args...);
+}
+
 template <typename T>
-static int launch_loop(Eng<T> E, GridBar* gb, int init, const LoopShape& sh, cudaStream_t s) {
+static void g_apply(bool pdl, const Eng<T>& E, const Shape& sh, const T* in, T* out, T* tmp, int mode,
+                    cudaStream_t s) {
+    const int g = grid_of(sh, E.nblk), b = sh.block;
+    klaunch(pdl, k_eng_axsub<T>, g, b, s, E, in, tmp);
+    klaunch(pdl, k_eng_sweep<T>, g, b, s, E, 0, (const T*)tmp, out);
+    klaunch(pdl, k_eng_sweep<T>, g, b, s, E, 1, (const T*)out, tmp);
+    klaunch(pdl, k_eng_sweep<T>, g, b, s, E, 2, (const T*)tmp, out);
+    klaunch(pdl, k_eng_sweep<T>, g, b, s, E, 3, (const T*)out, tmp);
+    if (mode == 0) klaunch(pdl, k_eng_sweep56<T, 0>, g, b, s, E, (const T*)tmp, out);
+    if (mode == 1) klaunch(pdl, k_eng_sweep56<T, 1>, g, b, s, E, (const T*)tmp, out);
+    if (mode == 2) klaunch(pdl, k_eng_sweep56<T, 2>, g, b, s, E, (const T*)tmp, out);
+}
+
+template <typename T>
+static void g_iteration(bool pdl, const Eng<T>& E, const Shape& sh, cudaStream_t s) {
+    const int g = grid_of(sh, E.nblk), b = sh.block;
+    g_apply(pdl, E, sh, (const T*)E.p, E.q, E.t, 1, s);
+    klaunch(pdl, k_eng_eupdate<T>, g, b, s, E);
+    g_apply(pdl, E, sh, (const T*)E.e, E.v, E.t, 2, s);
+    klaunch(pdl, k_eng_xrupdate<T>, g, b, s, E);
+    klaunch(pdl, k_eng_pupdate<T>, g, b, s, E);
+}
+
+// Graph cache: one instantiated loop graph per (workspace, row space, precision)
+struct GraphKey {
+    const void* work;
+    long NV;
+    int M, prec;
+    bool operator<(const GraphKey& o) const {
+        return std::tie(work, NV, M, prec) < std::tie(o.work, o.NV, o.M, o.prec);
+    }
+};
+static std::mutex g_graph_mu;
+static std::map<GraphKey, cudaGraphExec_t> g_graphs;
+static cudaStream_t g_cap = nullptr;
+
+void release_all_graphs() {
+    std::lock_guard<std::mutex> lk(g_graph_mu);
+    for (auto& kv : g_graphs) cudaGraphExecDestroy(kv.second);
+    g_graphs.clear();
+}
+
+void release_graphs_for(const void* work) {
+    std::lock_guard<std::mutex> lk(g_graph_mu);
+    for (auto it = g_graphs.begin(); it != g_graphs.end();) {
+        if (it->first.work == work) {
+            cudaGraphExecDestroy(it->second);
+            it = g_graphs.erase(it);
+        } else {
+            ++it;
+        }
+    }
+}
+
+// WHILE { iteration ; guard } captured into a fresh graph
+template <typename T>
+static int build_loop_graph(const Eng<T>& E, bool pdl, cudaGraphExec_t* out) {
+    if (!g_cap) CLOWNS_CUDA_TRY(cudaStreamCreateWithFlags(&g_cap, cudaStreamNonBlocking));
+    cudaGraph_t graph;
+    CLOWNS_CUDA_TRY(cudaGraphCreate(&graph, 0));
+    cudaGraphConditionalHandle h;
+    CLOWNS_CUDA_TRY(cudaGraphConditionalHandleCreate(&h, graph, 1, cudaGraphCondAssignDefault));
+    cudaGraphNodeParams cp = {cudaGraphNodeTypeConditional};
+    cp.conditional.handle = h;
+    cp.conditional.type = cudaGraphCondTypeWhile;
+    cp.conditional.size = 1;
+    cudaGraphNode_t cnode;
+    CLOWNS_CUDA_TRY(cudaGraphAddNode(&cnode, graph, nullptr, nullptr, 0, &cp));
+    cudaGraph_t body = cp.conditional.phGraph_out[0];
+    CLOWNS_CUDA_TRY(cudaStreamBeginCaptureToGraph(g_cap, body, nullptr, nullptr, 0, cudaStreamCaptureModeThreadLocal));
+    const Shape sh;
+    g_iteration(pdl, E, sh, g_cap);
+    klaunch(pdl, k_eng_guard, 1, 256, g_cap, E.S, E.M, E.ctrl, h);
+    cudaGraph_t captured;
+    cudaError_t ec = cudaStreamEndCapture(g_cap, &captured);
+    if (ec != cudaSuccess) {
+        cudaGetLastError();
+        cudaGraphDestroy(graph);
+        set_last_error(ec, "capture of the iteration graph", __FILE__, __LINE__);
+        return CLOWNS_ERR_CUDA;
+    }
+    cudaGraphExec_t ex;
+    cudaError_t ei = cudaGraphInstantiate(&ex, graph, 0);
+    cudaGraphDestroy(graph);
+    if (ei != cudaSuccess) {
+        cudaGetLastError();
+        set_last_error(ei, "instantiation of the iteration graph", __FILE__, __LINE__);
+        return CLOWNS_ERR_CUDA;
+    }
+    *out = ex;
+    return CLOWNS_OK;
+}
+
+template <typename T>
+static int loop_graph(const Eng<T>& E, const void* work, int prec, cudaGraphExec_t* out) {
+    std::lock_guard<std::mutex> lk(g_graph_mu);
+    GraphKey key{work, E.NV, E.M, prec};
+    auto it = g_graphs.find(key);
+    if (it != g_graphs.end()) { *out = it->second; return CLOWNS_OK; }
+    cudaGraphExec_t ex;
+    int rc = build_loop_graph(E, true, &ex);              // programmatic edges
+    if (rc) rc = build_loop_graph(E, false, &ex);         // plain edges if refused
+    if (rc) return rc;
+    if (g_graphs.size() >= 64) {
+        cudaGraphExecDestroy(g_graphs.begin()->second);
+        g_graphs.erase(g_graphs.begin());
+    }
+    g_graphs[key] = ex;
+    *out = ex;
+    return CLOWNS_OK;
+}
+
+// Kernels the calling thread's last solve launched (host launches plus the
+// kernel nodes executed inside loop graphs).
+static thread_local long t_launches = 0;
+constexpr int kIterKernels = 15;    // two operator applications (6 each) + 3 vector updates
+constexpr int kBodyKernels = kIterKernels + 1;   // + the loop guard
+
+// Kernel launches of one run_loop call, given the loop bodies it executed.
+static long loop_launches(const LoopShape& sh, long bodies) {
+    if (sh.graph == 1) return bodies * kBodyKernels;
+    if (sh.graph == 2) return bodies * kIterKernels;
+    return 1;
+}
+
+template <typename T>
+static int run_loop(Eng<T> E, const void* work, GridBar* gb, int prec, const LoopShape& sh, cudaStream_t s) {
+    if (sh.graph == 2) {
+        CLOWNS_CUDA_TRY(cudaMemsetAsync(gb, 0, sizeof(GridBar), s));
+        const Shape ksh;
+        int cap = 0;
+        CLOWNS_CUDA_TRY(cudaMemcpyAsync(&cap, E.ctrl + 1, sizeof(int), cudaMemcpyDeviceToHost, s));
+        CLOWNS_CUDA_TRY(cudaStreamSynchronize(s));
+        std::vector<MemberScalars> h(E.M);
+        for (long body = 0; body <= (long)cap + 16; body += 8) {
+            for (int k = 0; k < 8; k++) g_iteration(false, E, ksh, s);
+            CLOWNS_CUDA_TRY(cudaGetLastError());
+            CLOWNS_CUDA_TRY(cudaMemcpyAsync(h.data(), E.S, sizeof(MemberScalars) * E.M, cudaMemcpyDeviceToHost, s));
+            CLOWNS_CUDA_TRY(cudaStreamSynchronize(s));
+            bool any = false;
+            for (int m = 0; m < E.M; m++) any = any || !h[m].done;
+            if (!any) {
+                t_launches += loop_launches(sh, body + 8);
+                return CLOWNS_OK;
+            }
+        }
+        set_last_error_msg("pcgpme: stop flags not raised after ITER iterations");
+        return CLOWNS_ERR_NOCONV;
+    }
+    if (sh.graph) {
+        cudaGraphExec_t ex;
+        int rc = loop_graph(E, work, prec, &ex);
+        if (rc) return rc;
+        CLOWNS_CUDA_TRY(cudaMemsetAsync(gb, 0, sizeof(GridBar), s));
+        CLOWNS_CUDA_TRY(cudaGraphLaunch(ex, s));
+        return CLOWNS_OK;     // bodies are counted from ctrl[0] + ctrl[2] after the solve
+    }
     int grid = std::max(1, std::min(sh.grid, E.nblk));
     CLOWNS_CUDA_TRY(cudaMemsetAsync(gb, 0, sizeof(GridBar), s));
+    int init = 0;
     void* args[] = {(void*)&E, (void*)&gb, (void*)&init};
     CLOWNS_CUDA_TRY(cudaLaunchCooperativeKernel(loop_fn<T>(sh.minb), dim3(grid), dim3(sh.block), args, 0, s));
+    t_launches += 1;
     return CLOWNS_OK;
 }
 
@@ -478,31 +731,43 @@ static int check_abort(GridBar* gb, cudaStream_t s) {
     return CLOWNS_OK;
 }
 
-// Autotuner: time a few iterations of the persistent loop for candidate block
-// and grid sizes on the actual row space; the fastest shape is cached per
-// (row-space size, precision).  `prime` re-creates the state a loop starts from.
+// Autotuner: time eight iterations of the loop for each candidate -- the
+// persistent kernel at two register budgets and three grid sizes, and the
+// graph -- on the actual row space; cache the fastest per (row-space size,
+// precision).  `prime` re-creates the state the loop starts from.
 template <typename T, typename Prime>
-static int tune_loop(Eng<T> E, GridBar* gb, long key_nv, int key_prec, int init, Prime prime, cudaStream_t s,
-                     LoopShape* out) {
+static int tune_loop(Eng<T> E, const void* work, GridBar* gb, long key_nv, int key_prec, Prime prime,
+                     cudaStream_t s, LoopShape* out) {
+    const int forced = forced_loop_mode();
+    if (forced == 1 || forced == 2) {
+        LoopShape sh;
+        sh.graph = forced;
+        *out = sh;
+        return CLOWNS_OK;
+    }
     {
         std::lock_guard<std::mutex> lk(g_loop_mu);
         auto it = g_loop_shapes.find({key_nv, key_prec});
         if (it != g_loop_shapes.end()) { *out = it->second; return CLOWNS_OK; }
     }
     std::vector<LoopShape> cands;
-    for (int minb : {8, 4})
-        for (int b : {kStepBlock}) {
-            int gmax = 0;
-            int rc = loop_max_grid<T>(b, minb, &gmax);
-            if (rc) return rc;
-            for (int frac : {4, 3, 2}) {
-                LoopShape sh;
-                sh.block = b;
-                sh.minb = minb;
-                sh.grid = std::max(1, gmax * frac / 4);
-                cands.push_back(sh);
-            }
+    for (int minb : {8, 4}) {
+        int gmax = 0;
+        int rc = loop_max_grid<T>(kStepBlock, minb, &gmax);
+        if (rc) return rc;
+        for (int frac : {4, 3, 2}) {
+            LoopShape sh;
+            sh.block = kStepBlock;
+            sh.minb = minb;
+            sh.grid = std::max(1, gmax * frac / 4);
+            cands.push_back(sh);
         }
+    }
+    if (forced != 0) {
+        LoopShape gsh;
+        gsh.graph = 1;
+        cands.push_back(gsh);
+    }
     cudaEvent_t e0, e1;
     CLOWNS_CUDA_TRY(cudaEventCreate(&e0));
     CLOWNS_CUDA_TRY(cudaEventCreate(&e1));
@@ -510,18 +775,19 @@ static int tune_loop(Eng<T> E, GridBar* gb, long key_nv, int key_prec, int init,
     float best_ms = 1e30f;
     for (const LoopShape& sh : cands) {
         float ms = 0.f;
-        for (int rep = 0; rep < 2; rep++) {
+        bool ok = true;
+        for (int rep = 0; rep < 2 && ok; rep++) {
             prime(s);
             CLOWNS_CUDA_TRY(cudaEventRecord(e0, s));
-            int rc = launch_loop(E, gb, init, sh, s);
-            if (rc) return rc;
+            int rc = run_loop(E, work, gb, key_prec, sh, s);
+            if (rc) { ok = false; break; }
             CLOWNS_CUDA_TRY(cudaEventRecord(e1, s));
             CLOWNS_CUDA_TRY(cudaEventSynchronize(e1));
             CLOWNS_CUDA_TRY(cudaEventElapsedTime(&ms, e0, e1));
             int rc2 = check_abort(gb, s);
             if (rc2) return rc2;
         }
-        if (ms < best_ms) { best_ms = ms; best = sh; }
+        if (ok && ms < best_ms) { best_ms = ms; best = sh; }
     }
     cudaEventDestroy(e0);
     cudaEventDestroy(e1);
@@ -536,15 +802,14 @@ int engine_tuned_shape(long nv, int prec, int* block, int* grid, int* minb) {
     auto it = g_loop_shapes.find({nv, prec});
     if (it == g_loop_shapes.end()) return CLOWNS_ERR_ARG;
     *block = it->second.block;
-    *grid = it->second.grid;
-    *minb = it->second.minb;
+    *grid = it->second.graph ? 0 : it->second.grid;
+    *minb = it->second.graph ? 0 : it->second.minb;
     return CLOWNS_OK;
 }
 
 long engine_row_space(int M, const int* n, int mixed) { return eng_layout(M, n, mixed).NV; }
 
-void release_all_graphs() {}
-void release_graphs_for(const void*) {}
+long engine_last_launches() { return t_launches; }
 
 // ---------------------------------------------------------------------------
 // Solves
@@ -559,11 +824,17 @@ static void params(int n, double eps, double parm, int iter, double* eps_o, int*
     *P2 = p1 + 1.0;
 }
 
-static int read_infos(void* work, const EngLayout& L, cudaStream_t s, clowns_solve_info* info, int mixed) {
+// Per-member results; also adds the kernel nodes executed by loop graphs
+// (16 per body, ctrl[0] + ctrl[2] bodies) to the launch count.
+static int read_infos(void* work, const EngLayout& L, cudaStream_t s, clowns_solve_info* info, int mixed,
+                      const LoopShape& sh) {
     std::vector<MemberScalars> h(L.M);
+    int ctrl[8];
     CLOWNS_CUDA_TRY(cudaMemcpyAsync(h.data(), (char*)work + L.o_S, sizeof(MemberScalars) * L.M,
                                     cudaMemcpyDeviceToHost, s));
+    CLOWNS_CUDA_TRY(cudaMemcpyAsync(ctrl, (char*)work + L.o_ctrl, sizeof(ctrl), cudaMemcpyDeviceToHost, s));
     CLOWNS_CUDA_TRY(cudaStreamSynchronize(s));
+    if (sh.graph == 1) t_launches += loop_launches(sh, (long)ctrl[0] + ctrl[2]);
     if (!info) return CLOWNS_OK;
     for (int m = 0; m < L.M; m++) {
         clowns_solve_info& o = info[m];
@@ -637,19 +908,30 @@ int engine_solve_plain(int M, const MemberIn* ins, double eps, double parm, int 
         if (nl == 6) k_eng_setup<double, 6><<<gs, kEngBlock, 0, cs>>>(E, P1, P2, 0);
         else k_eng_setup<double, 4><<<gs, kEngBlock, 0, cs>>>(E, P1, P2, 0);
     };
+    // PCGPME's start (b^ = PM W b, q = PM A x0, residuals) as plain launches
+    const Shape ksh;
+    auto start = [&](cudaStream_t cs) {
+        launch_ldusub_inplace(E, ksh, E.p, E.t, E.q, cs);
+        launch_apply(E, ksh, E.xi, E.q, E.t, 0, cs);
+        k_eng_initres<double><<<grid_of(ksh, E.nblk), ksh.block, 0, cs>>>(E);
+    };
     LoopShape sh;
-    // tuning runs: eight iterations from the real start
-    rc = tune_loop(E, gb, L.NV, 0, 1, [&](cudaStream_t cs) { prime(cs, 1e-300, 8); }, s, &sh);
+    // tuning runs: eight iterations from the real start (not counted as the solve's launches)
+    rc = tune_loop(E, work, gb, L.NV, 0, [&](cudaStream_t cs) { prime(cs, 1e-300, 8); start(cs); }, s, &sh);
     if (rc) return rc;
+    t_launches = 0;
     prime(s, eps_r, iter_r);
+    start(s);
+    t_launches += 2 + 12;
     CLOWNS_CUDA_TRY(cudaGetLastError());
-    rc = launch_loop(E, gb, 1, sh, s);
+    rc = run_loop(E, work, gb, 0, sh, s);
     if (rc) return rc;
     k_eng_copy_out<double><<<gs, kEngBlock, 0, s>>>(E);
+    t_launches += 1;
     CLOWNS_CUDA_TRY(cudaGetLastError());
     rc = check_abort(gb, s);
     if (rc) return rc;
-    return read_infos(work, L, s, info, 0);
+    return read_infos(work, L, s, info, 0, sh);
 }
 
 // Mixed precision: FP32 coefficients and Krylov vectors in the inner BiCGSTAB,
@@ -694,28 +976,33 @@ int engine_solve_mixed(int M, const MemberIn* ins, double eps, double parm, doub
         k_mx_normalize<float><<<kg, ksh.block, 0, cs>>>(E);
     };
     LoopShape sh;
-    rc = tune_loop(E, gb, L.NV, 1, 0, [&](cudaStream_t cs) { setup(cs); sweep_head(cs, 1e-30, 8); }, s, &sh);
+    rc = tune_loop(E, work, gb, L.NV, 1, [&](cudaStream_t cs) { setup(cs); sweep_head(cs, 1e-30, 8); }, s, &sh);
     if (rc) return rc;
+    t_launches = 0;
     setup(s);
+    t_launches += 7;
     CLOWNS_CUDA_TRY(cudaGetLastError());
     std::vector<MemberScalars> h(M);
     for (int sweep = 0; sweep <= max_outer + 1; sweep++) {
         sweep_head(s, inner_tol, inner_max);
+        t_launches += 8;
         CLOWNS_CUDA_TRY(cudaMemcpyAsync(h.data(), E.S, sizeof(MemberScalars) * M, cudaMemcpyDeviceToHost, s));
         CLOWNS_CUDA_TRY(cudaStreamSynchronize(s));
         bool all = true;
         for (int m = 0; m < M; m++) all = all && h[m].odone;
         if (all) break;
-        rc = launch_loop(E, gb, 0, sh, s);
+        rc = run_loop(E, work, gb, 1, sh, s);
         if (rc) return rc;
         k_mx_update<float><<<kg, ksh.block, 0, s>>>(E);
+        t_launches += 1;
         CLOWNS_CUDA_TRY(cudaGetLastError());
         rc = check_abort(gb, s);
         if (rc) return rc;
     }
     k_mx_copy_out<float><<<gs, kEngBlock, 0, s>>>(E);
+    t_launches += 1;
     CLOWNS_CUDA_TRY(cudaGetLastError());
-    return read_infos(work, L, s, info, 1);
+    return read_infos(work, L, s, info, 1, sh);
 }
 
 // Test hooks -------------------------------------------------------------------
@@ -843,6 +1130,11 @@ static int static_upload_tables(void* work, const EngLayout& L, int n, const Mem
         blk_rows[b] = (int)std::max(0L, std::min((long)kTile, rows));
     }
     const int off = 0, nblk = (n + kTile - 1) / kTile, blk0 = 0;
+    constexpr int kStaticMaxGrp = (kStaticMaxBlk + kGroupTiles - 1) / kGroupTiles;
+    int blk_group[kStaticMaxBlk], grp_blk0[kStaticMaxGrp], grp_nblk[kStaticMaxGrp], mem_grp0 = 0, mem_ngrp = 0;
+    const unsigned zeros[kStaticMaxGrp] = {};
+    for (int q = 0; q < L.nblk; q++) blk_group[q] = -1;
+    fill_groups(1, &blk0, &nblk, blk_group, grp_blk0, grp_nblk, &mem_grp0, &mem_ngrp);
     const unsigned zero = 0u;
     char* b = (char*)work;
     CLOWNS_CUDA_TRY(cudaMemcpyAsync(b + L.o_blk_member, blk_member, sizeof(int) * L.nblk, cudaMemcpyHostToDevice, s));
@@ -852,6 +1144,12 @@ static int static_upload_tables(void* work, const EngLayout& L, int n, const Mem
     CLOWNS_CUDA_TRY(cudaMemcpyAsync(b + L.o_mem_nblk, &nblk, sizeof(int), cudaMemcpyHostToDevice, s));
     CLOWNS_CUDA_TRY(cudaMemcpyAsync(b + L.o_mem_blk0, &blk0, sizeof(int), cudaMemcpyHostToDevice, s));
     CLOWNS_CUDA_TRY(cudaMemcpyAsync(b + L.o_ticket, &zero, sizeof(unsigned), cudaMemcpyHostToDevice, s));
+    CLOWNS_CUDA_TRY(cudaMemcpyAsync(b + L.o_blk_group, blk_group, sizeof(int) * L.nblk, cudaMemcpyHostToDevice, s));
+    CLOWNS_CUDA_TRY(cudaMemcpyAsync(b + L.o_grp_blk0, grp_blk0, sizeof(int) * L.ngrp, cudaMemcpyHostToDevice, s));
+    CLOWNS_CUDA_TRY(cudaMemcpyAsync(b + L.o_grp_nblk, grp_nblk, sizeof(int) * L.ngrp, cudaMemcpyHostToDevice, s));
+    CLOWNS_CUDA_TRY(cudaMemcpyAsync(b + L.o_mem_grp0, &mem_grp0, sizeof(int), cudaMemcpyHostToDevice, s));
+    CLOWNS_CUDA_TRY(cudaMemcpyAsync(b + L.o_mem_ngrp, &mem_ngrp, sizeof(int), cudaMemcpyHostToDevice, s));
+    CLOWNS_CUDA_TRY(cudaMemcpyAsync(b + L.o_gticket, zeros, sizeof(unsigned) * L.ngrp, cudaMemcpyHostToDevice, s));
     CLOWNS_CUDA_TRY(cudaMemcpyAsync(b + L.o_in, &in, sizeof(MemberIn), cudaMemcpyHostToDevice, s));
     CLOWNS_CUDA_TRY(cudaStreamSynchronize(s));   // stack sources must outlive the copies
     return CLOWNS_OK;

@@ -20,6 +20,7 @@ constexpr int kEngBlock = 256;
 constexpr int kRowsPerThread = 4;   // rows a thread handles per step (explicit ILP)
 constexpr int kStepBlock = kTile / kRowsPerThread;   // threads covering one tile in one step
 constexpr int kEngMaxGrid = kNumSMs * 8;
+constexpr int kGroupTiles = 64;    // tiles per first-level reduction group
 
 // Per-member scalars; names follow pcgpme_para.F90:47.
 struct MemberScalars {
@@ -71,11 +72,18 @@ struct Eng {
     const int* mem_n;         // rows of each member
     const int* mem_nblk;      // blocks with real rows per member
     const int* mem_blk0;      // first block of each member
+    const int* blk_group;     // reduction group of each block with real rows
+    const int* grp_blk0;      // first block of each group
+    const int* grp_nblk;      // blocks in each group
+    const int* mem_grp0;      // first group of each member
+    const int* mem_ngrp;      // groups of each member
+    unsigned* gticket;        // one per group
+    double* gpartials;        // 2 per group
     const MemberIn* in;       // per-member inputs (device copy of the table)
     MemberScalars* S;
     double* partials;         // 2 per block
     unsigned* ticket;         // one per member
-    int* ctrl;                // [0] loop-body count, [1] max ITER over members
+    int* ctrl;                // [0] loop-body count, [1] max ITER over members, [2] bodies of earlier sweeps
 };
 
 // ---------------------------------------------------------------------------
@@ -106,36 +114,56 @@ __device__ __forceinline__ bool tile_active(const Eng<T>& E, int blk, int& m, lo
     return true;
 }
 
-// Reduce (v0, v1) over the block, record the block's partial and, if this is the
-// last block of member m, return true in the whole block with tot[] holding the
-// member totals (summed over the member's blocks in block order).
+// Reduce (v0, v1) over the block and record the block's partial.  Two levels of
+// "last one sums": the last block of a group of kGroupTiles tiles sums the
+// group's partials, and the last group of member m sums the member's group
+// partials.  Returns true in the whole block that completed member m, with
+// tot[] holding the member totals.  Every sum uses a fixed assignment of terms
+// to threads and a fixed-order block reduction, so the result is deterministic
+// for a given layout and block size.
 template <typename T>
 __device__ __forceinline__ bool member_reduce(const Eng<T>& E, int blk, int m, double v0, double v1,
                                               double* red, double (&tot)[2]) {
     __shared__ int s_last;
     double acc[2] = {v0, v1};
     block_sum<2>(acc, red);
+    const int g = E.blk_group[blk];
     if (threadIdx.x == 0) {
         E.partials[2L * blk + 0] = acc[0];
         E.partials[2L * blk + 1] = acc[1];
         __threadfence();
-        unsigned t = atomicAdd(&E.ticket[m], 1u);
-        s_last = (t == (unsigned)E.mem_nblk[m] - 1u);
+        const unsigned t = atomicAdd(&E.gticket[g], 1u);
+        s_last = (t == (unsigned)E.grp_nblk[g] - 1u);
     }
     __syncthreads();
-    const bool last = s_last;
-    __syncthreads();
-    if (!last) return false;
+    if (!s_last) return false;
     __threadfence();
     {
-        // the member's blocks are contiguous; every thread sums a fixed stride,
-        // then a fixed-order block reduction: deterministic for a given layout
-        const int b0 = E.mem_blk0[m];
-        const int nb = E.mem_nblk[m];
+        const int b0 = E.grp_blk0[g], nb = E.grp_nblk[g];
         double s2[2] = {0.0, 0.0};
         for (int b = threadIdx.x; b < nb; b += blockDim.x) {
             s2[0] += __ldcg(E.partials + 2L * (b0 + b) + 0);
             s2[1] += __ldcg(E.partials + 2L * (b0 + b) + 1);
+        }
+        block_sum<2>(s2, red);
+        if (threadIdx.x == 0) {
+            E.gpartials[2L * g + 0] = s2[0];
+            E.gpartials[2L * g + 1] = s2[1];
+            E.gticket[g] = 0;
+            __threadfence();
+            const unsigned t = atomicAdd(&E.ticket[m], 1u);
+            s_last = (t == (unsigned)E.mem_ngrp[m] - 1u);
+        }
+    }
+    __syncthreads();
+    if (!s_last) return false;
+    __threadfence();
+    {
+        const int g0 = E.mem_grp0[m], ng = E.mem_ngrp[m];
+        double s2[2] = {0.0, 0.0};
+        for (int q = threadIdx.x; q < ng; q += blockDim.x) {
+            s2[0] += __ldcg(E.gpartials + 2L * (g0 + q) + 0);
+            s2[1] += __ldcg(E.gpartials + 2L * (g0 + q) + 1);
         }
         block_sum<2>(s2, red);
         tot[0] = s2[0];
@@ -238,7 +266,7 @@ static __global__ void k_eng_init_scalars(MemberScalars* S, int M, double eps, i
         z.mode = mode;
         S[m] = z;
     }
-    if (threadIdx.x == 0) { ctrl[0] = 0; ctrl[1] = iter; }
+    if (threadIdx.x == 0) { ctrl[0] = 0; ctrl[1] = iter; ctrl[2] = 0; }
 }
 
 // ---------------------------------------------------------------------------
@@ -565,28 +593,76 @@ __device__ __forceinline__ void ph_initres(const Eng<T>& E) {
     }
 }
 
-// Standalone kernels (one block per tile): the same phases.
+// Standalone kernels (one block per tile): the same phases.  Each kernel opens
+// with pdl_enter(): under programmatic dependent launch (graph mode) it lets the
+// next kernel's blocks be scheduled as this grid's blocks retire, then waits
+// for the previous grid to complete; without PDL both calls are no-ops.
+__device__ __forceinline__ void pdl_enter() {
+#if defined(__CUDA_ARCH__) && (__CUDA_ARCH__ >= 900)
+    cudaTriggerProgrammaticLaunchCompletion();
+    cudaGridDependencySynchronize();
+#endif
+}
+
 template <typename T>
 __global__ void __launch_bounds__(kEngBlock) k_eng_axsub(Eng<T> E, const T* __restrict__ in, T* __restrict__ out) {
+    pdl_enter();
     ph_axsub(E, in, out);
 }
 template <typename T>
 __global__ void __launch_bounds__(kEngBlock) k_eng_sweep(Eng<T> E, int k, const T* __restrict__ in,
                                                         T* __restrict__ out) {
+    pdl_enter();
     ph_sweep(E, k, in, out);
 }
 template <typename T, int MODE>
 __global__ void __launch_bounds__(kEngBlock) k_eng_sweep56(Eng<T> E, const T* __restrict__ in, T* __restrict__ out) {
+    pdl_enter();
     ph_sweep56<T, MODE>(E, in, out);
 }
 template <typename T>
-__global__ void __launch_bounds__(kEngBlock) k_eng_eupdate(Eng<T> E) { ph_eupdate(E); }
+__global__ void __launch_bounds__(kEngBlock) k_eng_eupdate(Eng<T> E) {
+    pdl_enter();
+    ph_eupdate(E);
+}
 template <typename T>
-__global__ void __launch_bounds__(kEngBlock) k_eng_xrupdate(Eng<T> E) { ph_xrupdate(E); }
+__global__ void __launch_bounds__(kEngBlock) k_eng_xrupdate(Eng<T> E) {
+    pdl_enter();
+    ph_xrupdate(E);
+}
 template <typename T>
-__global__ void __launch_bounds__(kEngBlock) k_eng_pupdate(Eng<T> E) { ph_pupdate(E); }
+__global__ void __launch_bounds__(kEngBlock) k_eng_pupdate(Eng<T> E) {
+    pdl_enter();
+    ph_pupdate(E);
+}
 template <typename T>
-__global__ void __launch_bounds__(kEngBlock) k_eng_initres(Eng<T> E) { ph_initres(E); }
+__global__ void __launch_bounds__(kEngBlock) k_eng_initres(Eng<T> E) {
+    pdl_enter();
+    ph_initres(E);
+}
+
+// Graph mode: the last node of the WHILE body and the only writer of the loop
+// condition.  Continue while any member iterates; as a backstop no correct
+// run reaches, stop after max ITER + 2 bodies.
+static __global__ void k_eng_guard(MemberScalars* S, int M, int* ctrl, cudaGraphConditionalHandle h) {
+    pdl_enter();
+    __shared__ int any;
+    if (threadIdx.x == 0) any = 0;
+    __syncthreads();
+    for (int m = threadIdx.x; m < M; m += blockDim.x)
+        if (!sld(&S[m].done)) atomicOr(&any, 1);
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        ctrl[0] += 1;
+        int go = any;
+        if (go && ctrl[0] > ctrl[1] + 1) {
+            go = 0;
+            for (int m = 0; m < M; m++)
+                if (!S[m].done) stop_member(S + m, CLOWNS_STOP_MAXITER, S[m].mode == 0 ? CLOWNS_IER_MAXITER : 0);
+        }
+        cudaGraphSetConditional(h, go ? 1u : 0u);
+    }
+}
 
 // ---------------------------------------------------------------------------
 // Persistent iteration loop.

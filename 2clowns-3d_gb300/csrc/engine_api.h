@@ -22,6 +22,7 @@ int engine_apply_pm_a(const MemberIn& in, double parm, const double* x, double* 
 void release_all_graphs();
 int engine_tuned_shape(long nv, int prec, int* block, int* grid, int* minb);
 long engine_row_space(int M, const int* n, int mixed);
+long engine_last_launches();
 void release_graphs_for(const void* work);
 
 }  // namespace clowns

@@ -107,6 +107,8 @@ extern "C" int clowns_tuned_shape(int m, const int* n, int precision, int* block
         set_last_error_msg("tuned_shape: no solve of this size has run yet");
         return rc;
     }
-    *regs = minb == 4 ? 64 : 32;
+    *regs = minb == 4 ? 64 : (minb == 8 ? 32 : 0);   // 0: graph mode
     return CLOWNS_OK;
 }
+
+extern "C" long clowns_last_kernel_launches(void) { return engine_last_launches(); }

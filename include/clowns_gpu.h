@@ -162,11 +162,18 @@ int clowns_pcgpme_batched_dev(int m, const clowns_member* members, int precision
                               double parm, int iter, double inner_tol, int inner_max, int max_outer,
                               void* work, size_t work_bytes, void* stream, clowns_solve_info* infos);
 
-/* Launch shape the autotuner chose for the persistent iteration kernel of a row
- * space (m systems of sizes n[], precision as above): threads per block, blocks
- * (all co-resident) and the register budget per thread.  CLOWNS_ERR_ARG until a
- * solve of that size has run. */
+/* Execution the autotuner chose for the iteration loop of a row space (m
+ * systems of sizes n[], precision as above): threads per block, and either the
+ * blocks (all co-resident) and register budget of the persistent kernel, or
+ * grid = regs = 0 for the CUDA-graph execution.  CLOWNS_ERR_ARG until a solve
+ * of that size has run. */
 int clowns_tuned_shape(int m, const int* n, int precision, int* block, int* grid, int* regs);
+
+/* Kernels the calling thread's last solve (plain or mixed, single or batched)
+ * launched: host launches plus the kernel nodes its loop graphs executed
+ * (16 per iteration), not counting the autotuner's one-time trial runs.
+ * Engine bookkeeping with no counterpart in the reference. */
+long clowns_last_kernel_launches(void);
 
 /* Test hooks of the solve's building blocks (device pointers; workspace sized by
  * clowns_pcgpme_workspace_bytes(n, nl)).  clowns_pcgpme_setup_dev performs only
