@@ -93,7 +93,8 @@ _SIGS = {
     "clowns_pcgpme_static_dev": (C.c_int, [C.c_void_p, C.c_int, C.c_int, C.c_void_p, C.c_void_p, C.c_int,
                                            C.c_void_p, C.c_void_p, C.c_double, C.c_double, C.c_int,
                                            C.c_void_p, C.c_void_p]),
-    "clowns_tuned_shape": (C.c_int, [C.c_int, C.c_void_p, C.c_int, C.c_void_p, C.c_void_p, C.c_void_p]),
+    "clowns_tuned_shape": (C.c_int, [C.c_int, C.c_void_p, C.c_int, C.c_void_p, C.c_void_p, C.c_void_p,
+                                     C.c_void_p]),
     "clowns_last_kernel_launches": (C.c_long, []),
     "clowns_session_create": (C.c_int, [C.c_void_p, C.c_void_p, C.c_int, C.c_int, C.c_int] + [C.c_void_p] * 7),
     "clowns_session_set_fields": (C.c_int, [C.c_void_p] * 9),
@@ -335,15 +336,18 @@ PREC_MIXED = 1
 
 
 def tuned_shape(sizes, precision=0):
-    """(block, grid, registers) the autotuner chose for this row space, or None."""
+    """Execution the autotuner chose for the iteration loop of this row space:
+    {"mode": "graph" | "persistent" | "wave", "block": .., "grid": .., "registers": ..},
+    or None before a solve of that size has run."""
     L = lib()
     arr = (C.c_int * len(sizes))(*[int(v) for v in sizes])
-    b, g, r = C.c_int(0), C.c_int(0), C.c_int(0)
-    if L.clowns_tuned_shape(len(sizes), arr, precision, C.byref(b), C.byref(g), C.byref(r)) != 0:
+    mo, b, g, r = C.c_int(0), C.c_int(0), C.c_int(0), C.c_int(0)
+    if L.clowns_tuned_shape(len(sizes), arr, precision, C.byref(mo), C.byref(b), C.byref(g), C.byref(r)) != 0:
         return None
-    if g.value == 0:
+    if mo.value == 1:
         return {"mode": "graph", "block": b.value}
-    return {"mode": "persistent", "block": b.value, "grid": g.value, "registers": r.value}
+    return {"mode": {0: "persistent", 3: "wave"}.get(mo.value, str(mo.value)), "block": b.value,
+            "grid": g.value, "registers": r.value}
 
 
 def last_kernel_launches():

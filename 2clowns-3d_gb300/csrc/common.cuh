@@ -39,6 +39,21 @@ __device__ __forceinline__ double warp_sum(double v) {
     return v;
 }
 
+// Sums of two values over a warp at the cost of one: lanes exchange across the
+// half-warps first, so that lanes 0-15 go on summing a and lanes 16-31 summing b
+// (5 additions per lane instead of 10).  Returns a's total in lanes 0-15 and b's
+// in lanes 16-31.  Fixed order: deterministic.
+template <typename A>
+__device__ __forceinline__ A warp_pair_sum(A a, A b) {
+    const bool hi = (threadIdx.x & 16) != 0;
+    A keep = hi ? b : a;
+    const A send = hi ? a : b;
+    keep += __shfl_xor_sync(0xffffffffu, send, 16);
+#pragma unroll
+    for (int o = 8; o > 0; o >>= 1) keep += __shfl_xor_sync(0xffffffffu, keep, o);
+    return keep;
+}
+
 template <int NV>
 __device__ __forceinline__ void block_sum(double (&v)[NV], double* smem /* >= 32*NV */) {
     const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;

@@ -127,7 +127,7 @@ __global__ void __launch_bounds__(kEngBlock) k_mx_sweep56(Eng<T> E, const double
                 }
             }
         }
-        __syncthreads();
+        __syncwarp();
     }
 }
 
@@ -157,7 +157,7 @@ __global__ void __launch_bounds__(kEngBlock) k_mx_normalize(Eng<T> E) {
             E.S[m].BN = tot[0];
             E.S[m].C1 = tot[0];
         }
-        __syncthreads();
+        __syncwarp();
     }
 }
 
@@ -228,17 +228,20 @@ static inline int member_groups(int n) {
 
 struct EngLayout {
     long NV = 0;
-    int M = 0, nblk = 0, ngrp = 0, mixed = 0, tsize = 8;
+    int M = 0, nblk = 0, ngrp = 0, mixed = 0, tsize = 8, wave = 0, nchunk = 0;
     size_t o_blk_member, o_blk_rows, o_mem_off, o_mem_n, o_mem_nblk, o_mem_blk0, o_ticket, o_ctrl;
     size_t o_blk_group, o_grp_blk0, o_grp_nblk, o_mem_grp0, o_mem_ngrp, o_gticket, o_gpartials;
     size_t o_in, o_S, o_partials, o_bar, o_al, o_ll, o_d, o_vec[8], o_W, o_x64, o_r64, o_s64, o_t64;
+    size_t o_wave, o_wbuf[kWaveBufs];
     size_t total = 0;
 };
 
-static EngLayout eng_layout(int M, const int* n, int mixed) {
+// wave: -1 = the wavefront loop's buffers for single systems (M == 1), 0 = none.
+static EngLayout eng_layout(int M, const int* n, int mixed, int wave = -1) {
     EngLayout L;
     L.M = M;
     L.mixed = mixed;
+    L.wave = wave < 0 ? (M == 1) : wave;
     L.tsize = mixed ? 4 : 8;
     long NV = 0;
     int ngrp = 0;
@@ -282,6 +285,14 @@ static EngLayout eng_layout(int M, const int* n, int mixed) {
         L.o_t64 = take(sizeof(double) * NV);
     } else {
         L.o_W = L.o_x64 = L.o_r64 = L.o_s64 = L.o_t64 = 0;
+    }
+    L.nchunk = (L.nblk + kWaveChunk - 1) / kWaveChunk;
+    if (L.wave) {
+        L.o_wave = take(sizeof(WaveCtl) + sizeof(unsigned) * 12 * (size_t)L.nchunk);
+        for (int k = 0; k < kWaveBufs; k++) L.o_wbuf[k] = take((size_t)L.tsize * NV);
+    } else {
+        L.o_wave = 0;
+        for (int k = 0; k < kWaveBufs; k++) L.o_wbuf[k] = 0;
     }
     L.total = o;
     return L;
@@ -327,6 +338,8 @@ static Eng<T> eng_bind(void* work, const EngLayout& L) {
     } else {
         E.W = E.x64 = E.r64 = E.s64 = E.t64 = nullptr;
     }
+    E.wave = L.wave ? (WaveCtl*)(b + L.o_wave) : nullptr;
+    for (int k = 0; k < kWaveBufs; k++) E.w[k] = L.wave ? (T*)(b + L.o_wbuf[k]) : nullptr;
     return E;
 }
 
@@ -500,10 +513,12 @@ struct LoopShape {
     int block = kStepBlock;
     int grid = 0;
     int minb = 8;     // register budget of the loop kernel: 8 -> 32, 4 -> 64 registers
-    int graph = 0;    // 1: run the loop as a CUDA graph; 2: host-launched kernels
+    int graph = 0;    // 1: CUDA graph; 2: host-launched kernels; 3: wavefront kernel
+    int wk = 1;       // wavefront: tiles per item
+    int wslack = 3;   // wavefront: slack rounds
 };
 
-// CLOWNS_LOOP_MODE=graph|persistent|launch forces one execution of the loop
+// CLOWNS_LOOP_MODE=graph|persistent|launch|wave forces one execution of the loop
 // ("launch": the iteration's kernels launched from the host, eight iterations
 // between polls of the stop flags -- the same kernels, visible one by one to a
 // profiler); unset or "auto": the autotuner decides.
@@ -513,6 +528,7 @@ static int forced_loop_mode() {
     if (!strcmp(v, "persistent")) return 0;
     if (!strcmp(v, "graph")) return 1;
     if (!strcmp(v, "launch")) return 2;
+    if (!strcmp(v, "wave")) return 3;
     return -1;
 }
 
@@ -521,13 +537,19 @@ static const void* loop_fn(int minb) {
     return minb == 4 ? (const void*)k_eng_loop<T, 4> : (const void*)k_eng_loop<T, 8>;
 }
 
+template <typename T>
+static const void* wave_fn(int minb) {
+    return minb == 12 ? (const void*)k_eng_wave<T, 12> : (const void*)k_eng_wave<T, 8>;
+}
+
 static std::mutex g_loop_mu;
-static std::map<std::pair<long, int>, LoopShape> g_loop_shapes;
+static std::map<std::tuple<long, int, int>, LoopShape> g_loop_shapes;   // (row space, precision, wave)
 
 template <typename T>
-static int loop_max_grid(int block, int minb, int* out) {
+static int loop_max_grid(int block, int minb, int* out, bool wave = false) {
     int per_sm = 0, dev = 0, sms = 0;
-    CLOWNS_CUDA_TRY(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, loop_fn<T>(minb), block, 0));
+    CLOWNS_CUDA_TRY(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, wave ? wave_fn<T>(minb) : loop_fn<T>(minb),
+                                                                  block, 0));
     CLOWNS_CUDA_TRY(cudaGetDevice(&dev));
     CLOWNS_CUDA_TRY(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
     *out = per_sm * sms;
@@ -703,6 +725,21 @@ static int run_loop(Eng<T> E, const void* work, GridBar* gb, int prec, const Loo
         set_last_error_msg("pcgpme: stop flags not raised after ITER iterations");
         return CLOWNS_ERR_NOCONV;
     }
+    if (sh.graph == 3) {
+        if (!E.wave || E.M != 1) {
+            set_last_error_msg("pcgpme: the wavefront loop serves single systems only");
+            return CLOWNS_ERR_ARG;
+        }
+        const int nchunk = (E.nblk + kWaveChunk - 1) / kWaveChunk;
+        CLOWNS_CUDA_TRY(cudaMemsetAsync(gb, 0, sizeof(GridBar), s));
+        CLOWNS_CUDA_TRY(cudaMemsetAsync(&E.wave->alp, 0, 3 * sizeof(unsigned), s));
+        CLOWNS_CUDA_TRY(cudaMemsetAsync(E.wave + 1, 0, sizeof(unsigned) * 12 * (size_t)nchunk, s));
+        int K = sh.wk, slack = sh.wslack;
+        void* args[] = {(void*)&E, (void*)&gb, (void*)&K, (void*)&slack};
+        CLOWNS_CUDA_TRY(cudaLaunchCooperativeKernel(wave_fn<T>(sh.minb), dim3(sh.grid), dim3(kStepBlock), args, 0, s));
+        t_launches += 1;
+        return CLOWNS_OK;
+    }
     if (sh.graph) {
         cudaGraphExec_t ex;
         int rc = loop_graph(E, work, prec, &ex);
@@ -739,19 +776,56 @@ template <typename T, typename Prime>
 static int tune_loop(Eng<T> E, const void* work, GridBar* gb, long key_nv, int key_prec, Prime prime,
                      cudaStream_t s, LoopShape* out) {
     const int forced = forced_loop_mode();
+    const bool wave_ok = E.wave != nullptr && E.M == 1;
     if (forced == 1 || forced == 2) {
         LoopShape sh;
         sh.graph = forced;
         *out = sh;
         return CLOWNS_OK;
     }
-    {
+    const auto key = std::make_tuple(key_nv, key_prec, (int)wave_ok);
+    // CLOWNS_WAVE_PARAMS="K,slack,minb,frac" pins the wavefront candidate (tuning sweeps; read on every call)
+    const char* wp = getenv("CLOWNS_WAVE_PARAMS");
+    int pk = 0, ps = 0, pm = 0, pf = 0;
+    const bool pinned = wp && sscanf(wp, "%d,%d,%d,%d", &pk, &ps, &pm, &pf) == 4 && (pk == 1 || pk == 2 ||
+                        pk == 4 || pk == 8 || pk == 16) && ps >= 0 && (pm == 8 || pm == 12) && pf >= 1 && pf <= 4;
+    if (!pinned) {
         std::lock_guard<std::mutex> lk(g_loop_mu);
-        auto it = g_loop_shapes.find({key_nv, key_prec});
+        auto it = g_loop_shapes.find(key);
         if (it != g_loop_shapes.end()) { *out = it->second; return CLOWNS_OK; }
     }
     std::vector<LoopShape> cands;
-    for (int minb : {8, 4}) {
+    if (wave_ok && (forced < 0 || forced == 3)) {
+        for (int minb : {8, 12}) {
+            if (pinned && minb != pm) continue;
+            int gmax = 0;
+            int rc = loop_max_grid<T>(kStepBlock, minb, &gmax, true);
+            if (rc) return rc;
+            for (int frac : {4, 3}) {
+                if (pinned && frac != pf) continue;
+                for (int wk : {1, 2}) {
+                    if (pinned && wk != pk) continue;
+                    LoopShape sh;
+                    sh.graph = 3;
+                    sh.minb = minb;
+                    sh.grid = std::max(1, gmax * (pinned ? pf : frac) / 4);
+                    sh.wk = pinned ? pk : wk;
+                    sh.wslack = pinned ? ps : 3;
+                    cands.push_back(sh);
+                }
+            }
+            if (pinned && cands.empty()) {
+                LoopShape sh;
+                sh.graph = 3;
+                sh.minb = pm;
+                sh.grid = std::max(1, gmax * pf / 4);
+                sh.wk = pk;
+                sh.wslack = ps;
+                cands.push_back(sh);
+            }
+        }
+    }
+    if (forced < 0 || forced == 0) for (int minb : {8, 4}) {
         int gmax = 0;
         int rc = loop_max_grid<T>(kStepBlock, minb, &gmax);
         if (rc) return rc;
@@ -763,10 +837,14 @@ static int tune_loop(Eng<T> E, const void* work, GridBar* gb, long key_nv, int k
             cands.push_back(sh);
         }
     }
-    if (forced != 0) {
+    if (forced < 0 || (forced == 3 && !wave_ok)) {     // forced wave: ensembles keep the graph
         LoopShape gsh;
         gsh.graph = 1;
         cands.push_back(gsh);
+    }
+    if (cands.empty()) {
+        set_last_error_msg("pcgpme: the forced loop execution does not serve this system");
+        return CLOWNS_ERR_ARG;
     }
     cudaEvent_t e0, e1;
     CLOWNS_CUDA_TRY(cudaEventCreate(&e0));
@@ -792,18 +870,21 @@ static int tune_loop(Eng<T> E, const void* work, GridBar* gb, long key_nv, int k
     cudaEventDestroy(e0);
     cudaEventDestroy(e1);
     std::lock_guard<std::mutex> lk(g_loop_mu);
-    g_loop_shapes[{key_nv, key_prec}] = best;
+    g_loop_shapes[key] = best;
     *out = best;
     return CLOWNS_OK;
 }
 
-int engine_tuned_shape(long nv, int prec, int* block, int* grid, int* minb) {
+// mode: 0 persistent, 1 CUDA graph, 3 wavefront
+int engine_tuned_shape(long nv, int prec, int single, int* mode, int* block, int* grid, int* minb) {
     std::lock_guard<std::mutex> lk(g_loop_mu);
-    auto it = g_loop_shapes.find({nv, prec});
+    auto it = g_loop_shapes.find(std::make_tuple(nv, prec, single));
     if (it == g_loop_shapes.end()) return CLOWNS_ERR_ARG;
-    *block = it->second.block;
-    *grid = it->second.graph ? 0 : it->second.grid;
-    *minb = it->second.graph ? 0 : it->second.minb;
+    const LoopShape& sh = it->second;
+    *mode = sh.graph;
+    *block = sh.block;
+    *grid = sh.graph == 1 ? 0 : sh.grid;
+    *minb = sh.graph == 1 ? 0 : sh.minb;
     return CLOWNS_OK;
 }
 
@@ -904,6 +985,7 @@ int engine_solve_plain(int M, const MemberIn* ins, double eps, double parm, int 
     GridBar* gb = (GridBar*)((char*)work + L.o_bar);
     const int gs = std::min(L.nblk * 2, kEngMaxGrid * 4);
     auto prime = [&](cudaStream_t cs, double e, int it) {
+        if (E.wave) cudaMemsetAsync(&E.wave->D, 0, sizeof(int), cs);
         k_eng_init_scalars<<<1, 256, 0, cs>>>(E.S, M, e, it, 0, E.ctrl);
         if (nl == 6) k_eng_setup<double, 6><<<gs, kEngBlock, 0, cs>>>(E, P1, P2, 0);
         else k_eng_setup<double, 4><<<gs, kEngBlock, 0, cs>>>(E, P1, P2, 0);
@@ -963,6 +1045,7 @@ int engine_solve_mixed(int M, const MemberIn* ins, double eps, double parm, doub
     const Shape ksh;                               // standalone FP64 refinement kernels
     const int kg = grid_of(ksh, E.nblk);
     auto setup = [&](cudaStream_t cs) {
+        if (E.wave) cudaMemsetAsync(&E.wave->D, 0, sizeof(int), cs);
         k_mixed_init_scalars<<<1, 256, 0, cs>>>(E.S, M, eps_r, max_outer, E.ctrl);
         if (nl == 6) k_eng_setup<float, 6><<<gs, kEngBlock, 0, cs>>>(E, P1, P2, 1);
         else k_eng_setup<float, 4><<<gs, kEngBlock, 0, cs>>>(E, P1, P2, 1);
@@ -1173,7 +1256,7 @@ extern "C" int clowns_pcgpme_static_dev(const double* al, int nl, int na, const 
     void* work = nullptr;
     int rc = static_scratch(&work);
     if (rc) return rc;
-    EngLayout L = eng_layout(1, &n, 0);
+    EngLayout L = eng_layout(1, &n, 0, 0);
     if (L.total > kStaticBytes || L.nblk > kStaticMaxBlk) {
         set_last_error_msg("pcgpme_static: layout exceeds the static scratch");
         return CLOWNS_ERR_LIMIT;

@@ -21,6 +21,21 @@ constexpr int kRowsPerThread = 4;   // rows a thread handles per step (explicit 
 constexpr int kStepBlock = kTile / kRowsPerThread;   // threads covering one tile in one step
 constexpr int kEngMaxGrid = kNumSMs * 8;
 constexpr int kGroupTiles = 64;    // tiles per first-level reduction group
+constexpr int kWaveChunk = 16;     // tiles per completion counter of the wavefront loop
+constexpr int kWaveStages = 7;     // stages of each of the wavefront loop's two apply segments
+constexpr int kWaveBufs = 5;       // intermediate vectors of one operator application
+
+// Control block of the wavefront loop (single system).  D: the largest
+// distance, in tiles, between a row and a real (non-zero-row) neighbour it
+// gathers from, set by the setup kernel.  alp/amu/beta: finalisations of the
+// three per-iteration reductions published in the current launch.  Followed
+// in the workspace by 12 x nchunk completion counters.
+struct WaveCtl {
+    int D;
+    int pad0;
+    unsigned alp, amu, beta;
+    int pad[27];
+};
 
 // Per-member scalars; names follow pcgpme_para.F90:47.
 struct MemberScalars {
@@ -79,6 +94,8 @@ struct Eng {
     const int* mem_ngrp;      // groups of each member
     unsigned* gticket;        // one per group
     double* gpartials;        // 2 per group
+    T* w[kWaveBufs];          // wavefront loop: intermediates of one application (single system)
+    WaveCtl* wave;            // wavefront loop control (nullptr: not available)
     const MemberIn* in;       // per-member inputs (device copy of the table)
     MemberScalars* S;
     double* partials;         // 2 per block
@@ -117,57 +134,68 @@ __device__ __forceinline__ bool tile_active(const Eng<T>& E, int blk, int& m, lo
 // Reduce (v0, v1) over the block and record the block's partial.  Two levels of
 // "last one sums": the last block of a group of kGroupTiles tiles sums the
 // group's partials, and the last group of member m sums the member's group
-// partials.  Returns true in the whole block that completed member m, with
-// tot[] holding the member totals.  Every sum uses a fixed assignment of terms
-// to threads and a fixed-order block reduction, so the result is deterministic
-// for a given layout and block size.
-template <typename T>
-__device__ __forceinline__ bool member_reduce(const Eng<T>& E, int blk, int m, double v0, double v1,
-                                              double* red, double (&tot)[2]) {
-    __shared__ int s_last;
-    double acc[2] = {v0, v1};
-    block_sum<2>(acc, red);
-    const int g = E.blk_group[blk];
-    if (threadIdx.x == 0) {
-        E.partials[2L * blk + 0] = acc[0];
-        E.partials[2L * blk + 1] = acc[1];
-        __threadfence();
-        const unsigned t = atomicAdd(&E.gticket[g], 1u);
-        s_last = (t == (unsigned)E.grp_nblk[g] - 1u);
-    }
+// partials.  Per-thread values are summed over the warp in their own type A
+// (float for the FP32 inner solve, whose FP64 pipe is scarce on this GPU) and
+// across warps and blocks in double.  After the block-wide step only warp 0
+// continues (the other warps retire); returns true in warp 0 of the block that
+// completed member m, with tot[] holding the member totals in all its lanes.
+// Every sum uses a fixed assignment of terms to lanes and a fixed tree, so the
+// result is deterministic for a given layout and block size.  `red` holds 64
+// doubles.
+template <typename T, typename A>
+__device__ __forceinline__ bool member_reduce(const Eng<T>& E, int blk, int m, A v0, A v1, double* red,
+                                              double (&tot)[2]) {
+    const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5, nw = blockDim.x >> 5;
+    const A w = warp_pair_sum(v0, v1);
+    if (lane == 0) red[wid] = (double)w;
+    if (lane == 16) red[32 + wid] = (double)w;
     __syncthreads();
-    if (!s_last) return false;
+    double a = 0.0, b = 0.0;
+    if (wid == 0 && lane < nw) {
+        a = red[lane];
+        b = red[32 + lane];
+    }
+    __syncthreads();                       // red is free for the next tile
+    if (wid != 0) return false;
+    double s = warp_pair_sum(a, b);
+    const int g = E.blk_group[blk];
+    unsigned last = 0;
+    if (lane == 0) E.partials[2L * blk + 0] = s;
+    if (lane == 16) E.partials[2L * blk + 1] = s;
+    if (lane == 0 || lane == 16) __threadfence();
+    __syncwarp();
+    if (lane == 0) last = atomicAdd(&E.gticket[g], 1u) == (unsigned)E.grp_nblk[g] - 1u;
+    if (!__shfl_sync(0xffffffffu, last, 0)) return false;
     __threadfence();
     {
         const int b0 = E.grp_blk0[g], nb = E.grp_nblk[g];
-        double s2[2] = {0.0, 0.0};
-        for (int b = threadIdx.x; b < nb; b += blockDim.x) {
-            s2[0] += __ldcg(E.partials + 2L * (b0 + b) + 0);
-            s2[1] += __ldcg(E.partials + 2L * (b0 + b) + 1);
+        a = b = 0.0;
+        for (int q = lane; q < nb; q += 32) {
+            a += __ldcg(E.partials + 2L * (b0 + q) + 0);
+            b += __ldcg(E.partials + 2L * (b0 + q) + 1);
         }
-        block_sum<2>(s2, red);
-        if (threadIdx.x == 0) {
-            E.gpartials[2L * g + 0] = s2[0];
-            E.gpartials[2L * g + 1] = s2[1];
+        s = warp_pair_sum(a, b);
+        if (lane == 0) E.gpartials[2L * g + 0] = s;
+        if (lane == 16) E.gpartials[2L * g + 1] = s;
+        if (lane == 0 || lane == 16) __threadfence();
+        __syncwarp();
+        if (lane == 0) {
             E.gticket[g] = 0;
-            __threadfence();
-            const unsigned t = atomicAdd(&E.ticket[m], 1u);
-            s_last = (t == (unsigned)E.mem_ngrp[m] - 1u);
+            last = atomicAdd(&E.ticket[m], 1u) == (unsigned)E.mem_ngrp[m] - 1u;
         }
     }
-    __syncthreads();
-    if (!s_last) return false;
+    if (!__shfl_sync(0xffffffffu, last, 0)) return false;
     __threadfence();
     {
         const int g0 = E.mem_grp0[m], ng = E.mem_ngrp[m];
-        double s2[2] = {0.0, 0.0};
-        for (int q = threadIdx.x; q < ng; q += blockDim.x) {
-            s2[0] += __ldcg(E.gpartials + 2L * (g0 + q) + 0);
-            s2[1] += __ldcg(E.gpartials + 2L * (g0 + q) + 1);
+        a = b = 0.0;
+        for (int q = lane; q < ng; q += 32) {
+            a += __ldcg(E.gpartials + 2L * (g0 + q) + 0);
+            b += __ldcg(E.gpartials + 2L * (g0 + q) + 1);
         }
-        block_sum<2>(s2, red);
-        tot[0] = s2[0];
-        tot[1] = s2[1];
+        s = warp_pair_sum(a, b);
+        tot[0] = __shfl_sync(0xffffffffu, s, 0);
+        tot[1] = __shfl_sync(0xffffffffu, s, 16);
     }
     return true;
 }
@@ -186,6 +214,7 @@ __device__ __forceinline__ void stop_member(MemberScalars* S, int reason, int ie
 // member's zero row.  init_x: copy the member's initial guess into xi / x64.
 template <typename T, int NL>
 __global__ void __launch_bounds__(kEngBlock) k_eng_setup(Eng<T> E, double P1, double P2, int mixed) {
+    int reach = 0;    // gather distance in tiles (wavefront loop), real neighbours only
     for (long i = (long)blockIdx.x * blockDim.x + threadIdx.x; i < E.NV; i += (long)gridDim.x * blockDim.x) {
         const int blk = (int)(i / kTile);
         const int m = E.blk_member[blk];
@@ -203,6 +232,9 @@ __global__ void __launch_bounds__(kEngBlock) k_eng_setup(Eng<T> E, double P1, do
             E.r[i] = T(0); E.p[i] = T(0); E.r0[i] = T(0); E.q[i] = T(0);
             E.e[i] = T(0); E.v[i] = T(0); E.t[i] = T(0); E.xi[i] = T(0);
             if (mixed) { E.W[i] = 0.0; E.x64[i] = 0.0; E.r64[i] = 0.0; E.s64[i] = 0.0; E.t64[i] = 0.0; }
+            if (E.wave)
+#pragma unroll
+                for (int k = 0; k < kWaveBufs; k++) E.w[k][i] = T(0);
             continue;
         }
         double a[6];
@@ -241,7 +273,11 @@ __global__ void __launch_bounds__(kEngBlock) k_eng_setup(Eng<T> E, double P1, do
             }
         }
 #pragma unroll
-        for (int k = 0; k < 6; k++) { E.al[k * NV + i] = T(a[k]); E.ll[k * NV + i] = c[k]; }
+        for (int k = 0; k < 6; k++) {
+            E.al[k * NV + i] = T(a[k]);
+            E.ll[k * NV + i] = c[k];
+            if (c[k] < pad) reach = max(reach, abs((int)(c[k] / kTile) - blk));
+        }
         E.d[i] = T(dd);
         const double x0 = in.x[li];
         if (mixed) {
@@ -254,6 +290,14 @@ __global__ void __launch_bounds__(kEngBlock) k_eng_setup(Eng<T> E, double P1, do
             E.p[i] = T(bb);
             E.xi[i] = T(x0);
         }
+    }
+    if (E.wave) {
+        __shared__ int s_reach;
+        if (threadIdx.x == 0) s_reach = 0;
+        __syncthreads();
+        if (reach) atomicMax(&s_reach, reach);
+        __syncthreads();
+        if (threadIdx.x == 0 && s_reach) atomicMax(&E.wave->D, s_reach);
     }
 }
 
@@ -278,13 +322,13 @@ static __global__ void k_eng_init_scalars(MemberScalars* S, int M, double eps, i
 
 // out = D in + sum_k AL_k in[LL_k]   (AXSUB, pcgpme_para.F90:323-352)
 template <typename T>
-__device__ __forceinline__ void ph_axsub(const Eng<T>& E, const T* __restrict__ in, T* __restrict__ out) {
+__device__ __forceinline__ void tl_axsub(const Eng<T>& E, int blk, const T* __restrict__ in, T* __restrict__ out) {
     constexpr int R = kRowsPerThread;
     const long NV = E.NV;
-    for (int blk = blockIdx.x; blk < E.nblk; blk += gridDim.x) {
+    {
         int m, rows;
         long row0;
-        if (!tile_active(E, blk, m, row0, rows)) continue;
+        if (!tile_active(E, blk, m, row0, rows)) return;
         for (int base = threadIdx.x; base < rows; base += blockDim.x * R) {
             T s[R];
             bool ok[R];
@@ -315,17 +359,23 @@ __device__ __forceinline__ void ph_axsub(const Eng<T>& E, const T* __restrict__ 
     }
 }
 
+template <typename T>
+__device__ __forceinline__ void ph_axsub(const Eng<T>& E, const T* __restrict__ in, T* __restrict__ out) {
+    for (int blk = blockIdx.x; blk < E.nblk; blk += gridDim.x) tl_axsub(E, blk, in, out);
+}
+
 // One single-neighbour sweep of LDUSUB: out = in - AL_k in[LL_k]  (263-304)
 template <typename T>
-__device__ __forceinline__ void ph_sweep(const Eng<T>& E, int k, const T* __restrict__ in, T* __restrict__ out) {
+__device__ __forceinline__ void tl_sweep(const Eng<T>& E, int blk, int k, const T* __restrict__ in,
+                                         T* __restrict__ out) {
     constexpr int R = kRowsPerThread;
     const long NV = E.NV;
     const T* __restrict__ a = E.al + k * NV;
     const int* __restrict__ c = E.ll + k * NV;
-    for (int blk = blockIdx.x; blk < E.nblk; blk += gridDim.x) {
+    {
         int m, rows;
         long row0;
-        if (!tile_active(E, blk, m, row0, rows)) continue;
+        if (!tile_active(E, blk, m, row0, rows)) return;
         for (int base = threadIdx.x; base < rows; base += blockDim.x * R) {
             T av[R], xv[R], gv[R];
             int cv[R];
@@ -348,20 +398,26 @@ __device__ __forceinline__ void ph_sweep(const Eng<T>& E, int k, const T* __rest
     }
 }
 
+template <typename T>
+__device__ __forceinline__ void ph_sweep(const Eng<T>& E, int k, const T* __restrict__ in, T* __restrict__ out) {
+    for (int blk = blockIdx.x; blk < E.nblk; blk += gridDim.x) tl_sweep(E, blk, k, in, out);
+}
+
 // Last sweep (J=5,6, 306-318) with an optional fused per-member reduction:
 //   MODE 0 none; 1: RQ = (r0,out) -> ALP = C1/RQ; 2: AMU = (e,out)/(out,out)
+// Returns true in warp 0 of the block that finalised the member's scalars.
 template <typename T, int MODE>
-__device__ __forceinline__ void ph_sweep56(const Eng<T>& E, const T* __restrict__ in, T* __restrict__ out) {
-    __shared__ double red[64];
+__device__ __forceinline__ bool tl_sweep56(const Eng<T>& E, int blk, const T* __restrict__ in, T* __restrict__ out,
+                                           double* red) {
     const long NV = E.NV;
     const T* __restrict__ a5 = E.al + 4 * NV;
     const T* __restrict__ a6 = E.al + 5 * NV;
     const int* __restrict__ c5 = E.ll + 4 * NV;
     const int* __restrict__ c6 = E.ll + 5 * NV;
-    for (int blk = blockIdx.x; blk < E.nblk; blk += gridDim.x) {
+    {
         int m, rows;
         long row0;
-        if (!tile_active(E, blk, m, row0, rows)) continue;
+        if (!tile_active(E, blk, m, row0, rows)) return false;
         constexpr int R = kRowsPerThread;
         T acc0 = T(0), acc1 = T(0);
         for (int base = threadIdx.x; base < rows; base += blockDim.x * R) {
@@ -394,9 +450,9 @@ __device__ __forceinline__ void ph_sweep56(const Eng<T>& E, const T* __restrict_
                 if (MODE == 2) { acc0 += ldg2(E.e + i) * y; acc1 += y * y; }
             }
         }
-        if (MODE == 0) continue;
+        if (MODE == 0) return false;
         double tot[2];
-        if (!member_reduce(E, blk, m, (double)acc0, (double)acc1, red, tot)) continue;
+        if (!member_reduce(E, blk, m, acc0, acc1, red, tot)) return false;
         if (threadIdx.x == 0) {
             MemberScalars* S = E.S + m;
             E.ticket[m] = 0;
@@ -420,17 +476,24 @@ __device__ __forceinline__ void ph_sweep56(const Eng<T>& E, const T* __restrict_
             }
             __threadfence();
         }
-        __syncthreads();
+        __syncwarp();
+        return true;
     }
+}
+
+template <typename T, int MODE>
+__device__ __forceinline__ void ph_sweep56(const Eng<T>& E, const T* __restrict__ in, T* __restrict__ out) {
+    __shared__ double red[64];
+    for (int blk = blockIdx.x; blk < E.nblk; blk += gridDim.x) tl_sweep56<T, MODE>(E, blk, in, out, red);
 }
 
 // E = R - ALP Q  (171-175)
 template <typename T>
-__device__ __forceinline__ void ph_eupdate(const Eng<T>& E) {
-    for (int blk = blockIdx.x; blk < E.nblk; blk += gridDim.x) {
+__device__ __forceinline__ void tl_eupdate(const Eng<T>& E, int blk) {
+    {
         int m, rows;
         long row0;
-        if (!tile_active(E, blk, m, row0, rows)) continue;
+        if (!tile_active(E, blk, m, row0, rows)) return;
         const T ALP = T(sld(&E.S[m].ALP));
         constexpr int R = kRowsPerThread;
         for (int base = threadIdx.x; base < rows; base += blockDim.x * R) {
@@ -451,15 +514,20 @@ __device__ __forceinline__ void ph_eupdate(const Eng<T>& E) {
     }
 }
 
+template <typename T>
+__device__ __forceinline__ void ph_eupdate(const Eng<T>& E) {
+    for (int blk = blockIdx.x; blk < E.nblk; blk += gridDim.x) tl_eupdate(E, blk);
+}
+
 // X += ALP P + AMU E ; R = E - AMU V ; RN = (R,R) ; C1 = (R0,R)  (199-213),
 // then ERR and the stop tests (215-241).
+// Returns true in warp 0 of the block that finalised the member's scalars.
 template <typename T>
-__device__ __forceinline__ void ph_xrupdate(const Eng<T>& E) {
-    __shared__ double red[64];
-    for (int blk = blockIdx.x; blk < E.nblk; blk += gridDim.x) {
+__device__ __forceinline__ bool tl_xrupdate(const Eng<T>& E, int blk, double* red) {
+    {
         int m, rows;
         long row0;
-        if (!tile_active(E, blk, m, row0, rows)) continue;
+        if (!tile_active(E, blk, m, row0, rows)) return false;
         const T ALP = T(sld(&E.S[m].ALP)), AMU = T(sld(&E.S[m].AMU));
         T acc0 = T(0), acc1 = T(0);
         constexpr int R = kRowsPerThread;
@@ -488,7 +556,7 @@ __device__ __forceinline__ void ph_xrupdate(const Eng<T>& E) {
             }
         }
         double tot[2];
-        if (!member_reduce(E, blk, m, (double)acc0, (double)acc1, red, tot)) continue;
+        if (!member_reduce(E, blk, m, acc0, acc1, red, tot)) return false;
         if (threadIdx.x == 0) {
             MemberScalars* S = E.S + m;
             E.ticket[m] = 0;
@@ -529,17 +597,24 @@ __device__ __forceinline__ void ph_xrupdate(const Eng<T>& E) {
             }
             __threadfence();
         }
-        __syncthreads();
+        __syncwarp();
+        return true;
     }
+}
+
+template <typename T>
+__device__ __forceinline__ void ph_xrupdate(const Eng<T>& E) {
+    __shared__ double red[64];
+    for (int blk = blockIdx.x; blk < E.nblk; blk += gridDim.x) tl_xrupdate(E, blk, red);
 }
 
 // P = R + BETA (P - AMU Q)  (242-246)
 template <typename T>
-__device__ __forceinline__ void ph_pupdate(const Eng<T>& E) {
-    for (int blk = blockIdx.x; blk < E.nblk; blk += gridDim.x) {
+__device__ __forceinline__ void tl_pupdate(const Eng<T>& E, int blk) {
+    {
         int m, rows;
         long row0;
-        if (!tile_active(E, blk, m, row0, rows)) continue;
+        if (!tile_active(E, blk, m, row0, rows)) return;
         const T BETA = T(sld(&E.S[m].BETA)), AMU = T(sld(&E.S[m].AMU));
         constexpr int R = kRowsPerThread;
         for (int base = threadIdx.x; base < rows; base += blockDim.x * R) {
@@ -559,6 +634,11 @@ __device__ __forceinline__ void ph_pupdate(const Eng<T>& E) {
             }
         }
     }
+}
+
+template <typename T>
+__device__ __forceinline__ void ph_pupdate(const Eng<T>& E) {
+    for (int blk = blockIdx.x; blk < E.nblk; blk += gridDim.x) tl_pupdate(E, blk);
 }
 
 // BN = (b^,b^); R = b^ - q; C1 = (R,R); P = R0 = R  (129-145).  p holds b^ = PM W b
@@ -582,14 +662,14 @@ __device__ __forceinline__ void ph_initres(const Eng<T>& E) {
             E.r0[i] = temp;
         }
         double tot[2];
-        if (!member_reduce(E, blk, m, (double)acc0, (double)acc1, red, tot)) continue;
+        if (!member_reduce(E, blk, m, acc0, acc1, red, tot)) continue;
         if (threadIdx.x == 0) {
             E.ticket[m] = 0;
             E.S[m].BN = tot[0];
             E.S[m].C1 = tot[1];
             __threadfence();
         }
-        __syncthreads();
+        __syncwarp();
     }
 }
 
@@ -773,6 +853,164 @@ __global__ void __launch_bounds__(kEngBlock, MINB) k_eng_loop(Eng<T> E, GridBar*
         if (!grid_sync(gb)) return;
         ph_pupdate(E);                                        // p
         if (!grid_sync(gb)) return;
+    }
+}
+
+// ---------------------------------------------------------------------------
+// Wavefront loop (single system).
+//
+// One cooperative launch runs the iteration loop as a stream of (stage, tile)
+// items instead of kernel-wide phases.  An iteration has three segments, each
+// ended by one of BiCGSTAB's per-iteration reductions:
+//   A: p = r + BETA (p - AMU q) | q = PM A p (axsub, 4 sweeps, sweep56) | RQ -> ALP
+//   B: e = r - ALP q            | v = PM A e                            | AMU, SS
+//   C: x, r ; RN, C1 ; stop tests -> BETA
+// Within A and B a stage of tile t needs the previous stage only on tiles
+// [t-D, t+D] (D: gather reach), so stage s of tile t is ordered at key
+// t + s L with a lag L > D + kWaveChunk: every item comes after the items it
+// waits for, and the FP64-heavy axsub of one tile runs beside the memory-bound
+// sweeps of others.  Items are dealt round-robin to the co-resident blocks,
+// which take them in order; each waits on per-chunk completion counters
+// (monotone across iterations) and publishes its own.  The reductions keep the
+// engine's deterministic two-level "last block sums" scheme; their finalising
+// block publishes an epoch that the next segment waits for.  Every wait is
+// bounded (kBarSpinLimit polls): a block that gives up raises the abort flag,
+// every other block leaves at its next wait, and the host reports the error.
+
+__device__ __forceinline__ unsigned ld_relaxed_u32(const unsigned* p) {
+    unsigned v;
+    asm volatile("ld.relaxed.gpu.global.u32 %0, [%1];" : "=r"(v) : "l"(p) : "memory");
+    return v;
+}
+__device__ __forceinline__ int ld_relaxed_s32(const int* p) {
+    int v;
+    asm volatile("ld.relaxed.gpu.global.s32 %0, [%1];" : "=r"(v) : "l"(p) : "memory");
+    return v;
+}
+
+// Warp 0 waits until the counters of chunks c0..c1 reach (it + 1) x (tiles of
+// the chunk); the whole block then proceeds.  False: abort raised.
+__device__ __forceinline__ bool wave_wait_counts(const unsigned* cnt, int c0, int c1, int it, int nblk,
+                                                 GridBar* gb) {
+    __shared__ int s_ok;
+    if (threadIdx.x < 32) {
+        bool ok = true;
+        for (int c = c0 + (int)threadIdx.x; c <= c1 && ok; c += 32) {
+            const unsigned need = (unsigned)(it + 1) * (unsigned)min(kWaveChunk, nblk - c * kWaveChunk);
+            long spins = 0;
+            while (ld_relaxed_u32(cnt + c) < need) {
+                if (ld_relaxed_s32(&gb->abort)) { ok = false; break; }
+                if (++spins > kBarSpinLimit) { atomicExch(&gb->abort, 1); ok = false; break; }
+                __nanosleep(32);
+            }
+        }
+        ok = __all_sync(0xffffffffu, ok);
+        __threadfence();
+        if (threadIdx.x == 0) s_ok = ok;
+    }
+    __syncthreads();
+    return s_ok != 0;
+}
+
+// Thread 0 waits until *ep >= need.  False: abort raised.
+__device__ __forceinline__ bool wave_wait_epoch(const unsigned* ep, unsigned need, GridBar* gb) {
+    __shared__ int s_ok;
+    if (threadIdx.x == 0) {
+        bool ok = true;
+        long spins = 0;
+        while (ld_relaxed_u32(ep) < need) {
+            if (ld_relaxed_s32(&gb->abort)) { ok = false; break; }
+            if (++spins > kBarSpinLimit) { atomicExch(&gb->abort, 1); ok = false; break; }
+            __nanosleep(64);
+        }
+        __threadfence();
+        s_ok = ok;
+    }
+    __syncthreads();
+    return s_ok != 0;
+}
+
+// Stage s (0..6) of segment seg (0: A, 1: B) on tiles t0 .. t0+K-1 (K divides
+// kWaveChunk) in iteration it.
+template <typename T>
+__device__ __forceinline__ bool wave_item(const Eng<T>& E, GridBar* gb, unsigned* cnt, int nchunk, int seg, int s,
+                                          int t0, int K, int it, int D, double* red) {
+    const int nblk = E.nblk;
+    const int t1 = min(nblk, t0 + K);
+    if (s >= 1) {
+        const int lo = max(0, t0 - D), hi = min(nblk - 1, t1 - 1 + D);
+        if (!wave_wait_counts(cnt + (long)(seg * 6 + s - 1) * nchunk, lo / kWaveChunk, hi / kWaveChunk, it, nblk,
+                              gb))
+            return false;
+    }
+    for (int t = t0; t < t1; t++) {
+        if (s == 6) {
+            const bool fin = seg == 0 ? tl_sweep56<T, 1>(E, t, E.w[4], E.q, red)    // q = PM A p ; RQ ; ALP
+                                      : tl_sweep56<T, 2>(E, t, E.w[4], E.v, red);   // v = PM A e ; AMU
+            if (fin && threadIdx.x == 0) {
+                __threadfence();
+                atomicAdd(seg == 0 ? &E.wave->alp : &E.wave->amu, 1u);
+            }
+        } else if (s == 0) {
+            if (seg == 1) tl_eupdate(E, t);              // e = r - ALP q
+            else if (it > 0) tl_pupdate(E, t);           // p (the start set p = r0 before iteration 0)
+        } else if (s == 1) {
+            tl_axsub(E, t, seg == 0 ? (const T*)E.p : (const T*)E.e, E.w[0]);
+        } else {
+            tl_sweep(E, t, s - 2, (const T*)E.w[s - 2], E.w[s - 1]);
+        }
+    }
+    if (s < 6) {
+        __syncthreads();
+        if (threadIdx.x == 0) {
+            __threadfence();
+            atomicAdd(cnt + (long)(seg * 6 + s) * nchunk + t0 / kWaveChunk, (unsigned)(t1 - t0));
+        }
+    }
+    return true;
+}
+
+// K: tiles per item (divides kWaveChunk); slack: rounds of G items between an
+// item and the items it waits for, beyond the gather reach.
+template <typename T, int MINB>
+__global__ void __launch_bounds__(kStepBlock, MINB) k_eng_wave(Eng<T> E, GridBar* gb, int K, int slack) {
+    __shared__ double red[64];
+    WaveCtl* W = E.wave;
+    unsigned* cnt = (unsigned*)(W + 1);
+    const int G = gridDim.x;
+    const int nblk = E.nblk;
+    const int nchunk = (nblk + kWaveChunk - 1) / kWaveChunk;
+    const int D = min(__ldcg(&W->D), nblk);
+    const int nsup = (nblk + K - 1) / K;            // items per stage
+    // lag between stages, in items: beyond the reach (in items, chunk-rounded) by slack rounds
+    const long L = (long)(D + kWaveChunk + K) / K + 1 + (long)slack * ((G + kWaveStages - 1) / kWaveStages);
+    const long nitems = ((long)nsup + (kWaveStages - 1) * L) * kWaveStages;
+    const int cap = sld(E.ctrl + 1) + 2;
+    MemberScalars* S = E.S;
+    for (int it = 0;; it++) {
+        if (it > 0 && !wave_wait_epoch(&W->beta, (unsigned)it, gb)) return;
+        if (sld(&S->done)) return;
+        if (it >= cap) {                        // backstop: ITER stops the member first
+            if (blockIdx.x == 0 && threadIdx.x == 0)
+                stop_member(S, CLOWNS_STOP_MAXITER, sld(&S->mode) == 0 ? CLOWNS_IER_MAXITER : 0);
+            return;
+        }
+        for (int seg = 0; seg < 2; seg++) {
+            for (long q = blockIdx.x; q < nitems; q += G) {
+                const int s = (int)(q % kWaveStages);
+                const long u = q / kWaveStages - (long)s * L;
+                if (u < 0 || u >= nsup) continue;
+                if (!wave_item(E, gb, cnt, nchunk, seg, s, (int)u * K, K, it, D, red)) return;
+            }
+            if (!wave_wait_epoch(seg == 0 ? &W->alp : &W->amu, (unsigned)(it + 1), gb)) return;
+            if (sld(&S->done)) return;
+        }
+        for (int t = blockIdx.x; t < nblk; t += G) {
+            if (tl_xrupdate(E, t, red) && threadIdx.x == 0) {
+                __threadfence();
+                atomicAdd(&W->beta, 1u);
+            }
+        }
     }
 }
 

@@ -163,11 +163,18 @@ int clowns_pcgpme_batched_dev(int m, const clowns_member* members, int precision
                               void* work, size_t work_bytes, void* stream, clowns_solve_info* infos);
 
 /* Execution the autotuner chose for the iteration loop of a row space (m
- * systems of sizes n[], precision as above): threads per block, and either the
- * blocks (all co-resident) and register budget of the persistent kernel, or
- * grid = regs = 0 for the CUDA-graph execution.  CLOWNS_ERR_ARG until a solve
- * of that size has run. */
-int clowns_tuned_shape(int m, const int* n, int precision, int* block, int* grid, int* regs);
+ * systems of sizes n[], precision as above).  mode: CLOWNS_LOOP_PERSISTENT
+ * (one cooperative kernel, phases separated by grid barriers),
+ * CLOWNS_LOOP_GRAPH (a CUDA graph of per-phase kernels chained by programmatic
+ * dependent launch) or CLOWNS_LOOP_WAVE (one cooperative kernel running
+ * (stage, tile) items in wavefront order; single systems only).  block:
+ * threads per block; grid: blocks of the cooperative kernels (0 for the graph);
+ * regs: their register budget per thread (0 for the graph).  CLOWNS_ERR_ARG
+ * until a solve of that size has run. */
+#define CLOWNS_LOOP_PERSISTENT 0
+#define CLOWNS_LOOP_GRAPH 1
+#define CLOWNS_LOOP_WAVE 3
+int clowns_tuned_shape(int m, const int* n, int precision, int* mode, int* block, int* grid, int* regs);
 
 /* Kernels the calling thread's last solve (plain or mixed, single or batched)
  * launched: host launches plus the kernel nodes its loop graphs executed
