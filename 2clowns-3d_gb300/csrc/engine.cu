@@ -228,7 +228,7 @@ static inline int member_groups(int n) {
 
 struct EngLayout {
     long NV = 0;
-    int M = 0, nblk = 0, ngrp = 0, mixed = 0, tsize = 8, wave = 0, nchunk = 0;
+    int M = 0, nblk = 0, ngrp = 0, mixed = 0, tsize = 8, wave = 0, nchunk = 0, n1 = 0;
     size_t o_blk_member, o_blk_rows, o_mem_off, o_mem_n, o_mem_nblk, o_mem_blk0, o_ticket, o_ctrl;
     size_t o_blk_group, o_grp_blk0, o_grp_nblk, o_mem_grp0, o_mem_ngrp, o_gticket, o_gpartials;
     size_t o_in, o_S, o_partials, o_bar, o_al, o_ll, o_d, o_vec[8], o_W, o_x64, o_r64, o_s64, o_t64;
@@ -242,6 +242,7 @@ static EngLayout eng_layout(int M, const int* n, int mixed, int wave = -1) {
     L.M = M;
     L.mixed = mixed;
     L.wave = wave < 0 ? (M == 1) : wave;
+    L.n1 = M == 1 ? n[0] : 0;
     L.tsize = mixed ? 4 : 8;
     long NV = 0;
     int ngrp = 0;
@@ -305,6 +306,7 @@ static Eng<T> eng_bind(void* work, const EngLayout& L) {
     E.NV = L.NV;
     E.M = L.M;
     E.nblk = L.nblk;
+    E.n1 = L.n1;
     E.blk_member = (const int*)(b + L.o_blk_member);
     E.blk_rows = (const int*)(b + L.o_blk_rows);
     E.mem_off = (const int*)(b + L.o_mem_off);

@@ -72,6 +72,7 @@ template <typename T>
 struct Eng {
     long NV;                  // rows of the concatenated space (multiple of kTile)
     int M, nblk;              // members, kTile-blocks of the row space
+    int n1;                   // rows of the system when M == 1
     T* al;                    // 6 columns, stride NV, scaled + sorted
     int* ll;                  // 6 columns, global 0-based indices
     T* d;
@@ -120,14 +121,23 @@ __device__ __forceinline__ int sld(const int* p) { return __ldcg(p); }
 // ---------------------------------------------------------------------------
 // Tile walk helpers
 
+// Member, first row and real rows of tile blk; false for tiles without real
+// rows.  `done` (the member's stop flag) is loaded but not waited for: callers
+// issue their data loads first and test it before any store or reduction, so
+// its latency overlaps theirs.  A single system needs no table loads at all.
 template <typename T>
-__device__ __forceinline__ bool tile_active(const Eng<T>& E, int blk, int& m, long& row0, int& rows) {
-    m = E.blk_member[blk];
-    if (m < 0) return false;
-    rows = E.blk_rows[blk];
-    if (rows == 0) return false;
-    if (sld(&E.S[m].done)) return false;
+__device__ __forceinline__ bool tile_active(const Eng<T>& E, int blk, int& m, long& row0, int& rows, int& done) {
     row0 = (long)blk * kTile;
+    if (E.M == 1) {
+        m = 0;
+        rows = (int)max(0L, min((long)kTile, (long)E.n1 - row0));
+    } else {
+        m = E.blk_member[blk];
+        if (m < 0) return false;
+        rows = E.blk_rows[blk];
+    }
+    if (rows == 0) return false;
+    done = sld(&E.S[m].done);
     return true;
 }
 
@@ -328,7 +338,8 @@ __device__ __forceinline__ void tl_axsub(const Eng<T>& E, int blk, const T* __re
     {
         int m, rows;
         long row0;
-        if (!tile_active(E, blk, m, row0, rows)) return;
+        int done;
+        if (!tile_active(E, blk, m, row0, rows, done)) return;
         for (int base = threadIdx.x; base < rows; base += blockDim.x * R) {
             T s[R];
             bool ok[R];
@@ -354,7 +365,7 @@ __device__ __forceinline__ void tl_axsub(const Eng<T>& E, int blk, const T* __re
             }
 #pragma unroll
             for (int u = 0; u < R; u++)
-                if (ok[u]) out[row0 + base + u * blockDim.x] = s[u];
+                if (ok[u] && !done) out[row0 + base + u * blockDim.x] = s[u];
         }
     }
 }
@@ -375,7 +386,8 @@ __device__ __forceinline__ void tl_sweep(const Eng<T>& E, int blk, int k, const 
     {
         int m, rows;
         long row0;
-        if (!tile_active(E, blk, m, row0, rows)) return;
+        int done;
+        if (!tile_active(E, blk, m, row0, rows, done)) return;
         for (int base = threadIdx.x; base < rows; base += blockDim.x * R) {
             T av[R], xv[R], gv[R];
             int cv[R];
@@ -393,7 +405,7 @@ __device__ __forceinline__ void tl_sweep(const Eng<T>& E, int blk, int k, const 
             for (int u = 0; u < R; u++) gv[u] = ldg2(in + cv[u]);
 #pragma unroll
             for (int u = 0; u < R; u++)
-                if (ok[u]) out[row0 + base + u * blockDim.x] = xv[u] - av[u] * gv[u];
+                if (ok[u] && !done) out[row0 + base + u * blockDim.x] = xv[u] - av[u] * gv[u];
         }
     }
 }
@@ -417,7 +429,8 @@ __device__ __forceinline__ bool tl_sweep56(const Eng<T>& E, int blk, const T* __
     {
         int m, rows;
         long row0;
-        if (!tile_active(E, blk, m, row0, rows)) return false;
+        int done;
+        if (!tile_active(E, blk, m, row0, rows, done)) return false;
         constexpr int R = kRowsPerThread;
         T acc0 = T(0), acc1 = T(0);
         for (int base = threadIdx.x; base < rows; base += blockDim.x * R) {
@@ -442,7 +455,7 @@ __device__ __forceinline__ bool tl_sweep56(const Eng<T>& E, int blk, const T* __
             }
 #pragma unroll
             for (int u = 0; u < R; u++) {
-                if (!ok[u]) continue;
+                if (!ok[u] || done) continue;
                 const long i = row0 + base + u * blockDim.x;
                 const T y = xv[u] - a5v[u] * g5[u] - a6v[u] * g6[u];
                 out[i] = y;
@@ -450,7 +463,7 @@ __device__ __forceinline__ bool tl_sweep56(const Eng<T>& E, int blk, const T* __
                 if (MODE == 2) { acc0 += ldg2(E.e + i) * y; acc1 += y * y; }
             }
         }
-        if (MODE == 0) return false;
+        if (MODE == 0 || done) return false;
         double tot[2];
         if (!member_reduce(E, blk, m, acc0, acc1, red, tot)) return false;
         if (threadIdx.x == 0) {
@@ -493,7 +506,8 @@ __device__ __forceinline__ void tl_eupdate(const Eng<T>& E, int blk) {
     {
         int m, rows;
         long row0;
-        if (!tile_active(E, blk, m, row0, rows)) return;
+        int done;
+        if (!tile_active(E, blk, m, row0, rows, done)) return;
         const T ALP = T(sld(&E.S[m].ALP));
         constexpr int R = kRowsPerThread;
         for (int base = threadIdx.x; base < rows; base += blockDim.x * R) {
@@ -508,7 +522,7 @@ __device__ __forceinline__ void tl_eupdate(const Eng<T>& E, int blk) {
 #pragma unroll
             for (int u = 0; u < R; u++) {
                 const int r = base + u * blockDim.x;
-                if (r < rows) E.e[row0 + r] = rv[u] - ALP * qv[u];
+                if (r < rows && !done) E.e[row0 + r] = rv[u] - ALP * qv[u];
             }
         }
     }
@@ -527,7 +541,8 @@ __device__ __forceinline__ bool tl_xrupdate(const Eng<T>& E, int blk, double* re
     {
         int m, rows;
         long row0;
-        if (!tile_active(E, blk, m, row0, rows)) return false;
+        int done;
+        if (!tile_active(E, blk, m, row0, rows, done)) return false;
         const T ALP = T(sld(&E.S[m].ALP)), AMU = T(sld(&E.S[m].AMU));
         T acc0 = T(0), acc1 = T(0);
         constexpr int R = kRowsPerThread;
@@ -546,7 +561,7 @@ __device__ __forceinline__ bool tl_xrupdate(const Eng<T>& E, int blk, double* re
 #pragma unroll
             for (int u = 0; u < R; u++) {
                 const int r = base + u * blockDim.x;
-                if (r >= rows) continue;
+                if (r >= rows || done) continue;
                 const long i = row0 + r;
                 E.xi[i] = xv[u] + ALP * pv[u] + AMU * ev[u];
                 const T rn = ev[u] - AMU * vv[u];
@@ -555,6 +570,7 @@ __device__ __forceinline__ bool tl_xrupdate(const Eng<T>& E, int blk, double* re
                 acc1 += rn * r0v[u];
             }
         }
+        if (done) return false;
         double tot[2];
         if (!member_reduce(E, blk, m, acc0, acc1, red, tot)) return false;
         if (threadIdx.x == 0) {
@@ -614,7 +630,8 @@ __device__ __forceinline__ void tl_pupdate(const Eng<T>& E, int blk) {
     {
         int m, rows;
         long row0;
-        if (!tile_active(E, blk, m, row0, rows)) return;
+        int done;
+        if (!tile_active(E, blk, m, row0, rows, done)) return;
         const T BETA = T(sld(&E.S[m].BETA)), AMU = T(sld(&E.S[m].AMU));
         constexpr int R = kRowsPerThread;
         for (int base = threadIdx.x; base < rows; base += blockDim.x * R) {
@@ -630,7 +647,7 @@ __device__ __forceinline__ void tl_pupdate(const Eng<T>& E, int blk) {
 #pragma unroll
             for (int u = 0; u < R; u++) {
                 const int r = base + u * blockDim.x;
-                if (r < rows) E.p[row0 + r] = rv[u] + BETA * (pv[u] - AMU * qv[u]);
+                if (r < rows && !done) E.p[row0 + r] = rv[u] + BETA * (pv[u] - AMU * qv[u]);
             }
         }
     }
@@ -649,7 +666,8 @@ __device__ __forceinline__ void ph_initres(const Eng<T>& E) {
     for (int blk = blockIdx.x; blk < E.nblk; blk += gridDim.x) {
         int m, rows;
         long row0;
-        if (!tile_active(E, blk, m, row0, rows)) continue;
+        int done;
+        if (!tile_active(E, blk, m, row0, rows, done) || done) continue;
         T acc0 = T(0), acc1 = T(0);
         for (int r = threadIdx.x; r < rows; r += blockDim.x) {
             const long i = row0 + r;
