@@ -94,7 +94,7 @@ _SIGS = {
                                            C.c_void_p, C.c_void_p, C.c_double, C.c_double, C.c_int,
                                            C.c_void_p, C.c_void_p]),
     "clowns_tuned_shape": (C.c_int, [C.c_int, C.c_void_p, C.c_int, C.c_void_p, C.c_void_p, C.c_void_p,
-                                     C.c_void_p]),
+                                     C.c_void_p, C.c_void_p]),
     "clowns_last_kernel_launches": (C.c_long, []),
     "clowns_session_create": (C.c_int, [C.c_void_p, C.c_void_p, C.c_int, C.c_int, C.c_int] + [C.c_void_p] * 7),
     "clowns_session_set_fields": (C.c_int, [C.c_void_p] * 9),
@@ -337,15 +337,17 @@ PREC_MIXED = 1
 
 def tuned_shape(sizes, precision=0):
     """Execution the autotuner chose for the iteration loop of this row space:
-    {"mode": "graph" | "persistent" | "wave", "block": .., "grid": .., "registers": ..},
+    {"mode": "graph", "block": .., "fused_sweeps": ..} or
+    {"mode": "persistent" | "wave", "block": .., "grid": .., "registers": ..},
     or None before a solve of that size has run."""
     L = lib()
     arr = (C.c_int * len(sizes))(*[int(v) for v in sizes])
-    mo, b, g, r = C.c_int(0), C.c_int(0), C.c_int(0), C.c_int(0)
-    if L.clowns_tuned_shape(len(sizes), arr, precision, C.byref(mo), C.byref(b), C.byref(g), C.byref(r)) != 0:
+    mo, b, g, r, f = C.c_int(0), C.c_int(0), C.c_int(0), C.c_int(0), C.c_int(0)
+    if L.clowns_tuned_shape(len(sizes), arr, precision, C.byref(mo), C.byref(b), C.byref(g), C.byref(r),
+                            C.byref(f)) != 0:
         return None
     if mo.value == 1:
-        return {"mode": "graph", "block": b.value}
+        return {"mode": "graph", "block": b.value, "fused_sweeps": bool(f.value)}
     return {"mode": {0: "persistent", 3: "wave"}.get(mo.value, str(mo.value)), "block": b.value,
             "grid": g.value, "registers": r.value}
 

@@ -411,6 +411,7 @@ static int eng_upload_tables(void* work, const EngLayout& L, const int* n, const
 struct Shape {
     int block = kStepBlock;
     int grid = 0;   // 0: one block per tile
+    int fuse = 1;   // LDUSUB sweeps 1-2 and 3-4 as fused pairs (else four single sweeps)
 };
 
 static std::mutex g_shape_mu;
@@ -423,10 +424,8 @@ static void launch_apply(const Eng<T>& E, const Shape& sh, const T* in, T* out, 
                          cudaStream_t s) {
     const int g = grid_of(sh, E.nblk), b = sh.block;
     k_eng_axsub<T><<<g, b, 0, s>>>(E, in, tmp);
-    k_eng_sweep<T><<<g, b, 0, s>>>(E, 0, tmp, out);
-    k_eng_sweep<T><<<g, b, 0, s>>>(E, 1, out, tmp);
-    k_eng_sweep<T><<<g, b, 0, s>>>(E, 2, tmp, out);
-    k_eng_sweep<T><<<g, b, 0, s>>>(E, 3, out, tmp);
+    k_eng_sweep2<T><<<g, b, 0, s>>>(E, 0, tmp, out);
+    k_eng_sweep2<T><<<g, b, 0, s>>>(E, 2, out, tmp);
     if (mode == 0) k_eng_sweep56<T, 0><<<g, b, 0, s>>>(E, tmp, out);
     if (mode == 1) k_eng_sweep56<T, 1><<<g, b, 0, s>>>(E, tmp, out);
     if (mode == 2) k_eng_sweep56<T, 2><<<g, b, 0, s>>>(E, tmp, out);
@@ -435,10 +434,8 @@ static void launch_apply(const Eng<T>& E, const Shape& sh, const T* in, T* out, 
 template <typename T>
 static void launch_ldusub_inplace(const Eng<T>& E, const Shape& sh, T* vec, T* a, T* bb, cudaStream_t s) {
     const int g = grid_of(sh, E.nblk), b = sh.block;
-    k_eng_sweep<T><<<g, b, 0, s>>>(E, 0, vec, a);
-    k_eng_sweep<T><<<g, b, 0, s>>>(E, 1, a, bb);
-    k_eng_sweep<T><<<g, b, 0, s>>>(E, 2, bb, a);
-    k_eng_sweep<T><<<g, b, 0, s>>>(E, 3, a, bb);
+    k_eng_sweep2<T><<<g, b, 0, s>>>(E, 0, vec, a);
+    k_eng_sweep2<T><<<g, b, 0, s>>>(E, 2, a, bb);
     k_eng_sweep56<T, 0><<<g, b, 0, s>>>(E, bb, vec);
 }
 
@@ -518,9 +515,11 @@ struct LoopShape {
     int graph = 0;    // 1: CUDA graph; 2: host-launched kernels; 3: wavefront kernel
     int wk = 1;       // wavefront: tiles per item
     int wslack = 3;   // wavefront: slack rounds
+    int fuse = 1;     // graph / host launches: fused sweep pairs
 };
 
 // CLOWNS_LOOP_MODE=graph|persistent|launch|wave forces one execution of the loop
+// (with graph and launch, CLOWNS_SWEEP_FUSE=0 selects the four single sweeps)
 // ("launch": the iteration's kernels launched from the host, eight iterations
 // between polls of the stop flags -- the same kernels, visible one by one to a
 // profiler); unset or "auto": the autotuner decides.
@@ -582,10 +581,15 @@ static void g_apply(bool pdl, const Eng<T>& E, const Shape& sh, const T* in, T* 
                     cudaStream_t s) {
     const int g = grid_of(sh, E.nblk), b = sh.block;
     klaunch(pdl, k_eng_axsub<T>, g, b, s, E, in, tmp);
-    klaunch(pdl, k_eng_sweep<T>, g, b, s, E, 0, (const T*)tmp, out);
-    klaunch(pdl, k_eng_sweep<T>, g, b, s, E, 1, (const T*)out, tmp);
-    klaunch(pdl, k_eng_sweep<T>, g, b, s, E, 2, (const T*)tmp, out);
-    klaunch(pdl, k_eng_sweep<T>, g, b, s, E, 3, (const T*)out, tmp);
+    if (sh.fuse) {
+        klaunch(pdl, k_eng_sweep2<T>, g, b, s, E, 0, (const T*)tmp, out);
+        klaunch(pdl, k_eng_sweep2<T>, g, b, s, E, 2, (const T*)out, tmp);
+    } else {
+        klaunch(pdl, k_eng_sweep<T>, g, b, s, E, 0, (const T*)tmp, out);
+        klaunch(pdl, k_eng_sweep<T>, g, b, s, E, 1, (const T*)out, tmp);
+        klaunch(pdl, k_eng_sweep<T>, g, b, s, E, 2, (const T*)tmp, out);
+        klaunch(pdl, k_eng_sweep<T>, g, b, s, E, 3, (const T*)out, tmp);
+    }
     if (mode == 0) klaunch(pdl, k_eng_sweep56<T, 0>, g, b, s, E, (const T*)tmp, out);
     if (mode == 1) klaunch(pdl, k_eng_sweep56<T, 1>, g, b, s, E, (const T*)tmp, out);
     if (mode == 2) klaunch(pdl, k_eng_sweep56<T, 2>, g, b, s, E, (const T*)tmp, out);
@@ -605,9 +609,9 @@ static void g_iteration(bool pdl, const Eng<T>& E, const Shape& sh, cudaStream_t
 struct GraphKey {
     const void* work;
     long NV;
-    int M, prec;
+    int M, prec, fuse;
     bool operator<(const GraphKey& o) const {
-        return std::tie(work, NV, M, prec) < std::tie(o.work, o.NV, o.M, o.prec);
+        return std::tie(work, NV, M, prec, fuse) < std::tie(o.work, o.NV, o.M, o.prec, o.fuse);
     }
 };
 static std::mutex g_graph_mu;
@@ -634,7 +638,7 @@ void release_graphs_for(const void* work) {
 
 // WHILE { iteration ; guard } captured into a fresh graph
 template <typename T>
-static int build_loop_graph(const Eng<T>& E, bool pdl, cudaGraphExec_t* out) {
+static int build_loop_graph(const Eng<T>& E, bool pdl, int fuse, cudaGraphExec_t* out) {
     if (!g_cap) CLOWNS_CUDA_TRY(cudaStreamCreateWithFlags(&g_cap, cudaStreamNonBlocking));
     cudaGraph_t graph;
     CLOWNS_CUDA_TRY(cudaGraphCreate(&graph, 0));
@@ -648,7 +652,8 @@ static int build_loop_graph(const Eng<T>& E, bool pdl, cudaGraphExec_t* out) {
     CLOWNS_CUDA_TRY(cudaGraphAddNode(&cnode, graph, nullptr, nullptr, 0, &cp));
     cudaGraph_t body = cp.conditional.phGraph_out[0];
     CLOWNS_CUDA_TRY(cudaStreamBeginCaptureToGraph(g_cap, body, nullptr, nullptr, 0, cudaStreamCaptureModeThreadLocal));
-    const Shape sh;
+    Shape sh;
+    sh.fuse = fuse;
     g_iteration(pdl, E, sh, g_cap);
     klaunch(pdl, k_eng_guard, 1, 256, g_cap, E.S, E.M, E.ctrl, h);
     cudaGraph_t captured;
@@ -672,14 +677,14 @@ static int build_loop_graph(const Eng<T>& E, bool pdl, cudaGraphExec_t* out) {
 }
 
 template <typename T>
-static int loop_graph(const Eng<T>& E, const void* work, int prec, cudaGraphExec_t* out) {
+static int loop_graph(const Eng<T>& E, const void* work, int prec, int fuse, cudaGraphExec_t* out) {
     std::lock_guard<std::mutex> lk(g_graph_mu);
-    GraphKey key{work, E.NV, E.M, prec};
+    GraphKey key{work, E.NV, E.M, prec, fuse};
     auto it = g_graphs.find(key);
     if (it != g_graphs.end()) { *out = it->second; return CLOWNS_OK; }
     cudaGraphExec_t ex;
-    int rc = build_loop_graph(E, true, &ex);              // programmatic edges
-    if (rc) rc = build_loop_graph(E, false, &ex);         // plain edges if refused
+    int rc = build_loop_graph(E, true, fuse, &ex);              // programmatic edges
+    if (rc) rc = build_loop_graph(E, false, fuse, &ex);         // plain edges if refused
     if (rc) return rc;
     if (g_graphs.size() >= 64) {
         cudaGraphExecDestroy(g_graphs.begin()->second);
@@ -693,13 +698,14 @@ static int loop_graph(const Eng<T>& E, const void* work, int prec, cudaGraphExec
 // Kernels the calling thread's last solve launched (host launches plus the
 // kernel nodes executed inside loop graphs).
 static thread_local long t_launches = 0;
-constexpr int kIterKernels = 15;    // two operator applications (6 each) + 3 vector updates
-constexpr int kBodyKernels = kIterKernels + 1;   // + the loop guard
+// Kernels of one iteration: two operator applications (4 with fused sweep
+// pairs, else 6) + 3 vector updates; a graph body adds the loop guard.
+static int iter_kernels(int fuse) { return fuse ? 11 : 15; }
 
 // Kernel launches of one run_loop call, given the loop bodies it executed.
 static long loop_launches(const LoopShape& sh, long bodies) {
-    if (sh.graph == 1) return bodies * kBodyKernels;
-    if (sh.graph == 2) return bodies * kIterKernels;
+    if (sh.graph == 1) return bodies * (iter_kernels(sh.fuse) + 1);
+    if (sh.graph == 2) return bodies * iter_kernels(sh.fuse);
     return 1;
 }
 
@@ -707,7 +713,8 @@ template <typename T>
 static int run_loop(Eng<T> E, const void* work, GridBar* gb, int prec, const LoopShape& sh, cudaStream_t s) {
     if (sh.graph == 2) {
         CLOWNS_CUDA_TRY(cudaMemsetAsync(gb, 0, sizeof(GridBar), s));
-        const Shape ksh;
+        Shape ksh;
+        ksh.fuse = sh.fuse;
         int cap = 0;
         CLOWNS_CUDA_TRY(cudaMemcpyAsync(&cap, E.ctrl + 1, sizeof(int), cudaMemcpyDeviceToHost, s));
         CLOWNS_CUDA_TRY(cudaStreamSynchronize(s));
@@ -744,7 +751,7 @@ static int run_loop(Eng<T> E, const void* work, GridBar* gb, int prec, const Loo
     }
     if (sh.graph) {
         cudaGraphExec_t ex;
-        int rc = loop_graph(E, work, prec, &ex);
+        int rc = loop_graph(E, work, prec, sh.fuse, &ex);
         if (rc) return rc;
         CLOWNS_CUDA_TRY(cudaMemsetAsync(gb, 0, sizeof(GridBar), s));
         CLOWNS_CUDA_TRY(cudaGraphLaunch(ex, s));
@@ -782,6 +789,8 @@ static int tune_loop(Eng<T> E, const void* work, GridBar* gb, long key_nv, int k
     if (forced == 1 || forced == 2) {
         LoopShape sh;
         sh.graph = forced;
+        const char* fz = getenv("CLOWNS_SWEEP_FUSE");     // forced executions: fused pairs unless "0"
+        sh.fuse = !(fz && !strcmp(fz, "0"));
         *out = sh;
         return CLOWNS_OK;
     }
@@ -840,9 +849,12 @@ static int tune_loop(Eng<T> E, const void* work, GridBar* gb, long key_nv, int k
         }
     }
     if (forced < 0 || (forced == 3 && !wave_ok)) {     // forced wave: ensembles keep the graph
-        LoopShape gsh;
-        gsh.graph = 1;
-        cands.push_back(gsh);
+        for (int fuse : {1, 0}) {
+            LoopShape gsh;
+            gsh.graph = 1;
+            gsh.fuse = fuse;
+            cands.push_back(gsh);
+        }
     }
     if (cands.empty()) {
         set_last_error_msg("pcgpme: the forced loop execution does not serve this system");
@@ -877,8 +889,8 @@ static int tune_loop(Eng<T> E, const void* work, GridBar* gb, long key_nv, int k
     return CLOWNS_OK;
 }
 
-// mode: 0 persistent, 1 CUDA graph, 3 wavefront
-int engine_tuned_shape(long nv, int prec, int single, int* mode, int* block, int* grid, int* minb) {
+// mode: 0 persistent, 1 CUDA graph, 3 wavefront; fuse: fused sweep pairs (graph)
+int engine_tuned_shape(long nv, int prec, int single, int* mode, int* block, int* grid, int* minb, int* fuse) {
     std::lock_guard<std::mutex> lk(g_loop_mu);
     auto it = g_loop_shapes.find(std::make_tuple(nv, prec, single));
     if (it == g_loop_shapes.end()) return CLOWNS_ERR_ARG;
@@ -887,6 +899,7 @@ int engine_tuned_shape(long nv, int prec, int single, int* mode, int* block, int
     *block = sh.block;
     *grid = sh.graph == 1 ? 0 : sh.grid;
     *minb = sh.graph == 1 ? 0 : sh.minb;
+    *fuse = sh.graph == 1 ? sh.fuse : 0;
     return CLOWNS_OK;
 }
 
@@ -1006,7 +1019,7 @@ int engine_solve_plain(int M, const MemberIn* ins, double eps, double parm, int 
     t_launches = 0;
     prime(s, eps_r, iter_r);
     start(s);
-    t_launches += 2 + 12;
+    t_launches += 2 + 8;
     CLOWNS_CUDA_TRY(cudaGetLastError());
     rc = run_loop(E, work, gb, 0, sh, s);
     if (rc) return rc;

@@ -115,6 +115,11 @@ struct Eng {
 
 template <typename V>
 __device__ __forceinline__ V ldg2(const V* p) { return *p; }
+
+// c - a b with one rounding (the sweeps' update, written out so that fused and
+// separate sweeps round identically)
+__device__ __forceinline__ double fnma(double a, double b, double c) { return __fma_rn(-a, b, c); }
+__device__ __forceinline__ float fnma(float a, float b, float c) { return __fmaf_rn(-a, b, c); }
 __device__ __forceinline__ double sld(const double* p) { return __ldcg(p); }
 __device__ __forceinline__ int sld(const int* p) { return __ldcg(p); }
 
@@ -405,7 +410,7 @@ __device__ __forceinline__ void tl_sweep(const Eng<T>& E, int blk, int k, const 
             for (int u = 0; u < R; u++) gv[u] = ldg2(in + cv[u]);
 #pragma unroll
             for (int u = 0; u < R; u++)
-                if (ok[u] && !done) out[row0 + base + u * blockDim.x] = xv[u] - av[u] * gv[u];
+                if (ok[u] && !done) out[row0 + base + u * blockDim.x] = fnma(av[u], gv[u], xv[u]);
         }
     }
 }
@@ -413,6 +418,66 @@ __device__ __forceinline__ void tl_sweep(const Eng<T>& E, int blk, int k, const 
 template <typename T>
 __device__ __forceinline__ void ph_sweep(const Eng<T>& E, int k, const T* __restrict__ in, T* __restrict__ out) {
     for (int blk = blockIdx.x; blk < E.nblk; blk += gridDim.x) tl_sweep(E, blk, k, in, out);
+}
+
+// Two consecutive single-neighbour sweeps k, k+1 in one pass:
+//   o = in - AL_k in[LL_k] ;  out = o - AL_k+1 o[LL_k+1]
+// The value of o at the gathered row j = LL_k+1(i) is recomputed from in, AL_k
+// and LL_k at j with the same fused multiply-add, so the result equals two
+// separate sweeps bit for bit while the intermediate vector never goes to
+// memory and one kernel boundary goes away.  The zero row (j = pad) has
+// AL = 0, LL = pad and in = 0, so its o is 0 as it must be.
+template <typename T>
+__device__ __forceinline__ void tl_sweep2(const Eng<T>& E, int blk, int k, const T* __restrict__ in,
+                                          T* __restrict__ out) {
+    constexpr int R = kRowsPerThread;
+    const long NV = E.NV;
+    const T* __restrict__ a0 = E.al + k * NV;
+    const int* __restrict__ c0 = E.ll + k * NV;
+    const T* __restrict__ a1 = a0 + NV;
+    const int* __restrict__ c1 = c0 + NV;
+    {
+        int m, rows;
+        long row0;
+        int done;
+        if (!tile_active(E, blk, m, row0, rows, done)) return;
+        for (int base = threadIdx.x; base < rows; base += blockDim.x * R) {
+            T x[R], aa[R], ab[R], xj[R], aj[R];
+            int ca[R], cb[R], cj[R];
+            bool ok[R];
+#pragma unroll
+            for (int u = 0; u < R; u++) {
+                const int r = base + u * blockDim.x;
+                ok[u] = r < rows;
+                const long i = row0 + (ok[u] ? r : 0);
+                x[u] = ldg2(in + i);
+                aa[u] = ld_stream(a0 + i);
+                ca[u] = ld_stream(c0 + i);
+                ab[u] = ld_stream(a1 + i);
+                cb[u] = ld_stream(c1 + i);
+            }
+#pragma unroll
+            for (int u = 0; u < R; u++) {
+                xj[u] = ldg2(in + cb[u]);
+                aj[u] = ldg2(a0 + cb[u]);
+                cj[u] = ldg2(c0 + cb[u]);
+            }
+            T oi[R], oj[R];
+#pragma unroll
+            for (int u = 0; u < R; u++) {
+                oi[u] = fnma(aa[u], ldg2(in + ca[u]), x[u]);
+                oj[u] = fnma(aj[u], ldg2(in + cj[u]), xj[u]);
+            }
+#pragma unroll
+            for (int u = 0; u < R; u++)
+                if (ok[u] && !done) out[row0 + base + u * blockDim.x] = fnma(ab[u], oj[u], oi[u]);
+        }
+    }
+}
+
+template <typename T>
+__device__ __forceinline__ void ph_sweep2(const Eng<T>& E, int k, const T* __restrict__ in, T* __restrict__ out) {
+    for (int blk = blockIdx.x; blk < E.nblk; blk += gridDim.x) tl_sweep2(E, blk, k, in, out);
 }
 
 // Last sweep (J=5,6, 306-318) with an optional fused per-member reduction:
@@ -457,7 +522,7 @@ __device__ __forceinline__ bool tl_sweep56(const Eng<T>& E, int blk, const T* __
             for (int u = 0; u < R; u++) {
                 if (!ok[u] || done) continue;
                 const long i = row0 + base + u * blockDim.x;
-                const T y = xv[u] - a5v[u] * g5[u] - a6v[u] * g6[u];
+                const T y = fnma(a6v[u], g6[u], fnma(a5v[u], g5[u], xv[u]));
                 out[i] = y;
                 if (MODE == 1) acc0 += ldg2(E.r0 + i) * y;
                 if (MODE == 2) { acc0 += ldg2(E.e + i) * y; acc1 += y * y; }
@@ -713,6 +778,12 @@ __global__ void __launch_bounds__(kEngBlock) k_eng_sweep(Eng<T> E, int k, const 
     pdl_enter();
     ph_sweep(E, k, in, out);
 }
+template <typename T>
+__global__ void __launch_bounds__(kEngBlock) k_eng_sweep2(Eng<T> E, int k, const T* __restrict__ in,
+                                                         T* __restrict__ out) {
+    pdl_enter();
+    ph_sweep2(E, k, in, out);
+}
 template <typename T, int MODE>
 __global__ void __launch_bounds__(kEngBlock) k_eng_sweep56(Eng<T> E, const T* __restrict__ in, T* __restrict__ out) {
     pdl_enter();
@@ -816,13 +887,9 @@ template <typename T>
 __device__ __forceinline__ bool ph_apply(const Eng<T>& E, GridBar* gb, const T* in, T* out, T* tmp, int mode) {
     ph_axsub(E, in, tmp);
     if (!grid_sync(gb)) return false;
-    ph_sweep(E, 0, tmp, out);
+    ph_sweep2(E, 0, tmp, out);
     if (!grid_sync(gb)) return false;
-    ph_sweep(E, 1, out, tmp);
-    if (!grid_sync(gb)) return false;
-    ph_sweep(E, 2, tmp, out);
-    if (!grid_sync(gb)) return false;
-    ph_sweep(E, 3, out, tmp);
+    ph_sweep2(E, 2, out, tmp);
     if (!grid_sync(gb)) return false;
     if (mode == 0) ph_sweep56<T, 0>(E, tmp, out);
     if (mode == 1) ph_sweep56<T, 1>(E, tmp, out);
@@ -835,13 +902,9 @@ template <typename T, int MINB>
 __global__ void __launch_bounds__(kEngBlock, MINB) k_eng_loop(Eng<T> E, GridBar* gb, int init) {
     if (init) {
         // b^ = PM W b in place on p (sweeps p->t->q->t->q->p)
-        ph_sweep(E, 0, E.p, E.t);
+        ph_sweep2(E, 0, E.p, E.t);
         if (!grid_sync(gb)) return;
-        ph_sweep(E, 1, E.t, E.q);
-        if (!grid_sync(gb)) return;
-        ph_sweep(E, 2, E.q, E.t);
-        if (!grid_sync(gb)) return;
-        ph_sweep(E, 3, E.t, E.q);
+        ph_sweep2(E, 2, E.t, E.q);
         if (!grid_sync(gb)) return;
         ph_sweep56<T, 0>(E, E.q, E.p);
         if (!grid_sync(gb)) return;

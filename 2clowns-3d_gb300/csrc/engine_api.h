@@ -20,7 +20,7 @@ int engine_setup_export(const MemberIn& in, double parm, double* al_s, int* ll_s
 int engine_apply_pm_a(const MemberIn& in, double parm, const double* x, double* y, void* work,
                       size_t work_bytes, cudaStream_t s);
 void release_all_graphs();
-int engine_tuned_shape(long nv, int prec, int single, int* mode, int* block, int* grid, int* minb);
+int engine_tuned_shape(long nv, int prec, int single, int* mode, int* block, int* grid, int* minb, int* fuse);
 long engine_row_space(int M, const int* n, int mixed);
 long engine_last_launches();
 void release_graphs_for(const void* work);

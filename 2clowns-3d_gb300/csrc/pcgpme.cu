@@ -95,14 +95,15 @@ extern "C" int clowns_apply_pm_a_dev(const double* al, int nl, int na, const int
     return engine_apply_pm_a(in, parm, x, y, work, work_bytes, (cudaStream_t)stream);
 }
 
-extern "C" int clowns_tuned_shape(int m, const int* n, int precision, int* mode, int* block, int* grid, int* regs) {
-    if (m < 1 || !n || !mode || !block || !grid || !regs) {
+extern "C" int clowns_tuned_shape(int m, const int* n, int precision, int* mode, int* block, int* grid, int* regs,
+                                  int* fused) {
+    if (m < 1 || !n || !mode || !block || !grid || !regs || !fused) {
         set_last_error_msg("tuned_shape: invalid arguments");
         return CLOWNS_ERR_ARG;
     }
     const int mixed = precision == CLOWNS_PREC_MIXED;
     int minb = 0;
-    int rc = engine_tuned_shape(engine_row_space(m, n, mixed), mixed, m == 1, mode, block, grid, &minb);
+    int rc = engine_tuned_shape(engine_row_space(m, n, mixed), mixed, m == 1, mode, block, grid, &minb, fused);
     if (rc) {
         set_last_error_msg("tuned_shape: no solve of this size has run yet");
         return rc;

@@ -42,10 +42,24 @@ def measured_peaks():
     return 6800.0, "fallback"
 
 
+# Algorithmic bytes per row, w = bytes per stored word (8 FP64, 4 FP32); column
+# indices are 4-byte streams.  Gathered neighbour values are not counted (the
+# row's own value is).  One operator application PM A x:
+#   axsub   D, 6 AL, x, y                     9w + 6 indices
+#   sweeps  4 x (AL_k, in, out)              12w + 4 indices
+#   sweep56 AL5, AL6, in, out, dot vector     5w + 2 indices       -> 26w + 48 B
+# One iteration: 2 applications + e (3w) + x,r (7w) + p (4w)        -> 66w + 96 B
+# (fused sweep pairs read the same streams once, so the count is the same).
+# Setup + start of a solve: caller's matrix, b, x (96 B) + scaled copies (7w + 24 B)
+# + r, p, x (3w) + b^ = PM W b (16w + 24 B) + q = PM A x0 (25w + 48 B) + r, p, r0 (5w)
+#   -> 56w + 192 B;  copy-out w + 8 B.
+def bytes_iteration(w: int) -> float:
+    return 66.0 * w + 96.0
+
+
 def bytes_solve_fp64(n: int, iters: int) -> float:
-    """Algorithmic bytes of one FP64 solve: N (62 + 68 iters) words of 8 B
-    (floating-point streams only; see the design doc for the per-part count)."""
-    return float(n) * (62 + 68 * iters) * 8.0
+    """Algorithmic bytes of one FP64 solve (counted above)."""
+    return float(n) * (56 * 8 + 192 + 8 + 8 + bytes_iteration(8) * iters)
 
 
 class Clocks:
@@ -166,9 +180,13 @@ def run_reference(args, world, rank):
 
 
 def bytes_solve_mixed(n: int, inner_iters: int, outer: int) -> float:
-    """Algorithmic bytes of one mixed solve: N [96 + sum_outer(248 + 272 it_j) + 100 outer]
-    = N [96 + 248 outer + 272 iters + 100 outer] (FP32 words of 4 B, FP64 refinement)."""
-    return float(n) * (96 + 248 * outer + 272 * inner_iters + 100 * outer)
+    """Algorithmic bytes of one mixed solve: FP32 inner iterations (w = 4) plus,
+    per refinement sweep, the FP64 residual W (b - A x) from the caller's FP64
+    matrix (6 AL, 6 indices, D, b, x, W, r: 112 B), PM r on FP64 vectors with
+    FP32 coefficients (128 B), the inner right-hand side (24 B) and the FP64
+    accumulation (20 B); setup: caller's matrix (96 B), FP32 copies and FP64
+    W, x, r (76 B), ||PM W b|| (128 B); copy-out 16 B."""
+    return float(n) * (96 + 76 + 128 + 16 + (112 + 128 + 24 + 20) * outer + bytes_iteration(4) * inner_iters)
 
 
 def time_device(fn, steps, stream):

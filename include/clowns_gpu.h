@@ -169,12 +169,14 @@ int clowns_pcgpme_batched_dev(int m, const clowns_member* members, int precision
  * dependent launch) or CLOWNS_LOOP_WAVE (one cooperative kernel running
  * (stage, tile) items in wavefront order; single systems only).  block:
  * threads per block; grid: blocks of the cooperative kernels (0 for the graph);
- * regs: their register budget per thread (0 for the graph).  CLOWNS_ERR_ARG
- * until a solve of that size has run. */
+ * regs: their register budget per thread (0 for the graph); fused: 1 when the
+ * graph runs LDUSUB's sweeps 1-2 and 3-4 as fused pairs.  CLOWNS_ERR_ARG until
+ * a solve of that size has run. */
 #define CLOWNS_LOOP_PERSISTENT 0
 #define CLOWNS_LOOP_GRAPH 1
 #define CLOWNS_LOOP_WAVE 3
-int clowns_tuned_shape(int m, const int* n, int precision, int* mode, int* block, int* grid, int* regs);
+int clowns_tuned_shape(int m, const int* n, int precision, int* mode, int* block, int* grid, int* regs,
+                       int* fused);
 
 /* Kernels the calling thread's last solve (plain or mixed, single or batched)
  * launched: host launches plus the kernel nodes its loop graphs executed
