@@ -74,7 +74,10 @@ __global__ void __launch_bounds__(kEngBlock) k_mx_sweep(Eng<T> E, int k, const d
 // Last sweep on FP64 vectors with the squared norm of the result per member.
 //   PHASE 0: BN64 = ||PM W b||^2
 //   PHASE 1: ERR64 = sqrt(||PM r||^2 / BN64); stop the member at the outer
-//            tolerance or sweep cap, else arm its inner solve (mode 1).
+//            tolerance or sweep cap, else arm its inner solve (mode 1) with
+//            the relative reduction the outer tolerance still needs, halved
+//            for margin, but no tighter than inner_tol: the last sweep then
+//            stops near EPS64 instead of overshooting by up to inner_tol.
 template <typename T, int PHASE>
 __global__ void __launch_bounds__(kEngBlock) k_mx_sweep56(Eng<T> E, const double* __restrict__ in,
                                                          double* __restrict__ out, double inner_tol,
@@ -122,7 +125,7 @@ __global__ void __launch_bounds__(kEngBlock) k_mx_sweep56(Eng<T> E, const double
                     S->ERRP = 0.0;
                     S->done = 0;
                     S->mode = 1;
-                    S->EPS = inner_tol;
+                    S->EPS = fmax(inner_tol, 0.5 * S->EPS64 / err);
                     S->ITER = inner_max;
                 }
             }

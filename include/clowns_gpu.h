@@ -129,8 +129,10 @@ int clowns_pcgpme_dev(const double* al, int nl, int na, const int* ll, const dou
  * sorted coefficients and the Krylov vectors of an inner BiCGSTAB are stored in
  * FP32.  An FP64 outer loop forms r = W (b - A x) from the caller's original FP64
  * matrix, measures ERR = ||PM r|| / ||PM W b|| (the reference's EPS definition)
- * in FP64, solves PM W A d = PM r / ||PM r|| in FP32 to inner_tol (<= 0: 1e-4),
- * and accumulates x += ||PM r|| d in FP64, until ERR <= eps.  info->iter counts
+ * in FP64, solves PM W A d = PM r / ||PM r|| in FP32 to the relative residual
+ * max(inner_tol, eps / (2 ERR)) (inner_tol <= 0: 1e-4) -- no further than the
+ * outer tolerance still needs -- and accumulates x += ||PM r|| d in FP64, until
+ * ERR <= eps.  info->iter counts
  * inner iterations, info->outer the refinement sweeps; IER = 3000 after
  * max_outer sweeps (<= 0: 30).  inner_max <= 0: 2000. */
 size_t clowns_pcgpme_mixed_workspace_bytes(int n, int nl);
