@@ -19,6 +19,7 @@ from __future__ import annotations
 import argparse
 import json
 import os
+import platform
 import pathlib
 import statistics
 import subprocess
@@ -42,24 +43,34 @@ def measured_peaks():
     return 6800.0, "fallback"
 
 
-# Algorithmic bytes per row, w = bytes per stored word (8 FP64, 4 FP32); column
-# indices are 4-byte streams.  Gathered neighbour values are not counted (the
-# row's own value is).  One operator application PM A x:
-#   axsub   D, 6 AL, x, y                     9w + 6 indices
-#   sweeps  4 x (AL_k, in, out)              12w + 4 indices
-#   sweep56 AL5, AL6, in, out, dot vector     5w + 2 indices       -> 26w + 48 B
-# One iteration: 2 applications + e (3w) + x,r (7w) + p (4w)        -> 66w + 96 B
-# (fused sweep pairs read the same streams once, so the count is the same).
-# Setup + start of a solve: caller's matrix, b, x (96 B) + scaled copies (7w + 24 B)
-# + r, p, x (3w) + b^ = PM W b (16w + 24 B) + q = PM A x0 (25w + 48 B) + r, p, r0 (5w)
-#   -> 56w + 192 B;  copy-out w + 8 B.
-def bytes_iteration(w: int) -> float:
-    return 66.0 * w + 96.0
+# Algorithmic bytes (the fixed count roofline.achieved uses): floating-point
+# streams only, at the stored word size w (8 FP64, 4 FP32); index traffic and
+# gathered neighbour values are not counted.  One operator application PM A x:
+# AXSUB D + 6 AL + x + y = 9w, LDUSUB sweeps 1-4 3w each = 12w, sweep 5/6
+# AL5 + AL6 + in + out = 4w -> 25w.  One iteration: 2 applications (50w) + RQ 2w
+# + e 3w + AMU/SS 2w + x/r 7w + p 4w = 68w.  Setup of a solve: scaling 16w,
+# PM b 16w, PM A x0 25w, r0 pass 5w = 62w.  So FP64: N (496 + 544 iters).
+# Mixed: N [96 + sum over sweeps (248 + 272 inner iters) + 100 per sweep]
+# (FP32 inner iterations; 100 B per sweep for the FP64 refinement residual and
+# accumulation; 96 B for the FP64 -> FP32 conversion).
+# Measured DRAM bytes per row and iteration of the loop graph (ncu, the graph as
+# one unit, beach_256x256x96): profiles/pcgpme_loop_dram_beach_256x256x96.md.
+TRAFFIC_ROW_ITER_FP64 = 434.2
+TRAFFIC_ROW_ITER_MIXED = 248.9
 
 
 def bytes_solve_fp64(n: int, iters: int) -> float:
-    """Algorithmic bytes of one FP64 solve (counted above)."""
-    return float(n) * (56 * 8 + 192 + 8 + 8 + bytes_iteration(8) * iters)
+    return float(n) * (496 + 544 * iters)
+
+
+def bytes_solve_mixed(n: int, inner_iters: int, outer: int) -> float:
+    return float(n) * (96 + 248 * outer + 272 * inner_iters + 100 * outer)
+
+
+# The same count with the 4-byte column-index streams added (6 + 4 + 2 per
+# application: 96 B per iteration, 72 B in the setup), reported beside it.
+def bytes_solve_fp64_with_indices(n: int, iters: int) -> float:
+    return float(n) * (496 + 72 + (544 + 96) * iters)
 
 
 class Clocks:
@@ -172,6 +183,7 @@ def run_reference(args, world, rank):
         "vs_baseline": None, "dtype": "f64", "data": "synthetic (seeded generator)",
         "config": {"workload": WORKLOAD, "rows": sy.mnoe, "tol": case.eps0, "iters": last.iters},
         "cpu_baseline": {"value": value, "unit": "solves/s", "cores": threads, "kind": "port",
+                         "cpu_model": cpu_model(),
                          "sample": f"full solves of {WORKLOAD} (N={sy.mnoe}, {last.iters} iterations), "
                                    f"OpenMP restatement of pcgpme_para.F90, {threads} threads"},
         "e2e": {"value": value, "unit": "solves/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
@@ -179,14 +191,31 @@ def run_reference(args, world, rank):
     print(json.dumps(line), flush=True)
 
 
-def bytes_solve_mixed(n: int, inner_iters: int, outer: int) -> float:
-    """Algorithmic bytes of one mixed solve: FP32 inner iterations (w = 4) plus,
-    per refinement sweep, the FP64 residual W (b - A x) from the caller's FP64
-    matrix (6 AL, 6 indices, D, b, x, W, r: 112 B), PM r on FP64 vectors with
-    FP32 coefficients (128 B), the inner right-hand side (24 B) and the FP64
-    accumulation (20 B); setup: caller's matrix (96 B), FP32 copies and FP64
-    W, x, r (76 B), ||PM W b|| (128 B); copy-out 16 B."""
-    return float(n) * (96 + 76 + 128 + 16 + (112 + 128 + 24 + 20) * outer + bytes_iteration(4) * inner_iters)
+def true_residual(ds, x):
+    """||b - A x|| / ||b|| of the assembled (unscaled, unpreconditioned) system,
+    evaluated on the device with torch outside the timed region (alu/llu are
+    (6, mm2) column blocks, llu 1-based with 0 = no neighbour)."""
+    import torch
+    n = ds.mnoe
+    xv = x[:n]
+    ax = ds.de[:n] * xv
+    for k in range(ds.alu.shape[0]):
+        c = ds.llu[k, :n].long()
+        g = torch.where(c > 0, xv[(c - 1).clamp(min=0)], torch.zeros_like(xv))
+        ax = ax + ds.alu[k, :n] * g
+    b = ds.b[:n]
+    return float(torch.linalg.norm(b - ax) / torch.linalg.norm(b))
+
+
+def cpu_model() -> str:
+    try:
+        out = subprocess.run(["lscpu"], capture_output=True, text=True, timeout=10).stdout
+        for line in out.splitlines():
+            if line.startswith("Model name:"):
+                return line.split(":", 1)[1].strip()
+    except (OSError, subprocess.SubprocessError):
+        pass
+    return platform.processor() or platform.machine()
 
 
 def time_device(fn, steps, stream):
@@ -363,6 +392,7 @@ def run_gpu(args, world, rank, local):
     alg = bytes_solve_fp64(n, it)
     achieved = alg / per_solve_s / 1e9
     x_plain = x[:n].cpu().numpy().copy()
+    args.res_plain = true_residual(ds, x)
 
     legs = set(args.legs.split(","))
     if "apply" in legs:
@@ -414,6 +444,7 @@ def run_mixed(pkg, args, ds, case, world, stream):
     m_value = world * args.steps / (ms_m / 1000.0)
     m_alg = bytes_solve_mixed(n, minfo.iter, minfo.outer)
     x_mixed = xm[:n].cpu().numpy().copy()
+    args.res_mixed = true_residual(ds, xm)
     return m_value, ms_m, minfo, m_alg, x_mixed
 
 
@@ -452,9 +483,17 @@ def _report(pkg, args, world, rank, case, n, ms, infos, info, it, value, alg, ac
         cls, sm, sy = ora.prepare(case)
         threads = os.cpu_count() or 1
         t, r = cpu_reference_solve(ora, sy, case.eps0, threads)
+        # one thread: setup + 30 iterations, scaled to the full solve's iteration count
+        k1 = 30
+        t0 = time.perf_counter()
+        ora.pcgpme(sy.alu, sy.llu, sy.de[1:], sy.b[1:], sy.mnoe, eps=case.eps0, itmax=k1, nthreads=1)
+        t1 = (time.perf_counter() - t0) * (r.iters + 1) / (k1 + 1)
         cpu = {"value": 1.0 / t, "unit": "solves/s", "cores": threads, "kind": "port",
+               "cpu_model": cpu_model(),
                "sample": f"one full solve of {args.workload} (N={sy.mnoe}, {r.iters} iterations), OpenMP "
-                         f"restatement of pcgpme_para.F90 on {threads} threads"}
+                         f"restatement of pcgpme_para.F90 on {threads} threads",
+               "one_thread": {"value": 1.0 / t1, "unit": "solves/s",
+                              "sample": f"setup + {k1} iterations on 1 thread, scaled to {r.iters} iterations"}}
         nrm = np.linalg.norm(r.x)
         err_plain = float(np.linalg.norm(x_plain - r.x) / nrm)
         if x_mixed is not None:
@@ -468,12 +507,15 @@ def _report(pkg, args, world, rank, case, n, ms, infos, info, it, value, alg, ac
             "data": "synthetic (seeded generator)",
             "config": {"workload": args.workload, "rows": n, "tol": case.eps0, "iters": it,
                        "stop": pkg.STOP_NAMES.get(info.reason), "eps": info.eps,
-                       "rel_l2_vs_oracle": err_plain,
+                       "rel_l2_vs_oracle": err_plain, "true_rel_residual": args.res_plain,
                        "l2": "inputs larger than L2 (matrix %.0f MB)" % (n * 80 / 1e6),
                        "path": "plain FP64", "parallelism": f"replicas x{world}"},
             "roofline": {"bound": "hbm", "kernel": "pcgpme FP64 solve (one graph launch)",
                          "achieved": achieved, "peak": peak, "peak_kind": peak_kind, "unit": "GB/s",
-                         "frac": achieved / peak, "traffic": None,
+                         "frac": achieved / peak, "traffic": TRAFFIC_ROW_ITER_FP64 * n * it,
+                         "traffic_source": "ncu DRAM bytes of the loop graph per row-iteration, "
+                                           "profiles/pcgpme_loop_dram_beach_256x256x96.md",
+                         "frac_with_index_streams": bytes_solve_fp64_with_indices(n, it) / alg * achieved / peak,
                          "algorithmic_bytes_per_solve": alg},
             "e2e": {"value": e2e_value, "unit": "solves/s", "h2d_bytes_per_step": h2d,
                     "d2h_bytes_per_step": d2h},
@@ -484,8 +526,10 @@ def _report(pkg, args, world, rank, case, n, ms, infos, info, it, value, alg, ac
         if minfo is not None:
             line["mixed"] = {"value": m_value, "unit": "solves/s", "speedup_vs_fp64": m_value / value,
                              "inner_iters": minfo.iter, "outer": minfo.outer, "eps": minfo.eps,
-                             "rel_l2_vs_oracle": err_mixed, "ms_per_solve": ms_m / args.steps,
+                             "rel_l2_vs_oracle": err_mixed, "true_rel_residual": args.res_mixed,
+                             "ms_per_solve": ms_m / args.steps,
                              "achieved_gbs": m_alg / (ms_m / 1000.0 / args.steps) / 1e9,
+                             "traffic": TRAFFIC_ROW_ITER_MIXED * n * minfo.iter,
                              "algorithmic_bytes_per_solve": m_alg}
         if cpu:
             line["cpu_baseline"] = cpu
