@@ -780,10 +780,13 @@ static int check_abort(GridBar* gb, cudaStream_t s) {
     return CLOWNS_OK;
 }
 
-// Autotuner: time eight iterations of the loop for each candidate -- the
-// persistent kernel at two register budgets and three grid sizes, and the
-// graph -- on the actual row space; cache the fastest per (row-space size,
-// precision).  `prime` re-creates the state the loop starts from.
+// Autotuner: time kTuneIters iterations of the loop for each candidate -- the
+// graph with fused and with single sweep pairs, the persistent kernel and the
+// wavefront kernel -- on the actual row space, in four rounds over all
+// candidates (the first warms up and builds the graphs); cache the candidate
+// with the smallest best-of-three time per (row-space size, precision).
+// `prime` re-creates the state the loop starts from.
+constexpr int kTuneIters = 24;
 template <typename T, typename Prime>
 static int tune_loop(Eng<T> E, const void* work, GridBar* gb, long key_nv, int key_prec, Prime prime,
                      cudaStream_t s, LoopShape* out) {
@@ -809,15 +812,22 @@ static int tune_loop(Eng<T> E, const void* work, GridBar* gb, long key_nv, int k
         if (it != g_loop_shapes.end()) { *out = it->second; return CLOWNS_OK; }
     }
     std::vector<LoopShape> cands;
+    // Automatic tuning keeps one shape each of the wavefront and persistent
+    // kernels (their other shapes never came close on 0.1-8.5 M-row systems);
+    // CLOWNS_LOOP_MODE=wave|persistent times all of them.
+    const bool all_shapes = forced >= 0;
     if (wave_ok && (forced < 0 || forced == 3)) {
-        for (int minb : {8, 12}) {
+        for (int minb : {12, 8}) {
             if (pinned && minb != pm) continue;
+            if (!pinned && !all_shapes && minb != 12) continue;
             int gmax = 0;
             int rc = loop_max_grid<T>(kStepBlock, minb, &gmax, true);
             if (rc) return rc;
             for (int frac : {4, 3}) {
                 if (pinned && frac != pf) continue;
-                for (int wk : {1, 2}) {
+                if (!pinned && !all_shapes && frac != 4) continue;
+                for (int wk : {2, 1}) {
+                    if (!pinned && !all_shapes && wk != 2) continue;
                     if (pinned && wk != pk) continue;
                     LoopShape sh;
                     sh.graph = 3;
@@ -840,10 +850,12 @@ static int tune_loop(Eng<T> E, const void* work, GridBar* gb, long key_nv, int k
         }
     }
     if (forced < 0 || forced == 0) for (int minb : {8, 4}) {
+        if (!all_shapes && minb != 8) continue;
         int gmax = 0;
         int rc = loop_max_grid<T>(kStepBlock, minb, &gmax);
         if (rc) return rc;
         for (int frac : {4, 3, 2}) {
+            if (!all_shapes && frac != 4) continue;
             LoopShape sh;
             sh.block = kStepBlock;
             sh.minb = minb;
@@ -866,24 +878,31 @@ static int tune_loop(Eng<T> E, const void* work, GridBar* gb, long key_nv, int k
     cudaEvent_t e0, e1;
     CLOWNS_CUDA_TRY(cudaEventCreate(&e0));
     CLOWNS_CUDA_TRY(cudaEventCreate(&e1));
-    LoopShape best = cands[0];
-    float best_ms = 1e30f;
-    for (const LoopShape& sh : cands) {
-        float ms = 0.f;
-        bool ok = true;
-        for (int rep = 0; rep < 2 && ok; rep++) {
+    std::vector<float> best_of(cands.size(), 1e30f);
+    std::vector<char> failed(cands.size(), 0);
+    for (int round = 0; round < 4; round++) {
+        for (size_t c = 0; c < cands.size(); c++) {
+            if (failed[c]) continue;
             prime(s);
             CLOWNS_CUDA_TRY(cudaEventRecord(e0, s));
-            int rc = run_loop(E, work, gb, key_prec, sh, s);
-            if (rc) { ok = false; break; }
+            if (run_loop(E, work, gb, key_prec, cands[c], s)) {
+                cudaGetLastError();
+                failed[c] = 1;
+                continue;
+            }
             CLOWNS_CUDA_TRY(cudaEventRecord(e1, s));
             CLOWNS_CUDA_TRY(cudaEventSynchronize(e1));
+            float ms = 0.f;
             CLOWNS_CUDA_TRY(cudaEventElapsedTime(&ms, e0, e1));
             int rc2 = check_abort(gb, s);
             if (rc2) return rc2;
+            if (round > 0) best_of[c] = std::min(best_of[c], ms);
         }
-        if (ok && ms < best_ms) { best_ms = ms; best = sh; }
     }
+    LoopShape best = cands[0];
+    float best_ms = 1e30f;
+    for (size_t c = 0; c < cands.size(); c++)
+        if (!failed[c] && best_of[c] < best_ms) { best_ms = best_of[c]; best = cands[c]; }
     cudaEventDestroy(e0);
     cudaEventDestroy(e1);
     std::lock_guard<std::mutex> lk(g_loop_mu);
@@ -1016,8 +1035,8 @@ int engine_solve_plain(int M, const MemberIn* ins, double eps, double parm, int 
         k_eng_initres<double><<<grid_of(ksh, E.nblk), ksh.block, 0, cs>>>(E);
     };
     LoopShape sh;
-    // tuning runs: eight iterations from the real start (not counted as the solve's launches)
-    rc = tune_loop(E, work, gb, L.NV, 0, [&](cudaStream_t cs) { prime(cs, 1e-300, 8); start(cs); }, s, &sh);
+    // tuning runs: kTuneIters iterations from the real start (not counted as the solve's launches)
+    rc = tune_loop(E, work, gb, L.NV, 0, [&](cudaStream_t cs) { prime(cs, 1e-300, kTuneIters); start(cs); }, s, &sh);
     if (rc) return rc;
     t_launches = 0;
     prime(s, eps_r, iter_r);
@@ -1083,7 +1102,8 @@ int engine_solve_mixed(int M, const MemberIn* ins, double eps, double parm, doub
         k_mx_normalize<float><<<kg, ksh.block, 0, cs>>>(E);
     };
     LoopShape sh;
-    rc = tune_loop(E, work, gb, L.NV, 1, [&](cudaStream_t cs) { setup(cs); sweep_head(cs, 1e-30, 8); }, s, &sh);
+    rc = tune_loop(E, work, gb, L.NV, 1, [&](cudaStream_t cs) { setup(cs); sweep_head(cs, 1e-30, kTuneIters); },
+                   s, &sh);
     if (rc) return rc;
     t_launches = 0;
     setup(s);
