@@ -56,7 +56,7 @@ def measured_peaks():
 # Measured DRAM bytes per row and iteration of the loop graph (ncu, the graph as
 # one unit, beach_256x256x96): profiles/pcgpme_loop_dram_beach_256x256x96.md.
 TRAFFIC_ROW_ITER_FP64 = 434.2
-TRAFFIC_ROW_ITER_MIXED = 248.9
+TRAFFIC_ROW_ITER_MIXED = 249.2
 
 
 def bytes_solve_fp64(n: int, iters: int) -> float:
