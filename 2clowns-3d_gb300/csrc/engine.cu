@@ -417,8 +417,6 @@ struct Shape {
     int fuse = 1;   // LDUSUB sweeps 1-2 and 3-4 as fused pairs (else four single sweeps)
 };
 
-static std::mutex g_shape_mu;
-static std::map<std::pair<long, int>, Shape> g_shapes;
 
 static int grid_of(const Shape& sh, int nblk) { return sh.grid > 0 ? std::min(sh.grid, nblk) : nblk; }
 
@@ -463,53 +461,18 @@ static void launch_ldusub64(const Eng<T>& E, const Shape& sh, double inner_tol, 
     k_mx_sweep56<T, PHASE><<<g, b, 0, s>>>(E, E.t64, E.r64, inner_tol, inner_max);
 }
 
-// Time candidate shapes on one operator application; keep the fastest.
-template <typename T>
-static Shape autotune(const Eng<T>& E, long key_nv, int key_prec, cudaStream_t s) {
-    {
-        std::lock_guard<std::mutex> lk(g_shape_mu);
-        auto it = g_shapes.find({key_nv, key_prec});
-        if (it != g_shapes.end()) return it->second;
-    }
-    std::vector<Shape> cands;
-    for (int b : {128, 256})
-        for (int g : {0, kNumSMs * 4, kNumSMs * 8, kNumSMs * 16}) {
-            Shape sh;
-            sh.block = b;
-            sh.grid = g;
-            cands.push_back(sh);
-        }
-    cudaEvent_t e0, e1;
-    cudaEventCreate(&e0);
-    cudaEventCreate(&e1);
-    Shape best;
-    float best_ms = 1e30f;
-    for (const Shape& sh : cands) {
-        launch_apply(E, sh, E.p, E.q, E.t, 0, s);      // warm
-        cudaEventRecord(e0, s);
-        for (int rep = 0; rep < 3; rep++) launch_apply(E, sh, E.p, E.q, E.t, 0, s);
-        cudaEventRecord(e1, s);
-        cudaEventSynchronize(e1);
-        float ms = 0.f;
-        cudaEventElapsedTime(&ms, e0, e1);
-        if (ms < best_ms) { best_ms = ms; best = sh; }
-    }
-    cudaEventDestroy(e0);
-    cudaEventDestroy(e1);
-    std::lock_guard<std::mutex> lk(g_shape_mu);
-    g_shapes[{key_nv, key_prec}] = best;
-    return best;
-}
-
 // ---------------------------------------------------------------------------
-// The iteration loop, executed one of two ways (the autotuner times both on the
-// actual row space and keeps the faster):
-//   persistent: one cooperative launch of k_eng_loop; phases separated by grid
-//               barriers (no launch gaps, static tile assignment);
+// The iteration loop, executed one of three ways (the autotuner times them on
+// the actual row space and keeps the fastest):
 //   graph:      a CUDA graph whose WHILE node repeats the iteration's kernels,
 //               chained by programmatic dependent launch (dynamic scheduling,
 //               full occupancy, launch latency overlapped with the previous
-//               kernel's tail).
+//               kernel's tail), with fused or single LDUSUB sweep pairs;
+//   persistent: one cooperative launch of k_eng_loop; phases separated by grid
+//               barriers (no launch gaps, static tile assignment);
+//   wavefront:  one cooperative launch of k_eng_wave (single systems); (stage,
+//               tile) items ordered by gather reach, per-chunk completion
+//               counters instead of phase-wide barriers.
 
 struct LoopShape {
     int block = kStepBlock;

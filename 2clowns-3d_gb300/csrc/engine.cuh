@@ -784,8 +784,15 @@ __global__ void __launch_bounds__(kEngBlock) k_eng_sweep2(Eng<T> E, int k, const
     pdl_enter();
     ph_sweep2(E, k, in, out);
 }
+// Register budget of the dot-product kernels: the FP32 instances are held to
+// 48 registers (10 blocks of 128 threads per SM, no spills; 2-3 % faster inner
+// iterations measured), the FP64 instances keep their 61-64 (a cap spills and
+// was 4-13 % slower).
+template <typename T>
+constexpr int kReduceMinBlocks = sizeof(T) == 4 ? 5 : 0;   // blocks of kEngBlock threads (0: no bound)
+
 template <typename T, int MODE>
-__global__ void __launch_bounds__(kEngBlock) k_eng_sweep56(Eng<T> E, const T* __restrict__ in, T* __restrict__ out) {
+__global__ void __launch_bounds__(kEngBlock, kReduceMinBlocks<T>) k_eng_sweep56(Eng<T> E, const T* __restrict__ in, T* __restrict__ out) {
     pdl_enter();
     ph_sweep56<T, MODE>(E, in, out);
 }
@@ -795,7 +802,7 @@ __global__ void __launch_bounds__(kEngBlock) k_eng_eupdate(Eng<T> E) {
     ph_eupdate(E);
 }
 template <typename T>
-__global__ void __launch_bounds__(kEngBlock) k_eng_xrupdate(Eng<T> E) {
+__global__ void __launch_bounds__(kEngBlock, kReduceMinBlocks<T>) k_eng_xrupdate(Eng<T> E) {
     pdl_enter();
     ph_xrupdate(E);
 }
