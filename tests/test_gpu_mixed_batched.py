@@ -59,6 +59,30 @@ def test_mixed_matches_fp64_oracle(gpu, ora, systems, idx):
             assert err <= max(1e-9, 2 * err_oracle), (label, err, err_oracle, info.as_dict())
 
 
+@pytest.mark.parametrize("precision", ["fp64", "mixed"])
+def test_fused_kernels_bit_identical(gpu, systems, monkeypatch, precision):
+    """The fused LDUSUB sweep pairs (sweep J recomputed at the one row sweep J+1
+    gathers) round exactly like the separate sweeps: forcing the CUDA-graph loop
+    with and without them gives the same iterations and the same solution bit
+    for bit, in FP64 and in the FP32 inner solve."""
+    label, case, sy, ds = systems[1]
+    n = ds.mnoe
+    monkeypatch.setenv("CLOWNS_LOOP_MODE", "graph")
+    out = []
+    for fuse in ("0", "1"):
+        monkeypatch.setenv("CLOWNS_SWEEP_FUSE", fuse)
+        x = _x(ds)
+        if precision == "fp64":
+            info = gpu.Solver(n).solve(ds.alu, ds.llu, ds.de, ds.b, x, eps=1e-12)
+        else:
+            info = gpu.MixedSolver(n).solve(ds.alu, ds.llu, ds.de, ds.b, x, eps=1e-12)
+        assert info.ier == 0, info.as_dict()
+        out.append((info.iter, x.cpu().numpy()[:n].copy()))
+    for it, xv in out[1:]:
+        assert it == out[0][0]
+        assert np.array_equal(xv, out[0][1])
+
+
 def test_mixed_true_residual(gpu, ora, systems):
     """Unpreconditioned true residual of the mixed solution is at the FP64 level."""
     label, case, sy, ds = systems[1]
