@@ -62,6 +62,15 @@ _SIGS = {
     "pcgpme_gpu": (None, [C.c_void_p] * 13),
     "pcgpme_": (None, [C.c_void_p] * 13),
     "clowns_pcgpme_workspace_bytes": (C.c_size_t, [C.c_int, C.c_int]),
+    "pcgpme_will_gpu": (C.c_int, [C.c_void_p] * 11),
+    "pcgpme_will_": (C.c_int, [C.c_void_p] * 11),
+    "clowns_pcgpme_will_workspace_bytes": (C.c_size_t, [C.c_int, C.c_int]),
+    "clowns_pcgpme_will_dev": (C.c_int, [C.c_void_p, C.c_int, C.c_int, C.c_void_p, C.c_void_p, C.c_int,
+                                         C.c_void_p, C.c_double, C.c_double, C.c_int, C.c_void_p, C.c_size_t,
+                                         C.c_void_p, C.c_void_p]),
+    "clowns_will_postprocess_workspace_bytes": (C.c_size_t, [C.c_int]),
+    "clowns_will_postprocess_dev": (C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_int, C.c_int, C.c_int,
+                                              C.c_void_p, C.c_void_p, C.c_void_p, C.c_size_t, C.c_void_p]),
     "clowns_pcgpme_dev": (C.c_int, [C.c_void_p, C.c_int, C.c_int, C.c_void_p, C.c_void_p, C.c_int,
                                     C.c_void_p, C.c_void_p, C.c_double, C.c_double, C.c_int,
                                     C.c_void_p, C.c_size_t, C.c_void_p, C.c_void_p]),
@@ -168,6 +177,25 @@ def pcgpme(al: np.ndarray, ll: np.ndarray, d: np.ndarray, b: np.ndarray, x: np.n
                  C.addressof(c_n), C.addressof(c_n2), b.ctypes.data, x.ctypes.data, e.ctypes.data,
                  C.addressof(c_parm), C.addressof(c_it), C.addressof(c_ier))
     return float(e[0]), c_it.value, c_ier.value
+
+
+def pcgpme_will(al: np.ndarray, ll: np.ndarray, d: np.ndarray, b: np.ndarray, n: int, eps: float = 1e-10,
+                parm: float = 5.0, itmax: int = 10000, n2: int = 64) -> np.ndarray:
+    """PCGPME_WILL (the 2DH solve) through ``pcgpme_will_gpu`` with HOST arrays.
+    ``al``/``ll``: (nl, na) C-order == AL(NA,NL); ``b`` (rows 1..n at [0..n)) is
+    the right-hand side and is overwritten with what the reference leaves in B."""
+    L = lib()
+    nl, na = al.shape
+    assert al.dtype == np.float64 and ll.dtype == np.int32 and al.flags.c_contiguous and ll.flags.c_contiguous
+    assert b.dtype == np.float64 and b.flags.c_contiguous
+    c_nl, c_na, c_n, c_n2, c_it = C.c_int(nl), C.c_int(na), C.c_int(n), C.c_int(n2), C.c_int(itmax)
+    c_eps, c_parm = C.c_double(eps), C.c_double(parm)
+    d = np.ascontiguousarray(d, dtype=np.float64)
+    rc = L.pcgpme_will_gpu(al.ctypes.data, C.addressof(c_nl), C.addressof(c_na), ll.ctypes.data, d.ctypes.data,
+                           C.addressof(c_n), C.addressof(c_n2), b.ctypes.data, C.addressof(c_eps),
+                           C.addressof(c_parm), C.addressof(c_it))
+    _check(rc, "pcgpme_will_gpu")
+    return b
 
 
 # ---------------------------------------------------------------------------
@@ -586,3 +614,38 @@ class Session:
             self.close()
         except Exception:
             pass
+
+
+class WillSolver:
+    """Device-resident PCGPME_WILL (the 2DH dispersion solve) of one size."""
+
+    def __init__(self, n: int, nl: int = 4):
+        torch = _torch()
+        self.n, self.nl = n, nl
+        self.bytes = int(lib().clowns_pcgpme_will_workspace_bytes(n, nl))
+        self.work = torch.empty(max(self.bytes, 1), dtype=torch.uint8, device="cuda")
+
+    def solve(self, al, ll, d, b, eps: float = 1e-10, parm: float = 5.0, itmax: int = 10000) -> SolveInfo:
+        """al/ll: (nl, na) device tensors; b (device, >= n) is overwritten with
+        the reference's B output."""
+        info = SolveInfo()
+        nl, na = al.shape
+        rc = lib().clowns_pcgpme_will_dev(_ptr(al), nl, na, _ptr(ll), _ptr(d), self.n, _ptr(b), eps, parm, itmax,
+                                          _ptr(self.work), self.bytes, _stream(), C.byref(info))
+        _check(rc, "clowns_pcgpme_will_dev")
+        return info
+
+
+def will_postprocess_dev(x, r, ll, n: int):
+    """The post-processing of pcgpme_2DH.f90:268-279 on device vectors x, r
+    (ll: (nl, na) device tensor); returns (x_out, b) device tensors."""
+    torch = _torch()
+    nl, na = ll.shape
+    b = torch.empty(n, dtype=torch.float64, device="cuda")
+    xo = torch.empty(n, dtype=torch.float64, device="cuda")
+    nb = int(lib().clowns_will_postprocess_workspace_bytes(n))
+    work = torch.empty(nb, dtype=torch.uint8, device="cuda")
+    rc = lib().clowns_will_postprocess_dev(_ptr(x), _ptr(r), _ptr(ll), nl, na, n, _ptr(b), _ptr(xo), _ptr(work), nb,
+                                           _stream())
+    _check(rc, "clowns_will_postprocess_dev")
+    return xo, b

@@ -892,6 +892,10 @@ long engine_row_space(int M, const int* n, int mixed) { return eng_layout(M, n, 
 
 long engine_last_launches() { return t_launches; }
 
+double* engine_residual_ptr(void* work, int n) {
+    return (double*)((char*)work + eng_layout(1, &n, 0).o_vec[0]);
+}
+
 // ---------------------------------------------------------------------------
 // Solves
 
@@ -965,7 +969,7 @@ static int check_members(int M, const MemberIn* ins, std::vector<int>& n, int* n
 // Plain FP64 (reference method and stop tests) over M members: setup kernel,
 // one persistent launch for PCGPME's start and its whole iteration loop, copy-out.
 int engine_solve_plain(int M, const MemberIn* ins, double eps, double parm, int iter, void* work,
-                       size_t work_bytes, cudaStream_t s, clowns_solve_info* info) {
+                       size_t work_bytes, cudaStream_t s, clowns_solve_info* info, int variant) {
     std::vector<int> n;
     int nl = 6;
     int rc = check_members(M, ins, n, &nl);
@@ -979,6 +983,15 @@ int engine_solve_plain(int M, const MemberIn* ins, double eps, double parm, int 
     double eps_r, P1, P2;
     int iter_r;
     params(maxn, eps, parm, iter, &eps_r, &iter_r, &P1, &P2);
+    const int mode = variant == 2 ? 2 : 0;
+    if (variant == 2) {              // PCGPME_WILL: no EPS substitution, no ITER default
+        if (iter < 1) {
+            set_last_error_msg("pcgpme_will: iter must be at least 1");
+            return CLOWNS_ERR_ARG;
+        }
+        eps_r = eps;
+        iter_r = iter;
+    }
     rc = eng_upload_tables(work, L, n.data(), ins, s);
     if (rc) return rc;
     Eng<double> E = eng_bind<double>(work, L);
@@ -986,7 +999,7 @@ int engine_solve_plain(int M, const MemberIn* ins, double eps, double parm, int 
     const int gs = std::min(L.nblk * 2, kEngMaxGrid * 4);
     auto prime = [&](cudaStream_t cs, double e, int it) {
         if (E.wave) cudaMemsetAsync(&E.wave->D, 0, sizeof(int), cs);
-        k_eng_init_scalars<<<1, 256, 0, cs>>>(E.S, M, e, it, 0, E.ctrl);
+        k_eng_init_scalars<<<1, 256, 0, cs>>>(E.S, M, e, it, mode, E.ctrl);
         if (nl == 6) k_eng_setup<double, 6><<<gs, kEngBlock, 0, cs>>>(E, P1, P2, 0);
         else k_eng_setup<double, 4><<<gs, kEngBlock, 0, cs>>>(E, P1, P2, 0);
     };

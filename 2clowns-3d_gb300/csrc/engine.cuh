@@ -53,7 +53,7 @@ struct MemberScalars {
     int done;       // stop test fired (or member excluded)
     int reason;     // CLOWNS_STOP_*
     int ier;
-    int mode;       // 0: reference stop tests; 1: inner solve of the refinement loop
+    int mode;       // 0: PCGPME; 1: inner solve of the refinement loop; 2: PCGPME_WILL (2DH)
     int bad_index;  // an input column index was outside 0..n
     int total_iter; // iterations summed over refinement sweeps
 };
@@ -541,7 +541,7 @@ __device__ __forceinline__ bool tl_sweep56(const Eng<T>& E, int blk, const T* __
                 S->ALP = ALP;
                 if (!isfinite(tot[0]) || !isfinite(ALP)) {
                     S->K = sld(&S->K) + 1;
-                    stop_member(S, CLOWNS_STOP_NONFINITE, sld(&S->mode) == 0 ? CLOWNS_IER_NONFINITE : 0);
+                    stop_member(S, CLOWNS_STOP_NONFINITE, sld(&S->mode) != 1 ? CLOWNS_IER_NONFINITE : 0);
                 }
             } else {
                 S->SS = tot[1];
@@ -549,7 +549,7 @@ __device__ __forceinline__ bool tl_sweep56(const Eng<T>& E, int blk, const T* __
                 S->AMU = AMU;
                 if (!isfinite(tot[1]) || !isfinite(AMU)) {
                     S->K = sld(&S->K) + 1;
-                    stop_member(S, CLOWNS_STOP_NONFINITE, sld(&S->mode) == 0 ? CLOWNS_IER_NONFINITE : 0);
+                    stop_member(S, CLOWNS_STOP_NONFINITE, sld(&S->mode) != 1 ? CLOWNS_IER_NONFINITE : 0);
                 }
             }
             __threadfence();
@@ -653,7 +653,7 @@ __device__ __forceinline__ bool tl_xrupdate(const Eng<T>& E, int blk, double* re
             const double ERR = sqrt(RN / BN);                            // 215
             S->ERR = ERR;
             if (!isfinite(RN) || !isfinite(C1)) {
-                stop_member(S, CLOWNS_STOP_NONFINITE, mode == 0 ? CLOWNS_IER_NONFINITE : 0);
+                stop_member(S, CLOWNS_STOP_NONFINITE, mode != 1 ? CLOWNS_IER_NONFINITE : 0);
             } else if (K >= 10 && fabs(ERR - ERRP) <= ERR * 1.0e-6) {    // 228
                 stop_member(S, CLOWNS_STOP_STAGNATION, 0);
             } else if (ERR <= EPS) {                                     // 232
@@ -665,9 +665,10 @@ __device__ __forceinline__ bool tl_xrupdate(const Eng<T>& E, int blk, double* re
                 } else if (C1 == 0.0) {                                  // 240
                     stop_member(S, CLOWNS_STOP_C1_ZERO, 0);
                 } else {
-                    S->BETA = C1 / AMUs / RQ;                            // 241
+                    // 241 (pcgpme_para.F90); PCGPME_WILL forms C1 / (AMU RQ), pcgpme_2DH.f90:255
+                    S->BETA = mode == 2 ? C1 / (AMUs * RQ) : C1 / AMUs / RQ;
                     if (K >= ITER) {                                     // 250-254
-                        if (mode == 0) {
+                        if (mode != 1) {
                             stop_member(S, CLOWNS_STOP_MAXITER, CLOWNS_IER_MAXITER);
                             S->K = ITER + 1;
                         } else {
@@ -834,7 +835,7 @@ static __global__ void k_eng_guard(MemberScalars* S, int M, int* ctrl, cudaGraph
         if (go && ctrl[0] > ctrl[1] + 1) {
             go = 0;
             for (int m = 0; m < M; m++)
-                if (!S[m].done) stop_member(S + m, CLOWNS_STOP_MAXITER, S[m].mode == 0 ? CLOWNS_IER_MAXITER : 0);
+                if (!S[m].done) stop_member(S + m, CLOWNS_STOP_MAXITER, S[m].mode != 1 ? CLOWNS_IER_MAXITER : 0);
         }
         cudaGraphSetConditional(h, go ? 1u : 0u);
     }
@@ -1080,7 +1081,7 @@ __global__ void __launch_bounds__(kStepBlock, MINB) k_eng_wave(Eng<T> E, GridBar
         if (sld(&S->done)) return;
         if (it >= cap) {                        // backstop: ITER stops the member first
             if (blockIdx.x == 0 && threadIdx.x == 0)
-                stop_member(S, CLOWNS_STOP_MAXITER, sld(&S->mode) == 0 ? CLOWNS_IER_MAXITER : 0);
+                stop_member(S, CLOWNS_STOP_MAXITER, sld(&S->mode) != 1 ? CLOWNS_IER_MAXITER : 0);
             return;
         }
         for (int seg = 0; seg < 2; seg++) {

@@ -10,8 +10,12 @@ namespace clowns {
 struct MemberIn;
 
 size_t engine_workspace_bytes(int M, const int* n, int mixed);
+// variant 0: PCGPME (pcgpme_para.F90); 2: PCGPME_WILL's iteration (pcgpme_2DH.f90:
+// BETA = C1 / (AMU RQ), eps and iter taken as given, iter >= 1).
 int engine_solve_plain(int M, const MemberIn* ins, double eps, double parm, int iter, void* work,
-                       size_t work_bytes, cudaStream_t s, clowns_solve_info* info);
+                       size_t work_bytes, cudaStream_t s, clowns_solve_info* info, int variant = 0);
+// FP64 recursive residual r of a single-system solve left in its workspace.
+double* engine_residual_ptr(void* work, int n);
 int engine_solve_mixed(int M, const MemberIn* ins, double eps, double parm, double inner_tol,
                        int inner_max, int max_outer, void* work, size_t work_bytes, cudaStream_t s,
                        clowns_solve_info* info);

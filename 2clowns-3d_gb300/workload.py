@@ -339,3 +339,58 @@ def ensemble_case(spec: dict) -> Case:
                       slope=spec["slope"], n_obstacles=spec["n_obstacles"],
                       amplitude=spec["amplitude"],
                       label=f"member_{spec['nx']}x{spec['ny']}x{spec['nz']}")
+
+
+# ---------------------------------------------------------------------------
+# 2DH dispersion systems (the matrix PCGPME_WILL solves, pcgpme_2DH.f90), built
+# like disp_param (1sub-2DH-initial_reset.f90:470-506): one row per wet cell of
+# an nx x ny plan grid; per direction (x, then y) a cell on the domain edge gets
+# no entries, otherwise its wet minus and plus neighbours are packed into the
+# next slots of AL(NA,4) / LL(NA,4) (NA = N, LL 1-based, zeros only after the
+# last neighbour) with AL = A 2 h^2 / (dx (dx + dx)), and DIAG = -1 - sum(AL).
+# The depth h varies, so rows differ in scale.  Dry cells (a seeded island and
+# a shoreline band) are not rows.
+
+
+@dataclasses.dataclass
+class DispersionSystem:
+    al: np.ndarray      # (4, n) float64
+    ll: np.ndarray      # (4, n) int32
+    d: np.ndarray       # (n,)
+    b: np.ndarray       # (n,)
+    n: int
+    nx: int
+    ny: int
+
+
+def dispersion_system(nx: int, ny: int, seed: int = 7, dx: float = 0.5, A: float = 1.0 / 3.0) -> DispersionSystem:
+    rng = np.random.default_rng(seed)
+    xs = (np.arange(nx) + 0.5) / nx
+    ys = (np.arange(ny) + 0.5) / ny
+    X, Y = np.meshgrid(xs, ys, indexing="ij")
+    h = 0.2 + 2.0 * X + 0.3 * np.sin(6.0 * Y) * X          # depth, shallow near x = 0
+    wet = h > 0.25
+    cx, cy, r = rng.uniform(0.4, 0.7), rng.uniform(0.3, 0.7), rng.uniform(0.05, 0.12)
+    wet &= (X - cx) ** 2 + (Y - cy) ** 2 > r * r           # island
+    num = -np.ones((nx, ny), dtype=np.int64)
+    idx = np.argwhere(wet.T)                                # row order: i fastest within j
+    for row, (j, i) in enumerate(idx):
+        num[i, j] = row
+    n = len(idx)
+    al = np.zeros((4, n))
+    ll = np.zeros((4, n), dtype=np.int32)
+    d = -np.ones(n)
+    for row, (j, i) in enumerate(idx):
+        hc = h[i, j]
+        jj = 0
+        for (lo, hi) in (((i - 1, j), (i + 1, j)), ((i, j - 1), (i, j + 1))):
+            if not (0 <= lo[0] and 0 <= lo[1] and hi[0] < nx and hi[1] < ny):
+                continue                                    # domain edge in this direction
+            for (ii, kk) in (lo, hi):
+                if num[ii, kk] >= 0:
+                    al[jj, row] = A * 2.0 * hc * hc / dx / (dx + dx)
+                    ll[jj, row] = num[ii, kk] + 1
+                    jj += 1
+        d[row] -= al[:, row].sum()
+    b = rng.normal(0.0, 1.0, n) * np.exp(-((idx[:, 1] / nx - 0.5) ** 2) * 20.0)
+    return DispersionSystem(al=al, ll=ll, d=d, b=b, n=n, nx=nx, ny=ny)

@@ -186,6 +186,40 @@ int clowns_tuned_shape(int m, const int* n, int precision, int* mode, int* block
  * Engine bookkeeping with no counterpart in the reference. */
 long clowns_last_kernel_launches(void);
 
+/* PCGPME_WILL, the 2DH dispersion solve (replaces src2LOWNS/pcgpme_2DH.f90:1-374,
+ * called at 1sub-2DH-momentum.f90:325 as PCGPME_WILL(L%AL,4,L%indisp,L%LL,
+ * L%DIAG,L%indisp,64,PSI,eps0,PARM,ITER)).  The same preconditioned BiCGSTAB
+ * as PCGPME on an NL = 4 (or 6) matrix with BETA = C1 / (AMU RQ) (line 255),
+ * x0 = 0 and EPS used as given; AL, LL and D are not modified.  On return B
+ * holds what the reference leaves there (265-279): the solution with
+ * |x| <= 1e-14 set to 0 and x(i) replaced by a neighbour's value when they
+ * differ by at most 1e-14 (lower rows already processed, in row order), and,
+ * for a row whose neighbour loop ends before writing B (its first LL is 0, or
+ * its neighbours are itself or equal to it), the last recursive residual.
+ * The reference has no error argument: these return 0 or a CLOWNS_ERR_* code
+ * (ignored by a Fortran CALL) and leave B unchanged on error.  iter >= 1.
+ * pcgpme_will_ is the name ifort gives the subroutine (link-level drop-in). */
+int pcgpme_will_gpu(const double* al, const int* nl, const int* na, const int* ll, const double* d,
+                    const int* n, const int* n2, double* b, const double* eps, const double* parm,
+                    const int* iter);
+int pcgpme_will_(const double* al, const int* nl, const int* na, const int* ll, const double* d,
+                 const int* n, const int* n2, double* b, const double* eps, const double* parm,
+                 const int* iter);
+/* Device-resident PCGPME_WILL: device arrays, b in/out, a workspace of
+ * clowns_pcgpme_will_workspace_bytes(n, nl) bytes; info (may be NULL) as for
+ * clowns_pcgpme_dev (ier 3000 when ITER was reached, which the reference does
+ * not report). */
+size_t clowns_pcgpme_will_workspace_bytes(int n, int nl);
+int clowns_pcgpme_will_dev(const double* al, int nl, int na, const int* ll, const double* d, int n,
+                           double* b, double eps, double parm, int iter, void* work, size_t work_bytes,
+                           void* stream, clowns_solve_info* info);
+/* Test hook: the post-processing of pcgpme_2DH.f90:268-279 alone, on a
+ * solution x and residual r (device arrays of n), ll as the caller's LL:
+ * writes b and, if x_out is not NULL, the processed x. */
+size_t clowns_will_postprocess_workspace_bytes(int n);
+int clowns_will_postprocess_dev(const double* x, const double* r, const int* ll, int nl, int na, int n,
+                                double* b, double* x_out, void* work, size_t work_bytes, void* stream);
+
 /* Test hooks of the solve's building blocks (device pointers; workspace sized by
  * clowns_pcgpme_workspace_bytes(n, nl)).  clowns_pcgpme_setup_dev performs only
  * the row scaling and per-row sort of pcgpme_para.F90:77-112 and copies the

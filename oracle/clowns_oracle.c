@@ -624,6 +624,130 @@ done:
     free(LLTEMP);
 }
 
+/* ------------------------------------------------------------------------- */
+/* PCGPME_WILL (src2LOWNS/pcgpme_2DH.f90:1-374), the 2DH dispersion solve: the
+ * same scaling, sort, LDUSUB and AXSUB as PCGPME on copies of AL, LL and D
+ * (57-120), x0 = 0 (59-66), no EPS substitution, BETA = C1 / (AMU RQ) (255),
+ * and the solution post-processed into B (265-279). */
+
+/* Post-processing of pcgpme_2DH.f90:268-279, serial in row order: |x| <= 1e-14
+ * becomes 0; a neighbour (original LL, 0 ends the list, a self-reference is
+ * skipped) whose value differs by at most 1e-14 replaces x(i); B(i) = x(i) is
+ * written inside the neighbour loop only, so a row whose loop never reaches
+ * that statement keeps B(i), the last residual. */
+void ora_will_postprocess(double* X, double* B, const int* ll, int nl, long na, int n) {
+    const double L_Limit = 1.0e-14;
+    for (int i = 1; i <= n; i++) {
+        if (fabs(X[i - 1]) <= L_Limit) X[i - 1] = ZERO;
+        for (int k = 1; k <= nl; k++) {
+            const int j = ll[(long)(k - 1) * na + (i - 1)];
+            if (j == i) continue;
+            if (j == 0) break;
+            if (X[i - 1] == X[j - 1]) continue;
+            if (fabs(X[i - 1] - X[j - 1]) <= L_Limit) X[i - 1] = X[j - 1];
+            B[i - 1] = X[i - 1];
+        }
+    }
+}
+
+void ora_pcgpme_will(const double* al_in, int NL, int na, const int* ll_in, const double* d_in, int N, int N2,
+                     double* B, double EPS, double PARM, int ITER, int nthreads, int* iters_out, int* reason_out) {
+    long NA = na;
+    int nt = nthreads > 1 ? nthreads : 1;
+    double BN, C1, ALP, AMU, RN, RQ, BETA, ERR = ZERO, SS, ERRP = ZERO, P1, P2;
+    int K, reason = 4;
+    P1 = PARM;                                                       /* 51-53 */
+    if (PARM < ONE) P1 = TWO * TWO;
+    P2 = P1 + ONE;
+    long L = (long)N + N2;
+    double* al = (double*)malloc(sizeof(double) * (size_t)NA * NL);  /* ALTEMP, LLTEMP, DTEMP */
+    int* ll = (int*)malloc(sizeof(int) * (size_t)NA * NL);
+    double* D = (double*)malloc(sizeof(double) * (size_t)(N > 0 ? N : 1));
+    memcpy(al, al_in, sizeof(double) * (size_t)NA * NL);
+    memcpy(ll, ll_in, sizeof(int) * (size_t)NA * NL);
+    memcpy(D, d_in, sizeof(double) * (size_t)N);
+    double* X = (double*)calloc((size_t)L, sizeof(double));
+    double* WK = (double*)calloc((size_t)L * 5, sizeof(double));
+    double* W = (double*)calloc((size_t)L, sizeof(double));
+    double* WL = (double*)calloc((size_t)L, sizeof(double));
+    double* WK1 = WK;
+    double* WK2 = WK + L;
+    double* WK3 = WK + 2 * L;
+    double* WK4 = WK + 3 * L;
+    double* WK5 = WK + 4 * L;
+
+    setup_(al, NL, NA, ll, D, N, B, P1, P2, W, nt);                  /* 81-120 */
+    for (int I = 0; I < N; I++) WK1[I] = B[I];                       /* 122-126 */
+    ldusub_(al, NL, NA, ll, N, N2, WK1, WL, nt);                     /* 130 */
+    axsub_(al, NL, NA, ll, D, N, X, WK3, nt);                        /* 133 */
+    ldusub_(al, NL, NA, ll, N, N2, WK3, WL, nt);                     /* 134 */
+    BN = ZERO;
+    C1 = ZERO;
+#pragma omp parallel for schedule(static) reduction(+ : BN, C1) if (nt > 1) num_threads(nt)
+    for (int I = 0; I < N; I++) {                                    /* 139-150 */
+        double TEMP = WK1[I];
+        BN = BN + TEMP * TEMP;
+        TEMP = TEMP - WK3[I];
+        B[I] = TEMP;
+        C1 = C1 + TEMP * TEMP;
+        WK1[I] = TEMP;
+        WK2[I] = TEMP;
+    }
+    for (K = 1; K <= ITER; K++) {                                    /* 155 */
+        axsub_(al, NL, NA, ll, D, N, WK1, WK3, nt);
+        ldusub_(al, NL, NA, ll, N, N2, WK3, WL, nt);
+        RQ = ZERO;
+#pragma omp parallel for schedule(static) reduction(+ : RQ) if (nt > 1) num_threads(nt)
+        for (int I = 0; I < N; I++) RQ = RQ + WK2[I] * WK3[I];
+        ALP = C1 / RQ;
+#pragma omp parallel for schedule(static) if (nt > 1) num_threads(nt)
+        for (int I = 0; I < N; I++) WK4[I] = B[I] - ALP * WK3[I];
+        axsub_(al, NL, NA, ll, D, N, WK4, WK5, nt);
+        ldusub_(al, NL, NA, ll, N, N2, WK5, WL, nt);
+        AMU = ZERO;
+        SS = ZERO;
+#pragma omp parallel for schedule(static) reduction(+ : AMU, SS) if (nt > 1) num_threads(nt)
+        for (int I = 0; I < N; I++) {
+            double TEMP = WK5[I];
+            AMU = AMU + WK4[I] * TEMP;
+            SS = SS + TEMP * TEMP;
+        }
+        AMU = AMU / SS;
+        C1 = ZERO;
+        RN = ZERO;
+#pragma omp parallel for schedule(static) reduction(+ : RN, C1) if (nt > 1) num_threads(nt)
+        for (int I = 0; I < N; I++) {
+            double TEMP = WK4[I];
+            X[I] = X[I] + ALP * WK1[I] + AMU * TEMP;
+            TEMP = TEMP - AMU * WK5[I];
+            B[I] = TEMP;
+            RN = RN + TEMP * TEMP;
+            C1 = C1 + TEMP * WK2[I];
+        }
+        ERR = sqrt(RN / BN);                                         /* 222 */
+        if (K >= 10 && fabs(ERR - ERRP) <= ERR * 1.0e-6) { reason = 1; goto done; }  /* 246 */
+        if (ERR <= EPS) { reason = 0; goto done; }                   /* 250 */
+        ERRP = ERR;
+        if (AMU == ZERO) { reason = 2; goto done; }                  /* 252 */
+        if (C1 == ZERO) { reason = 3; goto done; }                   /* 254 */
+        BETA = C1 / (AMU * RQ);                                      /* 255 */
+#pragma omp parallel for schedule(static) if (nt > 1) num_threads(nt)
+        for (int I = 0; I < N; I++) WK1[I] = B[I] + BETA * (WK1[I] - AMU * WK3[I]);
+    }
+    reason = 4;                                                      /* 263: IER = 3000, not returned */
+done:
+    if (iters_out) *iters_out = K;
+    if (reason_out) *reason_out = reason;
+    ora_will_postprocess(X, B, ll_in, NL, NA, N);                    /* 265-279 */
+    free(al);
+    free(ll);
+    free(D);
+    free(X);
+    free(WK);
+    free(W);
+    free(WL);
+}
+
 void ora_pcgpme_setup(double* al, int nl, int na, int* ll, double* d, int n, double* b,
                       double parm) {
     double P1 = parm < ONE ? TWO * TWO : parm, P2 = P1 + ONE;

@@ -72,6 +72,15 @@ void ora_pcgpme(double* al, const int* nl, const int* na, int* ll, double* d,
                 const int* n, const int* n2, double* b, double* x, double* eps,
                 const double* parm, int* iter, int* ier, int nthreads, int* stop_reason);
 
+/* PCGPME_WILL (src2LOWNS/pcgpme_2DH.f90:1-374): AL, LL, D are left unchanged,
+ * B (length n) is the right-hand side on entry and the post-processed solution
+ * on return.  iters_out / reason_out (may be NULL) as for ora_pcgpme. */
+void ora_pcgpme_will(const double* al, int nl, int na, const int* ll, const double* d, int n, int n2,
+                     double* b, double eps, double parm, int iter, int nthreads, int* iters_out,
+                     int* reason_out);
+/* The post-processing alone (pcgpme_2DH.f90:268-279), in place on x and b. */
+void ora_will_postprocess(double* x, double* b, const int* ll, int nl, long na, int n);
+
 /* One operator application Q = PM * A * P using a matrix already scaled and
  * sorted by ora_pcgpme_setup (test helper). */
 void ora_pcgpme_setup(double* al, int nl, int na, int* ll, double* d, int n,

@@ -64,6 +64,10 @@ def lib():
             L.ora_transpose.argtypes = [i, i, P, P, P, P, P, P]
             L.ora_spmv.restype = None
             L.ora_spmv.argtypes = [i, i, P, P, P, P, P]
+            L.ora_pcgpme_will.restype = None
+            L.ora_pcgpme_will.argtypes = [P, i, i, P, P, i, i, P, d, d, i, i, P, P]
+            L.ora_will_postprocess.restype = None
+            L.ora_will_postprocess.argtypes = [P, P, P, i, C.c_long, i]
             _lib = L
     return _lib
 
@@ -214,6 +218,35 @@ def pcgpme(alu: np.ndarray, llu: np.ndarray, de: np.ndarray, b: np.ndarray, n: i
                  C.byref(ier), int(nthreads), C.byref(reason))
     return SolveResult(x=x[:n].copy(), eps=float(e[0]), iters=it.value, ier=ier.value,
                        reason=reason.value, al=al, ll=ll, d=d, b=bb)
+
+
+def pcgpme_will(al: np.ndarray, ll: np.ndarray, d: np.ndarray, b: np.ndarray, n: int, eps: float = 1e-10,
+                parm: float = 5.0, itmax: int = 10000, nthreads: int = 1, n2: int = 64):
+    """The restated PCGPME_WILL (pcgpme_2DH.f90:1-374).  al/ll: (nl, na) blocks
+    (column k of AL(NA,NL) is row k here), 1-based ll, 0 = none; returns
+    (b_out, iterations, stop reason) -- b_out is what the reference leaves in B."""
+    L = lib()
+    nl, na = al.shape
+    a = np.ascontiguousarray(al, dtype=np.float64)
+    l_ = np.ascontiguousarray(ll, dtype=np.int32)
+    dd = np.ascontiguousarray(d[:n], dtype=np.float64)
+    bb = np.ascontiguousarray(b[:n], dtype=np.float64).copy()
+    it = C.c_int(0)
+    reason = C.c_int(-1)
+    L.ora_pcgpme_will(_p(a), nl, na, _p(l_), _p(dd), n, n2, _p(bb), float(eps), float(parm), int(itmax),
+                      int(nthreads), C.byref(it), C.byref(reason))
+    return bb, it.value, reason.value
+
+
+def will_postprocess(x: np.ndarray, b: np.ndarray, ll: np.ndarray, n: int):
+    """pcgpme_2DH.f90:268-279 alone on copies: returns (x_out, b_out)."""
+    L = lib()
+    nl, na = ll.shape
+    xx = np.ascontiguousarray(x[:n], dtype=np.float64).copy()
+    bb = np.ascontiguousarray(b[:n], dtype=np.float64).copy()
+    l_ = np.ascontiguousarray(ll, dtype=np.int32)
+    L.ora_will_postprocess(_p(xx), _p(bb), _p(l_), nl, na, n)
+    return xx, bb
 
 
 def setup_scaled(alu, llu, de, b, n, parm=5.0):
