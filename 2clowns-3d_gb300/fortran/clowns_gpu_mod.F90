@@ -39,6 +39,16 @@ module clowns_gpu
             integer(c_int), intent(out) :: ier
         end subroutine pcgpme_gpu
 
+        ! PCGPME_WILL drop-in (2DH dispersion solve) with host arrays; B in: RHS,
+        ! out: what the reference leaves in B.  Returns 0 or a CLOWNS_ERR_* code.
+        integer(c_int) function pcgpme_will_gpu(al, nl, na, ll, d, n, n2, b, eps, parm, iter) &
+                bind(C, name="pcgpme_will_gpu")
+            import :: c_double, c_int
+            real(c_double), intent(in) :: al(*), d(*), eps, parm
+            integer(c_int), intent(in) :: nl, na, n, n2, iter, ll(*)
+            real(c_double), intent(inout) :: b(*)
+        end function pcgpme_will_gpu
+
         ! Device-resident solve: device addresses and a device workspace
         integer(c_size_t) function clowns_pcgpme_workspace_bytes(n, nl) &
                 bind(C, name="clowns_pcgpme_workspace_bytes")
@@ -95,5 +105,16 @@ contains
         integer, intent(out) :: ier
         call pcgpme_gpu(alu, nl, mm2, llu, de, mnoe, n2, b, xe, eps1, parm, iter, ier)
     end subroutine pcgpme_via_gpu
+
+    ! Same call shape as the reference's PCGPME_WILL, for an explicit swap at
+    ! 1sub-2DH-momentum.f90:325.
+    subroutine pcgpme_will_via_gpu(al, nl, na, ll, d, n, n2, b, eps, parm, iter)
+        integer, intent(in) :: nl, na, n, n2, iter
+        real*8, intent(in) :: al(na, nl), d(n), eps, parm
+        integer, intent(in) :: ll(na, nl)
+        real*8, intent(inout) :: b(n)
+        integer(c_int) :: rc
+        rc = pcgpme_will_gpu(al, nl, na, ll, d, n, n2, b, eps, parm, iter)
+    end subroutine pcgpme_will_via_gpu
 
 end module clowns_gpu
