@@ -374,23 +374,24 @@ def dispersion_system(nx: int, ny: int, seed: int = 7, dx: float = 0.5, A: float
     wet &= (X - cx) ** 2 + (Y - cy) ** 2 > r * r           # island
     num = -np.ones((nx, ny), dtype=np.int64)
     idx = np.argwhere(wet.T)                                # row order: i fastest within j
-    for row, (j, i) in enumerate(idx):
-        num[i, j] = row
     n = len(idx)
-    al = np.zeros((4, n))
-    ll = np.zeros((4, n), dtype=np.int32)
-    d = -np.ones(n)
-    for row, (j, i) in enumerate(idx):
-        hc = h[i, j]
-        jj = 0
-        for (lo, hi) in (((i - 1, j), (i + 1, j)), ((i, j - 1), (i, j + 1))):
-            if not (0 <= lo[0] and 0 <= lo[1] and hi[0] < nx and hi[1] < ny):
-                continue                                    # domain edge in this direction
-            for (ii, kk) in (lo, hi):
-                if num[ii, kk] >= 0:
-                    al[jj, row] = A * 2.0 * hc * hc / dx / (dx + dx)
-                    ll[jj, row] = num[ii, kk] + 1
-                    jj += 1
-        d[row] -= al[:, row].sum()
+    jr, ir = idx[:, 0], idx[:, 1]
+    num[ir, jr] = np.arange(n)
+    # candidates in the reference's order: x-, x+ (if the cell is inside in x), y-, y+
+    cand = -np.ones((n, 4), dtype=np.int64)
+    inx = (ir > 0) & (ir + 1 < nx)
+    iny = (jr > 0) & (jr + 1 < ny)
+    cand[inx, 0] = num[ir[inx] - 1, jr[inx]]
+    cand[inx, 1] = num[ir[inx] + 1, jr[inx]]
+    cand[iny, 2] = num[ir[iny], jr[iny] - 1]
+    cand[iny, 3] = num[ir[iny], jr[iny] + 1]
+    order = np.argsort(cand < 0, axis=1, kind="stable")     # pack existing neighbours first
+    packed = np.take_along_axis(cand, order, axis=1)
+    present = packed >= 0
+    hc = h[ir, jr]
+    coef = A * 2.0 * hc * hc / dx / (dx + dx)
+    al = np.where(present, coef[:, None], 0.0).T.copy()
+    ll = np.where(present, packed + 1, 0).astype(np.int32).T.copy()
+    d = -1.0 - (((al[0] + al[1]) + al[2]) + al[3])        # DIAG = -1 - sum(AL), summed in slot order
     b = rng.normal(0.0, 1.0, n) * np.exp(-((idx[:, 1] / nx - 0.5) ** 2) * 20.0)
     return DispersionSystem(al=al, ll=ll, d=d, b=b, n=n, nx=nx, ny=ny)

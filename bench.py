@@ -307,6 +307,59 @@ def run_ensemble(args):
     print(json.dumps(line), flush=True)
 
 
+def run_will(args):
+    """PCGPME_WILL (the 2DH dispersion solve) on a seeded 2DH system of
+    --will-grid cells (built like disp_param): device-resident solves/s, end to
+    end through the host drop-in, and the oracle's OpenMP restatement on the
+    host cores (rank 0).  Prints one JSON line."""
+    import torch
+    pkg = ge.load_package()
+    pkg.build()
+    nx, ny = (int(v) for v in args.will_grid.split("x"))
+    ds = pkg.workload.dispersion_system(nx, ny, seed=11)
+    n = ds.n
+    eps = 1e-10
+    al, ll, d = (torch.from_numpy(np.ascontiguousarray(a)).cuda() for a in (ds.al, ds.ll, ds.d))
+    b0 = torch.from_numpy(ds.b).cuda()
+    b = torch.empty_like(b0)
+    solver = pkg.WillSolver(n)
+    stream = torch.cuda.current_stream()
+
+    def step():
+        b.copy_(b0)
+        return solver.solve(al, ll, d, b, eps=eps)
+
+    for _ in range(max(3, args.warmup)):
+        step()
+    ms, infos = time_device(step, args.steps, stream)
+    info = infos[-1]
+    alh, llh = np.ascontiguousarray(ds.al), np.ascontiguousarray(ds.ll)
+    bh = ds.b.copy()
+    pkg.pcgpme_will(alh, llh, ds.d, bh, n, eps=eps)
+    t0 = time.perf_counter()
+    for _ in range(args.steps):
+        bh[:] = ds.b
+        pkg.pcgpme_will(alh, llh, ds.d, bh, n, eps=eps)
+    e2e_s = (time.perf_counter() - t0) / args.steps
+    ora = ge.load_oracle()
+    ora.build()
+    threads = os.cpu_count() or 1
+    t0 = time.perf_counter()
+    bo, it_o, reason = ora.pcgpme_will(ds.al, ds.ll, ds.d, ds.b, n, eps=eps, nthreads=threads)
+    t_cpu = time.perf_counter() - t0
+    bg = b.cpu().numpy()
+    line = {"metric": "2DH dispersion solves/s (PCGPME_WILL)", "unit": "solves/s", "grid": args.will_grid,
+            "rows": n, "tol": eps, "iters": info.iter, "iters_oracle": it_o,
+            "value": args.steps / (ms / 1000.0), "ms_per_solve": ms / args.steps,
+            "e2e": {"value": 1.0 / e2e_s, "unit": "solves/s",
+                    "h2d_bytes_per_step": n * (4 * 8 + 4 * 4 + 2 * 8), "d2h_bytes_per_step": n * 8},
+            "rel_l2_vs_oracle": float(np.linalg.norm(bg - bo) / np.linalg.norm(bo)),
+            "cpu_baseline": {"value": 1.0 / t_cpu, "unit": "solves/s", "cores": threads, "kind": "port",
+                             "cpu_model": cpu_model(),
+                             "sample": f"one solve, OpenMP restatement of pcgpme_2DH.f90 on {threads} threads"}}
+    print(json.dumps(line), flush=True)
+
+
 def run_adjoint(args):
     """Adjoint on the 192x192x64 beach: J = sum of 16 seeded gauge pressures with
     weights U(0.5,1.5); dJ/da for 200 seeded face fractions against central
@@ -551,6 +604,8 @@ def main():
     ap.add_argument("--members", type=int, default=64)
     ap.add_argument("--member-scale", type=float, default=1.0)
     ap.add_argument("--adjoint", action="store_true", help="adjoint vs finite differences instead")
+    ap.add_argument("--will", action="store_true", help="PCGPME_WILL (2DH dispersion solve) instead")
+    ap.add_argument("--will-grid", default="1600x1200", help="2DH plan grid of the --will leg")
     ap.add_argument("--faces", type=int, default=200)
     ap.add_argument("--workload", default=WORKLOAD,
                     help="beach_256x256x96 (default), beach_512x384x128, beach_192x192x64, "
@@ -566,6 +621,11 @@ def main():
         import torch
         torch.cuda.set_device(local)
         run_adjoint(args)
+        return
+    if args.will:
+        import torch
+        torch.cuda.set_device(local)
+        run_will(args)
         return
     if args.impl == "reference":
         run_reference(args, world, rank)
