@@ -375,7 +375,8 @@ def tuned_shape(sizes, precision=0):
                             C.byref(f)) != 0:
         return None
     if mo.value == 1:
-        return {"mode": "graph", "block": b.value, "fused_sweeps": bool(f.value)}
+        return {"mode": "graph", "block": b.value, "fused_sweeps": bool(f.value & 1),
+                "reduce_block": 64 if f.value & 2 else b.value}
     return {"mode": {0: "persistent", 3: "wave"}.get(mo.value, str(mo.value)), "block": b.value,
             "grid": g.value, "registers": r.value}
 

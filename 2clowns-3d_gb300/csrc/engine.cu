@@ -415,6 +415,7 @@ struct Shape {
     int block = kStepBlock;
     int grid = 0;   // 0: one block per tile
     int fuse = 1;   // LDUSUB sweeps 1-2 and 3-4 as fused pairs (else four single sweeps)
+    int rblock = kStepBlock;   // threads per tile of the dot-product kernels (64: 8 rows per thread)
 };
 
 
@@ -482,6 +483,7 @@ struct LoopShape {
     int wk = 1;       // wavefront: tiles per item
     int wslack = 3;   // wavefront: slack rounds
     int fuse = 1;     // graph / host launches: fused sweep pairs
+    int rblock = kStepBlock;   // graph / host launches: block of the dot-product kernels
 };
 
 // CLOWNS_LOOP_MODE=graph|persistent|launch|wave forces one execution of the loop
@@ -557,8 +559,8 @@ static void g_apply(bool pdl, const Eng<T>& E, const Shape& sh, const T* in, T* 
         klaunch(pdl, k_eng_sweep<T>, g, b, s, E, 3, (const T*)out, tmp);
     }
     if (mode == 0) klaunch(pdl, k_eng_sweep56<T, 0>, g, b, s, E, (const T*)tmp, out);
-    if (mode == 1) klaunch(pdl, k_eng_sweep56<T, 1>, g, b, s, E, (const T*)tmp, out);
-    if (mode == 2) klaunch(pdl, k_eng_sweep56<T, 2>, g, b, s, E, (const T*)tmp, out);
+    if (mode == 1) klaunch(pdl, k_eng_sweep56<T, 1>, g, sh.rblock, s, E, (const T*)tmp, out);
+    if (mode == 2) klaunch(pdl, k_eng_sweep56<T, 2>, g, sh.rblock, s, E, (const T*)tmp, out);
 }
 
 template <typename T>
@@ -567,7 +569,7 @@ static void g_iteration(bool pdl, const Eng<T>& E, const Shape& sh, cudaStream_t
     g_apply(pdl, E, sh, (const T*)E.p, E.q, E.t, 1, s);
     klaunch(pdl, k_eng_eupdate<T>, g, b, s, E);
     g_apply(pdl, E, sh, (const T*)E.e, E.v, E.t, 2, s);
-    klaunch(pdl, k_eng_xrupdate<T>, g, b, s, E);
+    klaunch(pdl, k_eng_xrupdate<T>, g, sh.rblock, s, E);
     klaunch(pdl, k_eng_pupdate<T>, g, b, s, E);
 }
 
@@ -575,9 +577,9 @@ static void g_iteration(bool pdl, const Eng<T>& E, const Shape& sh, cudaStream_t
 struct GraphKey {
     const void* work;
     long NV;
-    int M, prec, fuse;
+    int M, prec, fuse, rblock;
     bool operator<(const GraphKey& o) const {
-        return std::tie(work, NV, M, prec, fuse) < std::tie(o.work, o.NV, o.M, o.prec, o.fuse);
+        return std::tie(work, NV, M, prec, fuse, rblock) < std::tie(o.work, o.NV, o.M, o.prec, o.fuse, o.rblock);
     }
 };
 static std::mutex g_graph_mu;
@@ -604,7 +606,7 @@ void release_graphs_for(const void* work) {
 
 // WHILE { iteration ; guard } captured into a fresh graph
 template <typename T>
-static int build_loop_graph(const Eng<T>& E, bool pdl, int fuse, cudaGraphExec_t* out) {
+static int build_loop_graph(const Eng<T>& E, bool pdl, int fuse, int rblock, cudaGraphExec_t* out) {
     if (!g_cap) CLOWNS_CUDA_TRY(cudaStreamCreateWithFlags(&g_cap, cudaStreamNonBlocking));
     cudaGraph_t graph;
     CLOWNS_CUDA_TRY(cudaGraphCreate(&graph, 0));
@@ -620,6 +622,7 @@ static int build_loop_graph(const Eng<T>& E, bool pdl, int fuse, cudaGraphExec_t
     CLOWNS_CUDA_TRY(cudaStreamBeginCaptureToGraph(g_cap, body, nullptr, nullptr, 0, cudaStreamCaptureModeThreadLocal));
     Shape sh;
     sh.fuse = fuse;
+    sh.rblock = rblock;
     g_iteration(pdl, E, sh, g_cap);
     klaunch(pdl, k_eng_guard, 1, 256, g_cap, E.S, E.M, E.ctrl, h);
     cudaGraph_t captured;
@@ -643,14 +646,14 @@ static int build_loop_graph(const Eng<T>& E, bool pdl, int fuse, cudaGraphExec_t
 }
 
 template <typename T>
-static int loop_graph(const Eng<T>& E, const void* work, int prec, int fuse, cudaGraphExec_t* out) {
+static int loop_graph(const Eng<T>& E, const void* work, int prec, int fuse, int rblock, cudaGraphExec_t* out) {
     std::lock_guard<std::mutex> lk(g_graph_mu);
-    GraphKey key{work, E.NV, E.M, prec, fuse};
+    GraphKey key{work, E.NV, E.M, prec, fuse, rblock};
     auto it = g_graphs.find(key);
     if (it != g_graphs.end()) { *out = it->second; return CLOWNS_OK; }
     cudaGraphExec_t ex;
-    int rc = build_loop_graph(E, true, fuse, &ex);              // programmatic edges
-    if (rc) rc = build_loop_graph(E, false, fuse, &ex);         // plain edges if refused
+    int rc = build_loop_graph(E, true, fuse, rblock, &ex);              // programmatic edges
+    if (rc) rc = build_loop_graph(E, false, fuse, rblock, &ex);         // plain edges if refused
     if (rc) return rc;
     if (g_graphs.size() >= 64) {
         cudaGraphExecDestroy(g_graphs.begin()->second);
@@ -681,6 +684,7 @@ static int run_loop(Eng<T> E, const void* work, GridBar* gb, int prec, const Loo
         CLOWNS_CUDA_TRY(cudaMemsetAsync(gb, 0, sizeof(GridBar), s));
         Shape ksh;
         ksh.fuse = sh.fuse;
+        ksh.rblock = sh.rblock;
         int cap = 0;
         CLOWNS_CUDA_TRY(cudaMemcpyAsync(&cap, E.ctrl + 1, sizeof(int), cudaMemcpyDeviceToHost, s));
         CLOWNS_CUDA_TRY(cudaStreamSynchronize(s));
@@ -717,7 +721,7 @@ static int run_loop(Eng<T> E, const void* work, GridBar* gb, int prec, const Loo
     }
     if (sh.graph) {
         cudaGraphExec_t ex;
-        int rc = loop_graph(E, work, prec, sh.fuse, &ex);
+        int rc = loop_graph(E, work, prec, sh.fuse, sh.rblock, &ex);
         if (rc) return rc;
         CLOWNS_CUDA_TRY(cudaMemsetAsync(gb, 0, sizeof(GridBar), s));
         CLOWNS_CUDA_TRY(cudaGraphLaunch(ex, s));
@@ -760,6 +764,8 @@ static int tune_loop(Eng<T> E, const void* work, GridBar* gb, long key_nv, int k
         sh.graph = forced;
         const char* fz = getenv("CLOWNS_SWEEP_FUSE");     // forced executions: fused pairs unless "0"
         sh.fuse = !(fz && !strcmp(fz, "0"));
+        const char* rz = getenv("CLOWNS_REDUCE_BLOCK");   // forced executions: 128 unless "64"
+        sh.rblock = (rz && !strcmp(rz, "64")) ? 64 : kStepBlock;
         *out = sh;
         return CLOWNS_OK;
     }
@@ -827,12 +833,18 @@ static int tune_loop(Eng<T> E, const void* work, GridBar* gb, long key_nv, int k
         }
     }
     if (forced < 0 || (forced == 3 && !wave_ok)) {     // forced wave: ensembles keep the graph
-        for (int fuse : {1, 0}) {
-            LoopShape gsh;
-            gsh.graph = 1;
-            gsh.fuse = fuse;
-            cands.push_back(gsh);
-        }
+        // FP64 dot-product kernels may run 64 threads per tile (8 rows per
+        // thread before the warp sums: half the FP64 additions per row); the
+        // FP32 ones have FP32 warp sums and keep 128
+        for (int fuse : {1, 0})
+            for (int rb : {kStepBlock, 64}) {
+                if (rb != kStepBlock && sizeof(T) != 8) continue;
+                LoopShape gsh;
+                gsh.graph = 1;
+                gsh.fuse = fuse;
+                gsh.rblock = rb;
+                cands.push_back(gsh);
+            }
     }
     if (cands.empty()) {
         set_last_error_msg("pcgpme: the forced loop execution does not serve this system");
@@ -874,7 +886,8 @@ static int tune_loop(Eng<T> E, const void* work, GridBar* gb, long key_nv, int k
     return CLOWNS_OK;
 }
 
-// mode: 0 persistent, 1 CUDA graph, 3 wavefront; fuse: fused sweep pairs (graph)
+// mode: 0 persistent, 1 CUDA graph, 3 wavefront; fuse (graph): bit 0 fused sweep
+// pairs, bit 1 dot-product kernels at 64 threads per tile
 int engine_tuned_shape(long nv, int prec, int single, int* mode, int* block, int* grid, int* minb, int* fuse) {
     std::lock_guard<std::mutex> lk(g_loop_mu);
     auto it = g_loop_shapes.find(std::make_tuple(nv, prec, single));
@@ -884,7 +897,7 @@ int engine_tuned_shape(long nv, int prec, int single, int* mode, int* block, int
     *block = sh.block;
     *grid = sh.graph == 1 ? 0 : sh.grid;
     *minb = sh.graph == 1 ? 0 : sh.minb;
-    *fuse = sh.graph == 1 ? sh.fuse : 0;
+    *fuse = sh.graph == 1 ? (sh.fuse | (sh.rblock != kStepBlock ? 2 : 0)) : 0;
     return CLOWNS_OK;
 }
 

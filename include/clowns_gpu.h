@@ -171,8 +171,9 @@ int clowns_pcgpme_batched_dev(int m, const clowns_member* members, int precision
  * dependent launch) or CLOWNS_LOOP_WAVE (one cooperative kernel running
  * (stage, tile) items in wavefront order; single systems only).  block:
  * threads per block; grid: blocks of the cooperative kernels (0 for the graph);
- * regs: their register budget per thread (0 for the graph); fused: 1 when the
- * graph runs LDUSUB's sweeps 1-2 and 3-4 as fused pairs.  CLOWNS_ERR_ARG until
+ * regs: their register budget per thread (0 for the graph); fused (graph): bit 0
+ * set when LDUSUB's sweeps 1-2 and 3-4 run as fused pairs, bit 1 set when the
+ * dot-product kernels run 64 threads per 512-row tile (8 rows per thread).  CLOWNS_ERR_ARG until
  * a solve of that size has run. */
 #define CLOWNS_LOOP_PERSISTENT 0
 #define CLOWNS_LOOP_GRAPH 1
