@@ -127,9 +127,12 @@ __device__ __forceinline__ int sld(const int* p) { return __ldcg(p); }
 // Tile walk helpers
 
 // Member, first row and real rows of tile blk; false for tiles without real
-// rows.  `done` (the member's stop flag) is loaded but not waited for: callers
-// issue their data loads first and test it before any store or reduction, so
-// its latency overlaps theirs.  A single system needs no table loads at all.
+// rows.  Single system: `done` (the stop flag) is loaded but not waited for --
+// callers issue their data loads first and test it before any store or
+// reduction, so its latency overlaps theirs (it is set only once, at the end),
+// and no table loads are needed.  Ensembles: tiles of a stopped member return
+// at once (false), before any data load -- members stop at different
+// iterations, and their tiles must not keep streaming the matrix.
 template <typename T>
 __device__ __forceinline__ bool tile_active(const Eng<T>& E, int blk, int& m, long& row0, int& rows, int& done) {
     row0 = (long)blk * kTile;
@@ -143,7 +146,7 @@ __device__ __forceinline__ bool tile_active(const Eng<T>& E, int blk, int& m, lo
     }
     if (rows == 0) return false;
     done = sld(&E.S[m].done);
-    return true;
+    return E.M == 1 || !done;
 }
 
 // Reduce (v0, v1) over the block and record the block's partial.  Two levels of
