@@ -360,6 +360,78 @@ def run_will(args):
     print(json.dumps(line), flush=True)
 
 
+def run_session(args):
+    """The whole pressure-correction ik loop of one time step on the device
+    (clowns_session_pressure_loop: row numbering, RHS and dmax, assembly, PCGPME,
+    pressure and velocity correction, repeated until dmax < d0;
+    1sub-momentum.F90:41-60) for --workload, against the oracle running the same
+    loop on the host cores (rank 0).  Each timed step resets the fields first
+    (host upload outside the device timing, inside the end-to-end one).  Prints
+    one JSON line."""
+    import torch
+    pkg = ge.load_package()
+    pkg.build()
+    case = workload_case(pkg, args.workload)
+    d0, eps0 = 1e-5, case.eps0
+    p0 = np.zeros(case.inne2 + 2)
+    s = pkg.Session(case)
+
+    def reset():
+        s.set_fields(case.nf, case.nfb, case.f, case.fb, case.a, case.un, case.sp, p0)
+        return s.classify()
+
+    reset()
+    out = s.pressure_loop(case.dt, d0=d0, eps0=eps0)             # warm-up (autotuning, graphs)
+    dev_ms, e2e_s, outs = [], [], []
+    ev0 = torch.cuda.Event(enable_timing=True)
+    ev1 = torch.cuda.Event(enable_timing=True)
+    for _ in range(args.steps):
+        t0 = time.perf_counter()
+        reset()
+        torch.cuda.synchronize()
+        ev0.record()
+        out = s.pressure_loop(case.dt, d0=d0, eps0=eps0)
+        ev1.record()
+        torch.cuda.synchronize()
+        got = s.fields()
+        e2e_s.append(time.perf_counter() - t0)
+        dev_ms.append(ev0.elapsed_time(ev1))
+        outs.append(out)
+    s.close()
+    ora = ge.load_oracle()
+    ora.build()
+    threads = os.cpu_count() or 1
+    t0 = time.perf_counter()
+    cls = ora.set_nflag(case)
+    sm = ora.init_matrix(case, cls)
+    c = case.copy()
+    c.f = cls.f.copy()
+    pc = np.zeros(case.inne2 + 2)
+    un = case.un.copy()
+    ik = 0
+    while True:
+        c.un = un
+        sy = ora.rows_rhs_assemble(c, cls, sm)
+        if sy.dmax < d0 or ik >= 1000:
+            break
+        ik += 1
+        r = ora.pcgpme(sy.alu, sy.llu, sy.de[1:], sy.b[1:], sy.mnoe, eps=eps0, nthreads=threads)
+        pc, un = ora.correct(c, cls, sy, r.x, pc, un)
+    t_cpu = time.perf_counter() - t0
+    ms = statistics.median(dev_ms)
+    line = {"metric": "pressure-correction steps/s (whole ik loop on the device)", "unit": "steps/s",
+            "workload": args.workload, "rows": int(got["mnoe"]), "ik_passes": outs[-1]["ik"], "ik_passes_oracle": ik,
+            "solve_iters_last_pass": outs[-1]["iter"], "dmax": outs[-1]["dmax"], "icon": outs[-1]["icon"],
+            "value": 1000.0 / ms, "ms_per_step": ms,
+            "e2e": {"value": 1.0 / statistics.median(e2e_s), "unit": "steps/s"},
+            "rel_l2_p_vs_oracle": float(np.linalg.norm(got["p"] - pc) / np.linalg.norm(pc)),
+            "cpu_baseline": {"value": 1.0 / t_cpu, "unit": "steps/s", "cores": threads, "kind": "port",
+                             "cpu_model": cpu_model(),
+                             "sample": f"one step: the oracle's set_nflag, init_matrix and {ik} passes of numbering, "
+                                       f"RHS, assembly, PCGPME ({threads} threads) and correction"}}
+    print(json.dumps(line), flush=True)
+
+
 def run_adjoint(args):
     """Adjoint on the 192x192x64 beach: J = sum of 16 seeded gauge pressures with
     weights U(0.5,1.5); dJ/da for 200 seeded face fractions against central
@@ -605,6 +677,7 @@ def main():
     ap.add_argument("--member-scale", type=float, default=1.0)
     ap.add_argument("--adjoint", action="store_true", help="adjoint vs finite differences instead")
     ap.add_argument("--will", action="store_true", help="PCGPME_WILL (2DH dispersion solve) instead")
+    ap.add_argument("--session", action="store_true", help="the whole ik loop on the device instead")
     ap.add_argument("--will-grid", default="1600x1200", help="2DH plan grid of the --will leg")
     ap.add_argument("--faces", type=int, default=200)
     ap.add_argument("--workload", default=WORKLOAD,
@@ -626,6 +699,11 @@ def main():
         import torch
         torch.cuda.set_device(local)
         run_will(args)
+        return
+    if args.session:
+        import torch
+        torch.cuda.set_device(local)
+        run_session(args)
         return
     if args.impl == "reference":
         run_reference(args, world, rank)
