@@ -23,6 +23,7 @@ from typing import Optional
 import numpy as np
 
 from . import workload  # noqa: F401  (re-exported)
+from . import ingest  # noqa: F401  (re-exported)
 
 PKG = pathlib.Path(__file__).resolve().parent
 LIB_PATH = PKG / "libclowns_gpu.so"

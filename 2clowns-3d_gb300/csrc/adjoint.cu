@@ -100,7 +100,7 @@ extern "C" int clowns_face_grad_dev(const int* dims, int inne, int inne2, int if
                                     const int* in_, const int* jn, const int* kn, const int* nf, const int* mno,
                                     const double* alu_c, const int* ll_c, const double* a, const double* x,
                                     const double* lambda, double* grad, void* stream) {
-    if (!dims || inne < 1 || ifln < 0 || !fln || !in_ || !jn || !kn || !nf || !mno || !alu_c || !ll_c || !a ||
+    if (!grid_dims_ok(dims) || inne < 1 || ifln < 0 || !fln || !in_ || !jn || !kn || !nf || !mno || !alu_c || !ll_c || !a ||
         !x || !lambda || !grad) {
         set_last_error_msg("face_grad: invalid arguments");
         return CLOWNS_ERR_ARG;

@@ -310,7 +310,7 @@ extern "C" int clowns_init_matrix_dev(const int* dims, int inne, int mx2, const 
                                       const int* jn, const int* kn, const int* nf, const int* nfb,
                                       const double* a, const double* fb, const double* dx, double* mp,
                                       double* alu_c, int* ll_c, double* de_c, void* stream) {
-    if (!dims || inne < 1 || mx2 < 1 || !mn || !in_ || !jn || !kn || !nf || !nfb || !a || !fb || !dx || !mp ||
+    if (!grid_dims_ok(dims) || inne < 1 || mx2 < 1 || !mn || !in_ || !jn || !kn || !nf || !nfb || !a || !fb || !dx || !mp ||
         !alu_c || !ll_c || !de_c) {
         set_last_error_msg("init_matrix: invalid arguments");
         return CLOWNS_ERR_ARG;
@@ -335,7 +335,7 @@ extern "C" int clowns_rows_rhs_dev(const int* dims, int inne2, int mx2, const in
                                    int* mno2mn, double* b, double* xe, double* de, int* mnoe_out,
                                    double* dmax_out, void* work, size_t work_bytes, void* stream) {
     (void)inne2; (void)mx2;
-    if (!dims || !mn || !in_ || !jn || !kn || !nf || !nfb || !f || !fb || !a || !un || !dx || !mp || !fln ||
+    if (!grid_dims_ok(dims) || !mn || !in_ || !jn || !kn || !nf || !nfb || !f || !fb || !a || !un || !dx || !mp || !fln ||
         !mno || !mno2mn || !b || !xe || !de || !mnoe_out || ifln < 0 || mm2 < 1 || !work) {
         set_last_error_msg("rows_rhs: invalid arguments");
         return CLOWNS_ERR_ARG;
@@ -404,7 +404,7 @@ extern "C" int clowns_assemble_dev(const int* dims, int inne, int inne2, int mx2
                                    const int* ll_c, const double* de_c, int mm2, double* alu, int* llu, double* de,
                                    int* err_cell, void* stream) {
     (void)mx2;
-    if (!dims || inne < 1 || !in_ || !jn || !kn || !nf || !nfb || !x || !dx || !sp || !fln || !mno || !alu_c ||
+    if (!grid_dims_ok(dims) || inne < 1 || !in_ || !jn || !kn || !nf || !nfb || !x || !dx || !sp || !fln || !mno || !alu_c ||
         !ll_c || !de_c || mm2 < 1 || !alu || !llu || !de || !err_cell) {
         set_last_error_msg("assemble: invalid arguments");
         return CLOWNS_ERR_ARG;
@@ -425,7 +425,7 @@ extern "C" int clowns_correct_dev(const int* dims, int inne, int mx2, const int*
                                   double dt, int mnoe, const int* mno2mn, const int* mno, const double* xe0,
                                   double* p, double* un, void* stream) {
     (void)mx2;
-    if (!dims || inne < 1 || !mn || !in_ || !jn || !kn || !nf || !nfb || !a || !dx || mnoe < 0 || !mno2mn ||
+    if (!grid_dims_ok(dims) || inne < 1 || !mn || !in_ || !jn || !kn || !nf || !nfb || !a || !dx || mnoe < 0 || !mno2mn ||
         !mno || !xe0 || !p || !un) {
         set_last_error_msg("correct: invalid arguments");
         return CLOWNS_ERR_ARG;

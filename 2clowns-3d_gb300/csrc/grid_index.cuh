@@ -36,6 +36,14 @@ struct GridIdx {
     __host__ __device__ __forceinline__ long dxo(int l, int i) const { return 3L * (i - 1) + l; }
 };
 
+// The reference stores x(l, ls-2 .. le+1) in x(0:2, 1:mx2) (data_io.F90:114,
+// 0mod-arrays.F90:205) and numbers cells from ls-1, whose minus neighbours at
+// ls-2 are addressed in mn and mno: so ls >= 3 on every axis, and each axis
+// holds at least one cell.
+inline bool grid_dims_ok(const int* d) {
+    return d && d[0] >= 3 && d[1] >= 3 && d[2] >= 3 && d[3] > d[0] && d[4] > d[1] && d[5] > d[2];
+}
+
 // Exclusive scan of n int32 flags/counts: out[t] = sum_{u<t} in[u], *total = sum.
 size_t scan_workspace_bytes(long n);
 int exclusive_scan_dev(const int* in, int* out, long n, int* total, void* tmp, cudaStream_t s);

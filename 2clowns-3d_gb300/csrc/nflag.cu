@@ -351,7 +351,7 @@ extern "C" int clowns_set_nflag_dev(const int* dims, int inne, int inne2, int mx
                                     int* sfn, int* isfn_out, int* passes_out, void* work, size_t work_bytes,
                                     void* stream) {
     (void)mx2;
-    if (!dims || inne < 1 || !mn || !in_ || !jn || !kn || !nf || !nfb || !f || !fb || !a || !dx || !objno ||
+    if (!grid_dims_ok(dims) || inne < 1 || !mn || !in_ || !jn || !kn || !nf || !nfb || !f || !fb || !a || !dx || !objno ||
         !fln || !ifln_out || !sfn || !isfn_out || !work) {
         set_last_error_msg("set_nflag: invalid arguments");
         return CLOWNS_ERR_ARG;

@@ -96,7 +96,7 @@ static int download(void* dst, const void* src, size_t bytes, cudaStream_t s) {
 extern "C" int clowns_session_create(clowns_session** out, const int* dims, int inne, int inne2, int mx2,
                                      const int* mn, const int* in_, const int* jn, const int* kn,
                                      const double* x, const double* dx, const int* objno) {
-    if (!out || !dims || inne < 1 || inne2 < inne || mx2 < 1 || !mn || !in_ || !jn || !kn || !x || !dx ||
+    if (!out || !grid_dims_ok(dims) || inne < 1 || inne2 < inne || mx2 < 1 || !mn || !in_ || !jn || !kn || !x || !dx ||
         !objno) {
         set_last_error_msg("session_create: invalid arguments");
         return CLOWNS_ERR_ARG;

@@ -169,10 +169,12 @@ def test_iteration_cap_and_codes(gpu, prepared):
     assert ier == gpu.IER_ARG
 
 
-def test_correction_parity(gpu, ora, prepared):
-    """p -= xe and estimate_velocity2 against the oracle (bit-exact: same ops)."""
+@pytest.mark.parametrize("label", ["bore_40x24x32", "flume_40x24x20_ingested"])
+def test_correction_parity(gpu, ora, prepared, label):
+    """p -= xe and estimate_velocity2 against the oracle (bit-exact: same ops);
+    the flume adds the wave-boundary cells' own update (nf=-1, nfb=4)."""
     import torch
-    case, cls, sm, sy, dc, ds = prepared["bore_40x24x32"]
+    case, cls, sm, sy, dc, ds = prepared[label]
     n = sy.mnoe
     rng = np.random.default_rng(9)
     xe = rng.standard_normal(n) * 1e-3
