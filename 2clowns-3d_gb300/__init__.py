@@ -366,7 +366,9 @@ PREC_MIXED = 1
 
 def tuned_shape(sizes, precision=0):
     """Execution the autotuner chose for the iteration loop of this row space:
-    {"mode": "graph", "block": .., "fused_sweeps": ..} or
+    {"mode": "graph", "block": .., "fused_sweeps": .., "reduce_block": ..,
+    "balanced_rows": 0 | 4 | 8} (balanced_rows > 0: one-wave kernels over even
+    row ranges, that many rows per thread per step) or
     {"mode": "persistent" | "wave", "block": .., "grid": .., "registers": ..},
     or None before a solve of that size has run."""
     L = lib()
@@ -376,8 +378,9 @@ def tuned_shape(sizes, precision=0):
                             C.byref(f)) != 0:
         return None
     if mo.value == 1:
-        return {"mode": "graph", "block": b.value, "fused_sweeps": bool(f.value & 1),
-                "reduce_block": 64 if f.value & 2 else b.value}
+        bal = (8 if f.value & 8 else 4) if f.value & 4 else 0
+        return {"mode": "graph", "block": 256 if bal else b.value, "fused_sweeps": bool(f.value & 1),
+                "reduce_block": 64 if f.value & 2 else (256 if bal else b.value), "balanced_rows": bal}
     return {"mode": {0: "persistent", 3: "wave"}.get(mo.value, str(mo.value)), "block": b.value,
             "grid": g.value, "registers": r.value}
 

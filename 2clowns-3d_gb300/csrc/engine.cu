@@ -6,6 +6,7 @@
 #include <algorithm>
 #include <cmath>
 #include <cstdlib>
+#include <climits>
 #include <cstring>
 #include <map>
 #include <mutex>
@@ -416,6 +417,7 @@ struct Shape {
     int grid = 0;   // 0: one block per tile
     int fuse = 1;   // LDUSUB sweeps 1-2 and 3-4 as fused pairs (else four single sweeps)
     int rblock = kStepBlock;   // threads per tile of the dot-product kernels (64: 8 rows per thread)
+    int bal = 0;    // single systems: balanced one-wave kernels with bal rows per thread per step (4 or 8)
 };
 
 
@@ -484,10 +486,12 @@ struct LoopShape {
     int wslack = 3;   // wavefront: slack rounds
     int fuse = 1;     // graph / host launches: fused sweep pairs
     int rblock = kStepBlock;   // graph / host launches: block of the dot-product kernels
+    int bal = 0;      // graph / host launches, single systems: balanced kernels, rows per thread (4, 8)
 };
 
 // CLOWNS_LOOP_MODE=graph|persistent|launch|wave forces one execution of the loop
-// (with graph and launch, CLOWNS_SWEEP_FUSE=0 selects the four single sweeps)
+// (with graph and launch, CLOWNS_SWEEP_FUSE=0 selects the four single sweeps and,
+// for single systems, CLOWNS_BALANCED_ROWS=4|8 the balanced one-wave kernels)
 // ("launch": the iteration's kernels launched from the host, eight iterations
 // between polls of the stop flags -- the same kernels, visible one by one to a
 // profiler); unset or "auto": the autotuner decides.
@@ -563,8 +567,74 @@ static void g_apply(bool pdl, const Eng<T>& E, const Shape& sh, const T* in, T* 
     if (mode == 2) klaunch(pdl, k_eng_sweep56<T, 2>, g, sh.rblock, s, E, (const T*)tmp, out);
 }
 
+// One wave of a balanced kernel: its resident blocks per SM x SMs, at most one
+// block per tile (the reduction partials hold two values per tile).
+template <typename K>
+static int bal_grid(K kern, int nblk) {
+    int per_sm = 0, dev = 0, sms = 0;
+    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, kEngBlock, 0) != cudaSuccess ||
+        cudaGetDevice(&dev) != cudaSuccess ||
+        cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess) {
+        cudaGetLastError();
+        per_sm = 1;
+        sms = kNumSMs;
+    }
+    return std::max(1, std::min(std::max(1, per_sm) * sms, nblk));
+}
+
+struct BalGrids {
+    int ax, sw, s2, r1, r2, eu, xr, pu;
+};
+
+// The balanced kernels' one-wave grids (queried once; before any capture)
+template <typename T, int R>
+static const BalGrids& bal_grids() {
+    static const BalGrids g = {bal_grid(k_bal_axsub<T, R>, INT_MAX), bal_grid(k_bal_sweep<T, R>, INT_MAX),
+                               bal_grid(k_bal_sweep2<T, R>, INT_MAX), bal_grid(k_bal_sweep56<T, 1, R>, INT_MAX),
+                               bal_grid(k_bal_sweep56<T, 2, R>, INT_MAX), bal_grid(k_bal_eupdate<T, R>, INT_MAX),
+                               bal_grid(k_bal_xrupdate<T, R>, INT_MAX), bal_grid(k_bal_pupdate<T, R>, INT_MAX)};
+    return g;
+}
+
+template <typename T>
+static void prepare_bal(int bal) {
+    if (bal == 8) bal_grids<T, 8>();
+    else if (bal) bal_grids<T, 4>();
+}
+
+template <typename T, int R>
+static void g_iteration_bal(bool pdl, const Eng<T>& E, const Shape& sh, cudaStream_t s) {
+    const int B = kEngBlock, n = E.nblk;
+    const BalGrids& G = bal_grids<T, R>();
+    const int g_ax = G.ax, g_sw = G.sw, g_s2 = G.s2, g_r1 = G.r1, g_r2 = G.r2, g_eu = G.eu, g_xr = G.xr, g_pu = G.pu;
+    auto apply = [&](const T* in, T* out, int mode) {
+        klaunch(pdl, k_bal_axsub<T, R>, std::min(g_ax, n), B, s, E, in, E.t);
+        if (sh.fuse) {
+            klaunch(pdl, k_bal_sweep2<T, R>, std::min(g_s2, n), B, s, E, 0, (const T*)E.t, out);
+            klaunch(pdl, k_bal_sweep2<T, R>, std::min(g_s2, n), B, s, E, 2, (const T*)out, E.t);
+        } else {
+            klaunch(pdl, k_bal_sweep<T, R>, std::min(g_sw, n), B, s, E, 0, (const T*)E.t, out);
+            klaunch(pdl, k_bal_sweep<T, R>, std::min(g_sw, n), B, s, E, 1, (const T*)out, E.t);
+            klaunch(pdl, k_bal_sweep<T, R>, std::min(g_sw, n), B, s, E, 2, (const T*)E.t, out);
+            klaunch(pdl, k_bal_sweep<T, R>, std::min(g_sw, n), B, s, E, 3, (const T*)out, E.t);
+        }
+        if (mode == 1) klaunch(pdl, k_bal_sweep56<T, 1, R>, std::min(g_r1, n), B, s, E, (const T*)E.t, out);
+        else klaunch(pdl, k_bal_sweep56<T, 2, R>, std::min(g_r2, n), B, s, E, (const T*)E.t, out);
+    };
+    apply((const T*)E.p, E.q, 1);                                        // q = PM A p ; RQ ; ALP
+    klaunch(pdl, k_bal_eupdate<T, R>, std::min(g_eu, n), B, s, E);      // e = r - ALP q
+    apply((const T*)E.e, E.v, 2);                                        // v = PM A e ; AMU
+    klaunch(pdl, k_bal_xrupdate<T, R>, std::min(g_xr, n), B, s, E);     // x, r ; RN, C1 ; stop tests
+    klaunch(pdl, k_bal_pupdate<T, R>, std::min(g_pu, n), B, s, E);      // p
+}
+
 template <typename T>
 static void g_iteration(bool pdl, const Eng<T>& E, const Shape& sh, cudaStream_t s) {
+    if (sh.bal && E.M == 1) {
+        if (sh.bal == 8) g_iteration_bal<T, 8>(pdl, E, sh, s);
+        else g_iteration_bal<T, 4>(pdl, E, sh, s);
+        return;
+    }
     const int g = grid_of(sh, E.nblk), b = sh.block;
     g_apply(pdl, E, sh, (const T*)E.p, E.q, E.t, 1, s);
     klaunch(pdl, k_eng_eupdate<T>, g, b, s, E);
@@ -577,9 +647,10 @@ static void g_iteration(bool pdl, const Eng<T>& E, const Shape& sh, cudaStream_t
 struct GraphKey {
     const void* work;
     long NV;
-    int M, prec, fuse, rblock;
+    int M, prec, fuse, rblock, bal;
     bool operator<(const GraphKey& o) const {
-        return std::tie(work, NV, M, prec, fuse, rblock) < std::tie(o.work, o.NV, o.M, o.prec, o.fuse, o.rblock);
+        return std::tie(work, NV, M, prec, fuse, rblock, bal) <
+               std::tie(o.work, o.NV, o.M, o.prec, o.fuse, o.rblock, o.bal);
     }
 };
 static std::mutex g_graph_mu;
@@ -606,7 +677,7 @@ void release_graphs_for(const void* work) {
 
 // WHILE { iteration ; guard } captured into a fresh graph
 template <typename T>
-static int build_loop_graph(const Eng<T>& E, bool pdl, int fuse, int rblock, cudaGraphExec_t* out) {
+static int build_loop_graph(const Eng<T>& E, bool pdl, int fuse, int rblock, int bal, cudaGraphExec_t* out) {
     if (!g_cap) CLOWNS_CUDA_TRY(cudaStreamCreateWithFlags(&g_cap, cudaStreamNonBlocking));
     cudaGraph_t graph;
     CLOWNS_CUDA_TRY(cudaGraphCreate(&graph, 0));
@@ -619,10 +690,12 @@ static int build_loop_graph(const Eng<T>& E, bool pdl, int fuse, int rblock, cud
     cudaGraphNode_t cnode;
     CLOWNS_CUDA_TRY(cudaGraphAddNode(&cnode, graph, nullptr, nullptr, 0, &cp));
     cudaGraph_t body = cp.conditional.phGraph_out[0];
+    prepare_bal<T>(bal);
     CLOWNS_CUDA_TRY(cudaStreamBeginCaptureToGraph(g_cap, body, nullptr, nullptr, 0, cudaStreamCaptureModeThreadLocal));
     Shape sh;
     sh.fuse = fuse;
     sh.rblock = rblock;
+    sh.bal = bal;
     g_iteration(pdl, E, sh, g_cap);
     klaunch(pdl, k_eng_guard, 1, 256, g_cap, E.S, E.M, E.ctrl, h);
     cudaGraph_t captured;
@@ -646,14 +719,15 @@ static int build_loop_graph(const Eng<T>& E, bool pdl, int fuse, int rblock, cud
 }
 
 template <typename T>
-static int loop_graph(const Eng<T>& E, const void* work, int prec, int fuse, int rblock, cudaGraphExec_t* out) {
+static int loop_graph(const Eng<T>& E, const void* work, int prec, int fuse, int rblock, int bal,
+                      cudaGraphExec_t* out) {
     std::lock_guard<std::mutex> lk(g_graph_mu);
-    GraphKey key{work, E.NV, E.M, prec, fuse, rblock};
+    GraphKey key{work, E.NV, E.M, prec, fuse, rblock, bal};
     auto it = g_graphs.find(key);
     if (it != g_graphs.end()) { *out = it->second; return CLOWNS_OK; }
     cudaGraphExec_t ex;
-    int rc = build_loop_graph(E, true, fuse, rblock, &ex);              // programmatic edges
-    if (rc) rc = build_loop_graph(E, false, fuse, rblock, &ex);         // plain edges if refused
+    int rc = build_loop_graph(E, true, fuse, rblock, bal, &ex);              // programmatic edges
+    if (rc) rc = build_loop_graph(E, false, fuse, rblock, bal, &ex);         // plain edges if refused
     if (rc) return rc;
     if (g_graphs.size() >= 64) {
         cudaGraphExecDestroy(g_graphs.begin()->second);
@@ -685,6 +759,7 @@ static int run_loop(Eng<T> E, const void* work, GridBar* gb, int prec, const Loo
         Shape ksh;
         ksh.fuse = sh.fuse;
         ksh.rblock = sh.rblock;
+        ksh.bal = sh.bal;
         int cap = 0;
         CLOWNS_CUDA_TRY(cudaMemcpyAsync(&cap, E.ctrl + 1, sizeof(int), cudaMemcpyDeviceToHost, s));
         CLOWNS_CUDA_TRY(cudaStreamSynchronize(s));
@@ -721,7 +796,7 @@ static int run_loop(Eng<T> E, const void* work, GridBar* gb, int prec, const Loo
     }
     if (sh.graph) {
         cudaGraphExec_t ex;
-        int rc = loop_graph(E, work, prec, sh.fuse, sh.rblock, &ex);
+        int rc = loop_graph(E, work, prec, sh.fuse, sh.rblock, sh.bal, &ex);
         if (rc) return rc;
         CLOWNS_CUDA_TRY(cudaMemsetAsync(gb, 0, sizeof(GridBar), s));
         CLOWNS_CUDA_TRY(cudaGraphLaunch(ex, s));
@@ -766,6 +841,8 @@ static int tune_loop(Eng<T> E, const void* work, GridBar* gb, long key_nv, int k
         sh.fuse = !(fz && !strcmp(fz, "0"));
         const char* rz = getenv("CLOWNS_REDUCE_BLOCK");   // forced executions: 128 unless "64"
         sh.rblock = (rz && !strcmp(rz, "64")) ? 64 : kStepBlock;
+        const char* bz = getenv("CLOWNS_BALANCED_ROWS");  // forced executions: tile kernels unless 4 or 8
+        sh.bal = E.M != 1 || !bz ? 0 : !strcmp(bz, "8") ? 8 : !strcmp(bz, "4") ? 4 : 0;
         *out = sh;
         return CLOWNS_OK;
     }
@@ -845,6 +922,16 @@ static int tune_loop(Eng<T> E, const void* work, GridBar* gb, long key_nv, int k
                 gsh.rblock = rb;
                 cands.push_back(gsh);
             }
+        // single systems: the balanced one-wave kernels, 4 or 8 rows per thread per step
+        if (E.M == 1)
+            for (int fuse : {1, 0})
+                for (int rows : {4, 8}) {
+                    LoopShape gsh;
+                    gsh.graph = 1;
+                    gsh.fuse = fuse;
+                    gsh.bal = rows;
+                    cands.push_back(gsh);
+                }
     }
     if (cands.empty()) {
         set_last_error_msg("pcgpme: the forced loop execution does not serve this system");
@@ -887,7 +974,8 @@ static int tune_loop(Eng<T> E, const void* work, GridBar* gb, long key_nv, int k
 }
 
 // mode: 0 persistent, 1 CUDA graph, 3 wavefront; fuse (graph): bit 0 fused sweep
-// pairs, bit 1 dot-product kernels at 64 threads per tile
+// pairs, bit 1 dot-product kernels at 64 threads per tile, bit 2 balanced
+// one-wave kernels (bit 3: 8 rows per thread per step, else 4)
 int engine_tuned_shape(long nv, int prec, int single, int* mode, int* block, int* grid, int* minb, int* fuse) {
     std::lock_guard<std::mutex> lk(g_loop_mu);
     auto it = g_loop_shapes.find(std::make_tuple(nv, prec, single));
@@ -897,7 +985,7 @@ int engine_tuned_shape(long nv, int prec, int single, int* mode, int* block, int
     *block = sh.block;
     *grid = sh.graph == 1 ? 0 : sh.grid;
     *minb = sh.graph == 1 ? 0 : sh.minb;
-    *fuse = sh.graph == 1 ? (sh.fuse | (sh.rblock != kStepBlock ? 2 : 0)) : 0;
+    *fuse = sh.graph == 1 ? (sh.fuse | (sh.rblock != kStepBlock ? 2 : 0) | (sh.bal ? 4 : 0) | (sh.bal == 8 ? 8 : 0)) : 0;
     return CLOWNS_OK;
 }
 

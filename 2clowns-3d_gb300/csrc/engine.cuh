@@ -224,6 +224,71 @@ __device__ __forceinline__ void stop_member(MemberScalars* S, int reason, int ie
     if (ier) S->ier = ier;
 }
 
+// Finalisation of the reductions, by one thread once a member's totals are
+// known.  MODE 1: RQ -> ALP = C1 / RQ (pcgpme_para.F90:167); MODE 2: AMU =
+// (e,v) / (v,v) (197).
+template <int MODE>
+__device__ __forceinline__ void finish_sweep56(MemberScalars* S, const double (&tot)[2]) {
+    if (MODE == 1) {
+        const double C1 = sld(&S->C1);
+        S->RQ = tot[0];
+        const double ALP = C1 / tot[0];                         // 167
+        S->ALP = ALP;
+        if (!isfinite(tot[0]) || !isfinite(ALP)) {
+            S->K = sld(&S->K) + 1;
+            stop_member(S, CLOWNS_STOP_NONFINITE, sld(&S->mode) != 1 ? CLOWNS_IER_NONFINITE : 0);
+        }
+    } else {
+        S->SS = tot[1];
+        const double AMU = tot[0] / tot[1];                     // 197
+        S->AMU = AMU;
+        if (!isfinite(tot[1]) || !isfinite(AMU)) {
+            S->K = sld(&S->K) + 1;
+            stop_member(S, CLOWNS_STOP_NONFINITE, sld(&S->mode) != 1 ? CLOWNS_IER_NONFINITE : 0);
+        }
+    }
+}
+
+// RN, C1 -> ERR, the stop tests and BETA (pcgpme_para.F90:215-254).
+__device__ __forceinline__ void finish_xrupdate(MemberScalars* S, const double (&tot)[2]) {
+    const double RN = tot[0], C1 = tot[1];
+    const double AMUs = sld(&S->AMU), RQ = sld(&S->RQ), BN = sld(&S->BN);
+    const double ERRP = sld(&S->ERRP), EPS = sld(&S->EPS);
+    const int mode = sld(&S->mode), ITER = sld(&S->ITER);
+    S->RN = RN;
+    S->C1 = C1;
+    const int K = sld(&S->K) + 1;
+    S->K = K;
+    S->total_iter = sld(&S->total_iter) + 1;
+    const double ERR = sqrt(RN / BN);                            // 215
+    S->ERR = ERR;
+    if (!isfinite(RN) || !isfinite(C1)) {
+        stop_member(S, CLOWNS_STOP_NONFINITE, mode != 1 ? CLOWNS_IER_NONFINITE : 0);
+    } else if (K >= 10 && fabs(ERR - ERRP) <= ERR * 1.0e-6) {    // 228
+        stop_member(S, CLOWNS_STOP_STAGNATION, 0);
+    } else if (ERR <= EPS) {                                     // 232
+        stop_member(S, CLOWNS_STOP_TOL, 0);
+    } else {
+        S->ERRP = ERR;
+        if (AMUs == 0.0) {                                       // 234
+            stop_member(S, CLOWNS_STOP_AMU_ZERO, 0);
+        } else if (C1 == 0.0) {                                  // 240
+            stop_member(S, CLOWNS_STOP_C1_ZERO, 0);
+        } else {
+            // 241 (pcgpme_para.F90); PCGPME_WILL forms C1 / (AMU RQ), pcgpme_2DH.f90:255
+            S->BETA = mode == 2 ? C1 / (AMUs * RQ) : C1 / AMUs / RQ;
+            if (K >= ITER) {                                     // 250-254
+                if (mode != 1) {
+                    stop_member(S, CLOWNS_STOP_MAXITER, CLOWNS_IER_MAXITER);
+                    S->K = ITER + 1;
+                } else {
+                    stop_member(S, CLOWNS_STOP_MAXITER, 0);
+                }
+            }
+        }
+    }
+}
+
 // ---------------------------------------------------------------------------
 // Setup: scaling W = P2/(max(sum|AL|,D)+P1 D), scaled copies and the per-row
 // exchange sort (pcgpme_para.F90:77-112).  Explicitly rounded arithmetic so the
@@ -535,26 +600,8 @@ __device__ __forceinline__ bool tl_sweep56(const Eng<T>& E, int blk, const T* __
         double tot[2];
         if (!member_reduce(E, blk, m, acc0, acc1, red, tot)) return false;
         if (threadIdx.x == 0) {
-            MemberScalars* S = E.S + m;
             E.ticket[m] = 0;
-            if (MODE == 1) {
-                const double C1 = sld(&S->C1);
-                S->RQ = tot[0];
-                const double ALP = C1 / tot[0];                         // 167
-                S->ALP = ALP;
-                if (!isfinite(tot[0]) || !isfinite(ALP)) {
-                    S->K = sld(&S->K) + 1;
-                    stop_member(S, CLOWNS_STOP_NONFINITE, sld(&S->mode) != 1 ? CLOWNS_IER_NONFINITE : 0);
-                }
-            } else {
-                S->SS = tot[1];
-                const double AMU = tot[0] / tot[1];                     // 197
-                S->AMU = AMU;
-                if (!isfinite(tot[1]) || !isfinite(AMU)) {
-                    S->K = sld(&S->K) + 1;
-                    stop_member(S, CLOWNS_STOP_NONFINITE, sld(&S->mode) != 1 ? CLOWNS_IER_NONFINITE : 0);
-                }
-            }
+            finish_sweep56<MODE>(E.S + m, tot);
             __threadfence();
         }
         __syncwarp();
@@ -642,44 +689,8 @@ __device__ __forceinline__ bool tl_xrupdate(const Eng<T>& E, int blk, double* re
         double tot[2];
         if (!member_reduce(E, blk, m, acc0, acc1, red, tot)) return false;
         if (threadIdx.x == 0) {
-            MemberScalars* S = E.S + m;
             E.ticket[m] = 0;
-            const double RN = tot[0], C1 = tot[1];
-            const double AMUs = sld(&S->AMU), RQ = sld(&S->RQ), BN = sld(&S->BN);
-            const double ERRP = sld(&S->ERRP), EPS = sld(&S->EPS);
-            const int mode = sld(&S->mode), ITER = sld(&S->ITER);
-            S->RN = RN;
-            S->C1 = C1;
-            const int K = sld(&S->K) + 1;
-            S->K = K;
-            S->total_iter = sld(&S->total_iter) + 1;
-            const double ERR = sqrt(RN / BN);                            // 215
-            S->ERR = ERR;
-            if (!isfinite(RN) || !isfinite(C1)) {
-                stop_member(S, CLOWNS_STOP_NONFINITE, mode != 1 ? CLOWNS_IER_NONFINITE : 0);
-            } else if (K >= 10 && fabs(ERR - ERRP) <= ERR * 1.0e-6) {    // 228
-                stop_member(S, CLOWNS_STOP_STAGNATION, 0);
-            } else if (ERR <= EPS) {                                     // 232
-                stop_member(S, CLOWNS_STOP_TOL, 0);
-            } else {
-                S->ERRP = ERR;
-                if (AMUs == 0.0) {                                       // 234
-                    stop_member(S, CLOWNS_STOP_AMU_ZERO, 0);
-                } else if (C1 == 0.0) {                                  // 240
-                    stop_member(S, CLOWNS_STOP_C1_ZERO, 0);
-                } else {
-                    // 241 (pcgpme_para.F90); PCGPME_WILL forms C1 / (AMU RQ), pcgpme_2DH.f90:255
-                    S->BETA = mode == 2 ? C1 / (AMUs * RQ) : C1 / AMUs / RQ;
-                    if (K >= ITER) {                                     // 250-254
-                        if (mode != 1) {
-                            stop_member(S, CLOWNS_STOP_MAXITER, CLOWNS_IER_MAXITER);
-                            S->K = ITER + 1;
-                        } else {
-                            stop_member(S, CLOWNS_STOP_MAXITER, 0);
-                        }
-                    }
-                }
-            }
+            finish_xrupdate(E.S + m, tot);
             __threadfence();
         }
         __syncwarp();
@@ -819,6 +830,324 @@ template <typename T>
 __global__ void __launch_bounds__(kEngBlock) k_eng_initres(Eng<T> E) {
     pdl_enter();
     ph_initres(E);
+}
+
+// ---------------------------------------------------------------------------
+// Balanced kernels (single systems).  The iteration's kernels can instead run
+// as exactly one wave each: G = (resident blocks per SM) x SMs blocks, block b
+// owning the rows [n b / G, n (b+1) / G) and walking them R rows per thread
+// per step.  Every block then does the same work and all retire together, and
+// the per-block costs -- launch, the stop-flag and scalar loads, the reduction
+// tail -- are paid G times per kernel instead of once per 512-row tile (5517
+// times at 2.8 M rows).  The per-row arithmetic is the tile kernels'; dot
+// products are reduced once per block: the block's partial goes to
+// partials[b], and the last block to finish sums the G partials in index order
+// (deterministic for a given G) and finalises the scalars.  Callers keep G at
+// most nblk (the partials hold two values per tile).
+
+__device__ __forceinline__ void bal_range(long n, long& lo, long& hi) {
+    lo = n * (long)blockIdx.x / (long)gridDim.x;
+    hi = n * (long)(blockIdx.x + 1) / (long)gridDim.x;
+}
+
+// Block partial of (v0, v1), then the last block sums all partials; true in
+// every thread of that block, with the totals in tot[] of warp 0.
+template <typename T, typename A>
+__device__ __forceinline__ bool bal_reduce(const Eng<T>& E, A v0, A v1, double* red, double (&tot)[2]) {
+    __shared__ int s_last;
+    const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5, nw = blockDim.x >> 5;
+    const A w = warp_pair_sum(v0, v1);
+    if (lane == 0) red[wid] = (double)w;
+    if (lane == 16) red[32 + wid] = (double)w;
+    __syncthreads();
+    if (wid == 0) {
+        const double a = lane < nw ? red[lane] : 0.0, b = lane < nw ? red[32 + lane] : 0.0;
+        const double s = warp_pair_sum(a, b);
+        if (lane == 0) E.partials[2L * blockIdx.x + 0] = s;
+        if (lane == 16) E.partials[2L * blockIdx.x + 1] = s;
+        if (lane == 0 || lane == 16) __threadfence();
+        __syncwarp();
+        if (lane == 0) s_last = atomicAdd(&E.ticket[0], 1u) == gridDim.x - 1u;
+    }
+    __syncthreads();
+    if (!s_last) return false;
+    __threadfence();
+    double a = 0.0, b = 0.0;
+    for (int q = threadIdx.x; q < (int)gridDim.x; q += blockDim.x) {
+        a += __ldcg(E.partials + 2L * q + 0);
+        b += __ldcg(E.partials + 2L * q + 1);
+    }
+    const double w2 = warp_pair_sum(a, b);
+    __syncthreads();                          // every warp has read red[] above
+    if (lane == 0) red[wid] = w2;
+    if (lane == 16) red[32 + wid] = w2;
+    __syncthreads();
+    if (wid == 0) {
+        a = lane < nw ? red[lane] : 0.0;
+        b = lane < nw ? red[32 + lane] : 0.0;
+        const double s = warp_pair_sum(a, b);
+        tot[0] = __shfl_sync(0xffffffffu, s, 0);
+        tot[1] = __shfl_sync(0xffffffffu, s, 16);
+    }
+    return true;
+}
+
+template <typename T, int R>
+__global__ void __launch_bounds__(kEngBlock) k_bal_axsub(Eng<T> E, const T* __restrict__ in, T* __restrict__ out) {
+    pdl_enter();
+    const long NV = E.NV;
+    const int done = sld(&E.S[0].done);
+    long lo, hi;
+    bal_range(E.n1, lo, hi);
+    for (long base = lo + threadIdx.x; base < hi; base += (long)blockDim.x * R) {
+        T s[R];
+        bool ok[R];
+#pragma unroll
+        for (int u = 0; u < R; u++) {
+            const long r = base + (long)u * blockDim.x;
+            ok[u] = r < hi;
+            const long i = ok[u] ? r : lo;
+            s[u] = ldg2(in + i) * ld_stream(E.d + i);
+        }
+#pragma unroll
+        for (int k = 0; k < 6; k++) {
+            T a[R];
+            int c[R];
+#pragma unroll
+            for (int u = 0; u < R; u++) {
+                const long i = ok[u] ? base + (long)u * blockDim.x : lo;
+                a[u] = ld_stream(E.al + k * NV + i);
+                c[u] = ld_stream(E.ll + k * NV + i);
+            }
+#pragma unroll
+            for (int u = 0; u < R; u++) s[u] += a[u] * ldg2(in + c[u]);
+        }
+#pragma unroll
+        for (int u = 0; u < R; u++)
+            if (ok[u] && !done) out[base + (long)u * blockDim.x] = s[u];
+    }
+}
+
+template <typename T, int R>
+__global__ void __launch_bounds__(kEngBlock) k_bal_sweep(Eng<T> E, int k, const T* __restrict__ in,
+                                                        T* __restrict__ out) {
+    pdl_enter();
+    const long NV = E.NV;
+    const T* __restrict__ a = E.al + k * NV;
+    const int* __restrict__ c = E.ll + k * NV;
+    const int done = sld(&E.S[0].done);
+    long lo, hi;
+    bal_range(E.n1, lo, hi);
+    for (long base = lo + threadIdx.x; base < hi; base += (long)blockDim.x * R) {
+        T av[R], xv[R], gv[R];
+        int cv[R];
+        bool ok[R];
+#pragma unroll
+        for (int u = 0; u < R; u++) {
+            const long r = base + (long)u * blockDim.x;
+            ok[u] = r < hi;
+            const long i = ok[u] ? r : lo;
+            av[u] = ld_stream(a + i);
+            cv[u] = ld_stream(c + i);
+            xv[u] = ldg2(in + i);
+        }
+#pragma unroll
+        for (int u = 0; u < R; u++) gv[u] = ldg2(in + cv[u]);
+#pragma unroll
+        for (int u = 0; u < R; u++)
+            if (ok[u] && !done) out[base + (long)u * blockDim.x] = fnma(av[u], gv[u], xv[u]);
+    }
+}
+
+// the fused pair of sweeps k, k+1 (as tl_sweep2)
+template <typename T, int R>
+__global__ void __launch_bounds__(kEngBlock) k_bal_sweep2(Eng<T> E, int k, const T* __restrict__ in,
+                                                         T* __restrict__ out) {
+    pdl_enter();
+    const long NV = E.NV;
+    const T* __restrict__ a0 = E.al + k * NV;
+    const int* __restrict__ c0 = E.ll + k * NV;
+    const T* __restrict__ a1 = a0 + NV;
+    const int* __restrict__ c1 = c0 + NV;
+    const int done = sld(&E.S[0].done);
+    long lo, hi;
+    bal_range(E.n1, lo, hi);
+    for (long base = lo + threadIdx.x; base < hi; base += (long)blockDim.x * R) {
+        T x[R], aa[R], ab[R], xj[R], aj[R];
+        int ca[R], cb[R], cj[R];
+        bool ok[R];
+#pragma unroll
+        for (int u = 0; u < R; u++) {
+            const long r = base + (long)u * blockDim.x;
+            ok[u] = r < hi;
+            const long i = ok[u] ? r : lo;
+            x[u] = ldg2(in + i);
+            aa[u] = ld_stream(a0 + i);
+            ca[u] = ld_stream(c0 + i);
+            ab[u] = ld_stream(a1 + i);
+            cb[u] = ld_stream(c1 + i);
+        }
+#pragma unroll
+        for (int u = 0; u < R; u++) {
+            xj[u] = ldg2(in + cb[u]);
+            aj[u] = ldg2(a0 + cb[u]);
+            cj[u] = ldg2(c0 + cb[u]);
+        }
+        T oi[R], oj[R];
+#pragma unroll
+        for (int u = 0; u < R; u++) {
+            oi[u] = fnma(aa[u], ldg2(in + ca[u]), x[u]);
+            oj[u] = fnma(aj[u], ldg2(in + cj[u]), xj[u]);
+        }
+#pragma unroll
+        for (int u = 0; u < R; u++)
+            if (ok[u] && !done) out[base + (long)u * blockDim.x] = fnma(ab[u], oj[u], oi[u]);
+    }
+}
+
+// sweeps 5, 6 with the RQ (MODE 1) or AMU (MODE 2) reduction (as tl_sweep56)
+template <typename T, int MODE, int R>
+__global__ void __launch_bounds__(kEngBlock) k_bal_sweep56(Eng<T> E, const T* __restrict__ in, T* __restrict__ out) {
+    pdl_enter();
+    __shared__ double red[64];
+    const long NV = E.NV;
+    const T* __restrict__ a5 = E.al + 4 * NV;
+    const T* __restrict__ a6 = E.al + 5 * NV;
+    const int* __restrict__ c5 = E.ll + 4 * NV;
+    const int* __restrict__ c6 = E.ll + 5 * NV;
+    const int done = sld(&E.S[0].done);
+    T acc0 = T(0), acc1 = T(0);
+    long lo, hi;
+    bal_range(E.n1, lo, hi);
+    for (long base = lo + threadIdx.x; base < hi; base += (long)blockDim.x * R) {
+        T a5v[R], a6v[R], xv[R], g5[R], g6[R];
+        int c5v[R], c6v[R];
+        bool ok[R];
+#pragma unroll
+        for (int u = 0; u < R; u++) {
+            const long r = base + (long)u * blockDim.x;
+            ok[u] = r < hi;
+            const long i = ok[u] ? r : lo;
+            a5v[u] = ld_stream(a5 + i);
+            a6v[u] = ld_stream(a6 + i);
+            c5v[u] = ld_stream(c5 + i);
+            c6v[u] = ld_stream(c6 + i);
+            xv[u] = ldg2(in + i);
+        }
+#pragma unroll
+        for (int u = 0; u < R; u++) {
+            g5[u] = ldg2(in + c5v[u]);
+            g6[u] = ldg2(in + c6v[u]);
+        }
+#pragma unroll
+        for (int u = 0; u < R; u++) {
+            if (!ok[u] || done) continue;
+            const long i = base + (long)u * blockDim.x;
+            const T y = fnma(a6v[u], g6[u], fnma(a5v[u], g5[u], xv[u]));
+            out[i] = y;
+            if (MODE == 1) acc0 += ldg2(E.r0 + i) * y;
+            if (MODE == 2) { acc0 += ldg2(E.e + i) * y; acc1 += y * y; }
+        }
+    }
+    if (MODE == 0 || done) return;
+    double tot[2];
+    if (!bal_reduce(E, acc0, acc1, red, tot)) return;
+    if (threadIdx.x == 0) {
+        E.ticket[0] = 0;
+        finish_sweep56<MODE>(E.S, tot);
+        __threadfence();
+    }
+}
+
+template <typename T, int R>
+__global__ void __launch_bounds__(kEngBlock) k_bal_eupdate(Eng<T> E) {
+    pdl_enter();
+    const int done = sld(&E.S[0].done);
+    const T ALP = T(sld(&E.S[0].ALP));
+    long lo, hi;
+    bal_range(E.n1, lo, hi);
+    for (long base = lo + threadIdx.x; base < hi; base += (long)blockDim.x * R) {
+        T rv[R], qv[R];
+#pragma unroll
+        for (int u = 0; u < R; u++) {
+            const long r = base + (long)u * blockDim.x;
+            const long i = r < hi ? r : lo;
+            rv[u] = ldg2(E.r + i);
+            qv[u] = ldg2(E.q + i);
+        }
+#pragma unroll
+        for (int u = 0; u < R; u++) {
+            const long r = base + (long)u * blockDim.x;
+            if (r < hi && !done) E.e[r] = rv[u] - ALP * qv[u];
+        }
+    }
+}
+
+template <typename T, int R>
+__global__ void __launch_bounds__(kEngBlock) k_bal_xrupdate(Eng<T> E) {
+    pdl_enter();
+    __shared__ double red[64];
+    const int done = sld(&E.S[0].done);
+    const T ALP = T(sld(&E.S[0].ALP)), AMU = T(sld(&E.S[0].AMU));
+    T acc0 = T(0), acc1 = T(0);
+    long lo, hi;
+    bal_range(E.n1, lo, hi);
+    for (long base = lo + threadIdx.x; base < hi; base += (long)blockDim.x * R) {
+        T ev[R], xv[R], pv[R], vv[R], r0v[R];
+#pragma unroll
+        for (int u = 0; u < R; u++) {
+            const long r = base + (long)u * blockDim.x;
+            const long i = r < hi ? r : lo;
+            ev[u] = ldg2(E.e + i);
+            xv[u] = ldg2(E.xi + i);
+            pv[u] = ldg2(E.p + i);
+            vv[u] = ldg2(E.v + i);
+            r0v[u] = ldg2(E.r0 + i);
+        }
+#pragma unroll
+        for (int u = 0; u < R; u++) {
+            const long r = base + (long)u * blockDim.x;
+            if (r >= hi || done) continue;
+            E.xi[r] = xv[u] + ALP * pv[u] + AMU * ev[u];
+            const T rn = ev[u] - AMU * vv[u];
+            E.r[r] = rn;
+            acc0 += rn * rn;
+            acc1 += rn * r0v[u];
+        }
+    }
+    if (done) return;
+    double tot[2];
+    if (!bal_reduce(E, acc0, acc1, red, tot)) return;
+    if (threadIdx.x == 0) {
+        E.ticket[0] = 0;
+        finish_xrupdate(E.S, tot);
+        __threadfence();
+    }
+}
+
+template <typename T, int R>
+__global__ void __launch_bounds__(kEngBlock) k_bal_pupdate(Eng<T> E) {
+    pdl_enter();
+    const int done = sld(&E.S[0].done);
+    const T BETA = T(sld(&E.S[0].BETA)), AMU = T(sld(&E.S[0].AMU));
+    long lo, hi;
+    bal_range(E.n1, lo, hi);
+    for (long base = lo + threadIdx.x; base < hi; base += (long)blockDim.x * R) {
+        T rv[R], pv[R], qv[R];
+#pragma unroll
+        for (int u = 0; u < R; u++) {
+            const long r = base + (long)u * blockDim.x;
+            const long i = r < hi ? r : lo;
+            rv[u] = ldg2(E.r + i);
+            pv[u] = ldg2(E.p + i);
+            qv[u] = ldg2(E.q + i);
+        }
+#pragma unroll
+        for (int u = 0; u < R; u++) {
+            const long r = base + (long)u * blockDim.x;
+            if (r < hi && !done) E.p[r] = rv[u] + BETA * (pv[u] - AMU * qv[u]);
+        }
+    }
 }
 
 // Graph mode: the last node of the WHILE body and the only writer of the loop

@@ -173,7 +173,10 @@ int clowns_pcgpme_batched_dev(int m, const clowns_member* members, int precision
  * threads per block; grid: blocks of the cooperative kernels (0 for the graph);
  * regs: their register budget per thread (0 for the graph); fused (graph): bit 0
  * set when LDUSUB's sweeps 1-2 and 3-4 run as fused pairs, bit 1 set when the
- * dot-product kernels run 64 threads per 512-row tile (8 rows per thread).  CLOWNS_ERR_ARG until
+ * dot-product kernels run 64 threads per 512-row tile (8 rows per thread), bit 2
+ * set when a single system runs the balanced kernels (each kernel one wave of
+ * 256-thread blocks over even row ranges, one reduction per block), bit 3 set
+ * when those take 8 rows per thread per step (else 4).  CLOWNS_ERR_ARG until
  * a solve of that size has run. */
 #define CLOWNS_LOOP_PERSISTENT 0
 #define CLOWNS_LOOP_GRAPH 1

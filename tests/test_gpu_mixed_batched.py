@@ -59,15 +59,18 @@ def test_mixed_matches_fp64_oracle(gpu, ora, systems, idx):
             assert err <= max(1e-9, 2 * err_oracle), (label, err, err_oracle, info.as_dict())
 
 
+@pytest.mark.parametrize("balanced", ["0", "4", "8"])
 @pytest.mark.parametrize("precision", ["fp64", "mixed"])
-def test_fused_kernels_bit_identical(gpu, systems, monkeypatch, precision):
+def test_fused_kernels_bit_identical(gpu, systems, monkeypatch, precision, balanced):
     """The fused LDUSUB sweep pairs (sweep J recomputed at the one row sweep J+1
     gathers) round exactly like the separate sweeps: forcing the CUDA-graph loop
     with and without them gives the same iterations and the same solution bit
-    for bit, in FP64 and in the FP32 inner solve."""
+    for bit, in FP64 and in the FP32 inner solve, with the tile kernels and with
+    the balanced one-wave kernels (4 or 8 rows per thread per step)."""
     label, case, sy, ds = systems[1]
     n = ds.mnoe
     monkeypatch.setenv("CLOWNS_LOOP_MODE", "graph")
+    monkeypatch.setenv("CLOWNS_BALANCED_ROWS", balanced)
     out = []
     for fuse in ("0", "1"):
         monkeypatch.setenv("CLOWNS_SWEEP_FUSE", fuse)
@@ -81,6 +84,34 @@ def test_fused_kernels_bit_identical(gpu, systems, monkeypatch, precision):
     for it, xv in out[1:]:
         assert it == out[0][0]
         assert np.array_equal(xv, out[0][1])
+
+
+@pytest.mark.parametrize("balanced", ["4", "8"])
+@pytest.mark.parametrize("label", [c[0] for c in CASES])
+def test_balanced_kernels_match_oracle(gpu, ora, systems, monkeypatch, label, balanced):
+    """The balanced one-wave kernels (rows split evenly over one wave of blocks,
+    one reduction per block) solve to the oracle's pressure: within 1e-10
+    relative L2 at ERR <= 1e-13 in FP64, within the mixed path's bound at
+    ERR <= 1e-12 in mixed precision; iteration counts within 25 % of the
+    oracle's (the reduction order differs from the tile kernels')."""
+    idx = [c[0] for c in CASES].index(label)
+    _, case, sy, ds = systems[idx]
+    n = ds.mnoe
+    monkeypatch.setenv("CLOWNS_LOOP_MODE", "graph")
+    monkeypatch.setenv("CLOWNS_BALANCED_ROWS", balanced)
+    x = _x(ds)
+    info = gpu.Solver(n).solve(ds.alu, ds.llu, ds.de, ds.b, x, eps=1e-13)
+    ref = ora.pcgpme(sy.alu, sy.llu, sy.de[1:], sy.b[1:], n, eps=1e-13)
+    xg = x.cpu().numpy()[:n]
+    assert info.ier == 0 and ref.ier == 0, info.as_dict()
+    assert np.linalg.norm(xg - ref.x) <= 1e-10 * np.linalg.norm(ref.x)
+    assert abs(info.iter - ref.iters) <= max(5, ref.iters // 4), (info.iter, ref.iters)
+    x = _x(ds)
+    info = gpu.MixedSolver(n).solve(ds.alu, ds.llu, ds.de, ds.b, x, eps=1e-12)
+    assert info.ier == 0 and info.eps <= 1e-12, info.as_dict()
+    xd = _direct(ora, sy)
+    err_oracle = np.linalg.norm(ora.pcgpme(sy.alu, sy.llu, sy.de[1:], sy.b[1:], n, eps=1e-12).x - xd)
+    assert np.linalg.norm(x.cpu().numpy()[:n] - xd) <= max(1e-9 * np.linalg.norm(xd), 2 * err_oracle)
 
 
 def test_mixed_true_residual(gpu, ora, systems):
