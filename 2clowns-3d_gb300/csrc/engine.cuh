@@ -844,11 +844,23 @@ __global__ void __launch_bounds__(kEngBlock) k_eng_initres(Eng<T> E) {
 // partials[b], and the last block to finish sums the G partials in index order
 // (deterministic for a given G) and finalises the scalars.  Callers keep G at
 // most nblk (the partials hold two values per tile).
+//
+// Only the kernels whose results outlive a stop test read the stop flag:
+// sweep56 (its reduction and finalisation) and xrupdate (x, r and the stop
+// tests); after a stop the other kernels of the body write scratch vectors (t,
+// q, e, v, p) the finished solve no longer reads, and the loop guard ends the
+// graph at the end of the body.  (A flag load in every kernel cost 2-4 us per
+// kernel at 2.8 M rows, as did reading the scalars once per block behind a
+// barrier; each thread loads them, and the load overlaps its data loads.)
+// FP64 kernels at 4 rows per thread are held to 85 registers (3 blocks per SM).
 
 __device__ __forceinline__ void bal_range(long n, long& lo, long& hi) {
     lo = n * (long)blockIdx.x / (long)gridDim.x;
     hi = n * (long)(blockIdx.x + 1) / (long)gridDim.x;
 }
+
+template <typename T, int R>
+constexpr int kBalMinBlocks = sizeof(T) == 8 && R == 4 ? 3 : 1;
 
 // Block partial of (v0, v1), then the last block sums all partials; true in
 // every thread of that block, with the totals in tot[] of warp 0.
@@ -893,10 +905,9 @@ __device__ __forceinline__ bool bal_reduce(const Eng<T>& E, A v0, A v1, double* 
 }
 
 template <typename T, int R>
-__global__ void __launch_bounds__(kEngBlock) k_bal_axsub(Eng<T> E, const T* __restrict__ in, T* __restrict__ out) {
+__global__ void __launch_bounds__(kEngBlock, kBalMinBlocks<T, R>) k_bal_axsub(Eng<T> E, const T* __restrict__ in, T* __restrict__ out) {
     pdl_enter();
     const long NV = E.NV;
-    const int done = sld(&E.S[0].done);
     long lo, hi;
     bal_range(E.n1, lo, hi);
     for (long base = lo + threadIdx.x; base < hi; base += (long)blockDim.x * R) {
@@ -924,18 +935,17 @@ __global__ void __launch_bounds__(kEngBlock) k_bal_axsub(Eng<T> E, const T* __re
         }
 #pragma unroll
         for (int u = 0; u < R; u++)
-            if (ok[u] && !done) out[base + (long)u * blockDim.x] = s[u];
+            if (ok[u]) out[base + (long)u * blockDim.x] = s[u];
     }
 }
 
 template <typename T, int R>
-__global__ void __launch_bounds__(kEngBlock) k_bal_sweep(Eng<T> E, int k, const T* __restrict__ in,
+__global__ void __launch_bounds__(kEngBlock, kBalMinBlocks<T, R>) k_bal_sweep(Eng<T> E, int k, const T* __restrict__ in,
                                                         T* __restrict__ out) {
     pdl_enter();
     const long NV = E.NV;
     const T* __restrict__ a = E.al + k * NV;
     const int* __restrict__ c = E.ll + k * NV;
-    const int done = sld(&E.S[0].done);
     long lo, hi;
     bal_range(E.n1, lo, hi);
     for (long base = lo + threadIdx.x; base < hi; base += (long)blockDim.x * R) {
@@ -955,13 +965,13 @@ __global__ void __launch_bounds__(kEngBlock) k_bal_sweep(Eng<T> E, int k, const 
         for (int u = 0; u < R; u++) gv[u] = ldg2(in + cv[u]);
 #pragma unroll
         for (int u = 0; u < R; u++)
-            if (ok[u] && !done) out[base + (long)u * blockDim.x] = fnma(av[u], gv[u], xv[u]);
+            if (ok[u]) out[base + (long)u * blockDim.x] = fnma(av[u], gv[u], xv[u]);
     }
 }
 
 // the fused pair of sweeps k, k+1 (as tl_sweep2)
 template <typename T, int R>
-__global__ void __launch_bounds__(kEngBlock) k_bal_sweep2(Eng<T> E, int k, const T* __restrict__ in,
+__global__ void __launch_bounds__(kEngBlock, kBalMinBlocks<T, R>) k_bal_sweep2(Eng<T> E, int k, const T* __restrict__ in,
                                                          T* __restrict__ out) {
     pdl_enter();
     const long NV = E.NV;
@@ -969,7 +979,6 @@ __global__ void __launch_bounds__(kEngBlock) k_bal_sweep2(Eng<T> E, int k, const
     const int* __restrict__ c0 = E.ll + k * NV;
     const T* __restrict__ a1 = a0 + NV;
     const int* __restrict__ c1 = c0 + NV;
-    const int done = sld(&E.S[0].done);
     long lo, hi;
     bal_range(E.n1, lo, hi);
     for (long base = lo + threadIdx.x; base < hi; base += (long)blockDim.x * R) {
@@ -1001,13 +1010,13 @@ __global__ void __launch_bounds__(kEngBlock) k_bal_sweep2(Eng<T> E, int k, const
         }
 #pragma unroll
         for (int u = 0; u < R; u++)
-            if (ok[u] && !done) out[base + (long)u * blockDim.x] = fnma(ab[u], oj[u], oi[u]);
+            if (ok[u]) out[base + (long)u * blockDim.x] = fnma(ab[u], oj[u], oi[u]);
     }
 }
 
 // sweeps 5, 6 with the RQ (MODE 1) or AMU (MODE 2) reduction (as tl_sweep56)
 template <typename T, int MODE, int R>
-__global__ void __launch_bounds__(kEngBlock) k_bal_sweep56(Eng<T> E, const T* __restrict__ in, T* __restrict__ out) {
+__global__ void __launch_bounds__(kEngBlock, kBalMinBlocks<T, R>) k_bal_sweep56(Eng<T> E, const T* __restrict__ in, T* __restrict__ out) {
     pdl_enter();
     __shared__ double red[64];
     const long NV = E.NV;
@@ -1060,9 +1069,8 @@ __global__ void __launch_bounds__(kEngBlock) k_bal_sweep56(Eng<T> E, const T* __
 }
 
 template <typename T, int R>
-__global__ void __launch_bounds__(kEngBlock) k_bal_eupdate(Eng<T> E) {
+__global__ void __launch_bounds__(kEngBlock, kBalMinBlocks<T, R>) k_bal_eupdate(Eng<T> E) {
     pdl_enter();
-    const int done = sld(&E.S[0].done);
     const T ALP = T(sld(&E.S[0].ALP));
     long lo, hi;
     bal_range(E.n1, lo, hi);
@@ -1078,13 +1086,13 @@ __global__ void __launch_bounds__(kEngBlock) k_bal_eupdate(Eng<T> E) {
 #pragma unroll
         for (int u = 0; u < R; u++) {
             const long r = base + (long)u * blockDim.x;
-            if (r < hi && !done) E.e[r] = rv[u] - ALP * qv[u];
+            if (r < hi) E.e[r] = rv[u] - ALP * qv[u];
         }
     }
 }
 
 template <typename T, int R>
-__global__ void __launch_bounds__(kEngBlock) k_bal_xrupdate(Eng<T> E) {
+__global__ void __launch_bounds__(kEngBlock, kBalMinBlocks<T, R>) k_bal_xrupdate(Eng<T> E) {
     pdl_enter();
     __shared__ double red[64];
     const int done = sld(&E.S[0].done);
@@ -1126,9 +1134,8 @@ __global__ void __launch_bounds__(kEngBlock) k_bal_xrupdate(Eng<T> E) {
 }
 
 template <typename T, int R>
-__global__ void __launch_bounds__(kEngBlock) k_bal_pupdate(Eng<T> E) {
+__global__ void __launch_bounds__(kEngBlock, kBalMinBlocks<T, R>) k_bal_pupdate(Eng<T> E) {
     pdl_enter();
-    const int done = sld(&E.S[0].done);
     const T BETA = T(sld(&E.S[0].BETA)), AMU = T(sld(&E.S[0].AMU));
     long lo, hi;
     bal_range(E.n1, lo, hi);
@@ -1145,7 +1152,7 @@ __global__ void __launch_bounds__(kEngBlock) k_bal_pupdate(Eng<T> E) {
 #pragma unroll
         for (int u = 0; u < R; u++) {
             const long r = base + (long)u * blockDim.x;
-            if (r < hi && !done) E.p[r] = rv[u] + BETA * (pv[u] - AMU * qv[u]);
+            if (r < hi) E.p[r] = rv[u] + BETA * (pv[u] - AMU * qv[u]);
         }
     }
 }
