@@ -55,8 +55,8 @@ def measured_peaks():
 # accumulation; 96 B for the FP64 -> FP32 conversion).
 # Measured DRAM bytes per row and iteration of the loop graph (ncu, the graph as
 # one unit, beach_256x256x96): profiles/pcgpme_loop_dram_beach_256x256x96.md.
-TRAFFIC_ROW_ITER_FP64 = 477.6
-TRAFFIC_ROW_ITER_MIXED = 256.3
+TRAFFIC_ROW_ITER_FP64 = 448.8
+TRAFFIC_ROW_ITER_MIXED = 251.6
 
 
 def bytes_solve_fp64(n: int, iters: int) -> float:
