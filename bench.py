@@ -360,6 +360,85 @@ def run_will(args):
     print(json.dumps(line), flush=True)
 
 
+def run_ingest(args):
+    """Real-case ingestion: the workload written in the reference's case-file
+    format (sparse .xyzn and dense .xyz forms) to a scratch directory, then
+    timed from files to converged pressure -- read_case on the host, upload,
+    classification, coefficients, rows, assembly and the FP64 solve on the
+    device, the pressure read back.  Checks that the system built from the
+    files equals the one built from the generator bit for bit.  The host leg
+    runs the same files through the oracle (16-thread PCGPME).  One JSON line."""
+    import shutil
+    import tempfile
+    import torch
+    pkg = ge.load_package()
+    pkg.build()
+    case = workload_case(pkg, args.workload)
+    tmp = tempfile.mkdtemp(prefix="clowns_case_")
+    try:
+        out = {}
+        for form in ("sparse", "dense"):
+            prefix = os.path.join(tmp, f"{args.workload}_{form}")
+            paths = pkg.ingest.write_case(prefix, case, sparse=(form == "sparse"))
+            nbytes = sum(os.path.getsize(v) for v in paths.values())
+            times = []
+            for _ in range(max(1, args.steps)):
+                t0 = time.perf_counter()
+                got = pkg.ingest.read_case(prefix, eps0=case.eps0)
+                times.append(time.perf_counter() - t0)
+            t_read = statistics.median(times)
+            out[form] = {"file_mb": nbytes / 1e6, "read_s": t_read, "read_mb_per_s": nbytes / 1e6 / t_read,
+                         "prefix": prefix}
+        prefix = out["sparse"].pop("prefix")
+        out["dense"].pop("prefix")
+        # parity: the system from the files against the system from the generator
+        got = pkg.ingest.read_case(prefix, eps0=case.eps0).case
+        dc0, ds0 = pkg.prepare_dev(case)
+        dc1, ds1 = pkg.prepare_dev(got)
+        torch.cuda.synchronize()
+        same = (ds0.mnoe == ds1.mnoe and torch.equal(ds0.alu, ds1.alu) and torch.equal(ds0.llu, ds1.llu)
+                and torch.equal(ds0.de, ds1.de) and torch.equal(ds0.b, ds1.b))
+        n = ds1.mnoe
+        solver = pkg.Solver(n)
+
+        def files_to_pressure():
+            c = pkg.ingest.read_case(prefix, eps0=case.eps0).case
+            dc, ds = pkg.prepare_dev(c)
+            x = torch.zeros(ds.mm2, dtype=torch.float64, device="cuda")
+            info = solver.solve(ds.alu, ds.llu, ds.de, ds.b, x, eps=case.eps0)
+            return info, x[:ds.mnoe].cpu().numpy()
+
+        for _ in range(max(1, args.warmup)):
+            files_to_pressure()
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        for _ in range(args.steps):
+            info, xg = files_to_pressure()
+        torch.cuda.synchronize()
+        t_e2e = (time.perf_counter() - t0) / args.steps
+        line = {"metric": "case files to converged pressure per second", "unit": "cases/s",
+                "workload": args.workload, "rows": n, "cells": int(case.inne2),
+                "value": 1.0 / t_e2e, "s_per_case": t_e2e, "iters": info.iter, "tol": case.eps0,
+                "files": out, "system_from_files_equals_generated": bool(same)}
+        if not args.no_cpu:
+            ora = ge.load_oracle()
+            ora.build()
+            threads = os.cpu_count() or 1
+            t0 = time.perf_counter()
+            c = pkg.ingest.read_case(prefix, eps0=case.eps0).case
+            cls, sm, sy = ora.prepare(c)
+            ref = ora.pcgpme(sy.alu, sy.llu, sy.de[1:], sy.b[1:], sy.mnoe, eps=case.eps0, nthreads=threads)
+            t_cpu = time.perf_counter() - t0
+            line["rel_l2_vs_oracle"] = float(np.linalg.norm(xg - ref.x) / np.linalg.norm(ref.x))
+            line["cpu_baseline"] = {"value": 1.0 / t_cpu, "unit": "cases/s", "cores": threads, "kind": "port",
+                                    "cpu_model": cpu_model(),
+                                    "sample": "one case: read_case, the oracle's set_nflag, init_matrix, rows, "
+                                              f"assembly and PCGPME on {threads} threads"}
+        print(json.dumps(line), flush=True)
+    finally:
+        shutil.rmtree(tmp, ignore_errors=True)
+
+
 def run_session(args):
     """The whole pressure-correction ik loop of one time step on the device
     (clowns_session_pressure_loop: row numbering, RHS and dmax, assembly, PCGPME,
@@ -678,6 +757,7 @@ def main():
     ap.add_argument("--adjoint", action="store_true", help="adjoint vs finite differences instead")
     ap.add_argument("--will", action="store_true", help="PCGPME_WILL (2DH dispersion solve) instead")
     ap.add_argument("--session", action="store_true", help="the whole ik loop on the device instead")
+    ap.add_argument("--ingest", action="store_true", help="case files to converged pressure instead")
     ap.add_argument("--will-grid", default="1600x1200", help="2DH plan grid of the --will leg")
     ap.add_argument("--faces", type=int, default=200)
     ap.add_argument("--workload", default=WORKLOAD,
@@ -704,6 +784,11 @@ def main():
         import torch
         torch.cuda.set_device(local)
         run_session(args)
+        return
+    if args.ingest:
+        import torch
+        torch.cuda.set_device(local)
+        run_ingest(args)
         return
     if args.impl == "reference":
         run_reference(args, world, rank)
