@@ -391,9 +391,12 @@ def run_ingest(args):
                          "prefix": prefix}
         prefix = out["sparse"].pop("prefix")
         out["dense"].pop("prefix")
-        # parity: the system from the files against the system from the generator
+        # parity: the system from the files against the system from the generator, whose spacings get
+        # the rounding the reference's reader applies (set_dx, 1sub-main.F90:53-74)
         got = pkg.ingest.read_case(prefix, eps0=case.eps0).case
-        dc0, ds0 = pkg.prepare_dev(case)
+        gen = case.copy()
+        gen.x, gen.dx = pkg.ingest.set_dx(gen.dims, gen.x)
+        dc0, ds0 = pkg.prepare_dev(gen)
         dc1, ds1 = pkg.prepare_dev(got)
         torch.cuda.synchronize()
         same = (ds0.mnoe == ds1.mnoe and torch.equal(ds0.alu, ds1.alu) and torch.equal(ds0.llu, ds1.llu)
@@ -419,7 +422,9 @@ def run_ingest(args):
         line = {"metric": "case files to converged pressure per second", "unit": "cases/s",
                 "workload": args.workload, "rows": n, "cells": int(case.inne2),
                 "value": 1.0 / t_e2e, "s_per_case": t_e2e, "iters": info.iter, "tol": case.eps0,
-                "files": out, "system_from_files_equals_generated": bool(same)}
+                "files": out, "system_from_files_equals_generated": bool(same),
+                "note": "the reader rounds grid spacings as the reference does (set_dx); the generated case "
+                        "is compared after the same rounding"}
         if not args.no_cpu:
             ora = ge.load_oracle()
             ora.build()

@@ -260,3 +260,21 @@ def test_reader_rejects_bad_files(ing, pkg, tmp_path):
     (tmp_path / "e.xyzn").write_bytes(xyz.read_bytes())
     with pytest.raises(ing.FormatError):
         ing.read_case(tmp_path / "e")
+
+
+def test_reader_rounds_spacings_like_the_reference(ing, ora, pkg, tmp_path):
+    """A spacing of 0.8/24 is rounded to 0.033333 by set_dx (6 decimals for a
+    0.0333 first cell): the case read from files equals the generated one
+    after the same rounding, down to the assembled system."""
+    c = pkg.workload.make_case(20, 16, 24, dz=0.8 / 24, slope=0.5, n_obstacles=2, seed=6)
+    ing.write_case(tmp_path / "c", c, sparse=True)
+    r = ing.read_case(tmp_path / "c", eps0=c.eps0).case
+    x2, dx2 = ing.set_dx(c.dims, c.x)
+    assert np.array_equal(r.dx, dx2) and not np.array_equal(r.dx, c.dx)
+    assert r.dx[3, 2] == 0.033333
+    gen = c.copy()
+    gen.x, gen.dx = x2, dx2
+    _, _, s0 = ora.prepare(gen)
+    _, _, s1 = ora.prepare(r)
+    assert np.array_equal(s0.alu.view(np.int64), s1.alu.view(np.int64))
+    assert np.array_equal(s0.b.view(np.int64), s1.b.view(np.int64))
