@@ -24,6 +24,7 @@ import pathlib
 import statistics
 import subprocess
 import sys
+import tempfile
 import time
 
 import numpy as np
@@ -83,7 +84,7 @@ class Clocks:
     def __init__(self, gpu_index: int):
         self.proc = None
         self.gpu_index = gpu_index
-        self.path = ROOT / "gpurun_out" / f"clocks_{os.getpid()}.csv"
+        self.path = pathlib.Path(tempfile.gettempdir()) / f"clowns_clocks_{os.getpid()}.csv"
 
     def start(self):
         try:
