@@ -178,3 +178,32 @@ def test_batched_member_fault_is_isolated(gpu, systems):
             else:
                 assert info.ier == 0 and info.eps <= 1e-10, (k, info.as_dict())
     torch.cuda.synchronize()
+
+
+@pytest.mark.parametrize("balanced", ["4", "8"])
+def test_balanced_kernels_multi_step_ranges(gpu, ora, pkg, monkeypatch, balanced):
+    """A 1.1 M-row beach, where the one-wave grid (at most 608 blocks of 256
+    threads) is far smaller than the tile count and every thread walks more
+    than one step of its block's uneven row range: FP64 pressure within 1e-10
+    relative L2 of the oracle's (both to 1e-13), iterations within 25 %, and
+    the graph's forced fused and single sweeps bit-identical."""
+    import os
+    case = pkg.workload.beach_192x192x64()
+    cls, sm, sy = ora.prepare(case)
+    dc, ds = gpu.prepare_dev(case)
+    n = ds.mnoe
+    assert n > 608 * 256 * 4                        # more than one step of 4 rows per thread
+    ref = ora.pcgpme(sy.alu, sy.llu, sy.de[1:], sy.b[1:], n, eps=1e-13, nthreads=os.cpu_count() or 1)
+    monkeypatch.setenv("CLOWNS_LOOP_MODE", "graph")
+    monkeypatch.setenv("CLOWNS_BALANCED_ROWS", balanced)
+    out = []
+    for fuse in ("0", "1"):
+        monkeypatch.setenv("CLOWNS_SWEEP_FUSE", fuse)
+        x = _x(ds)
+        info = gpu.Solver(n).solve(ds.alu, ds.llu, ds.de, ds.b, x, eps=1e-13)
+        assert info.ier == 0, info.as_dict()
+        out.append((info.iter, x.cpu().numpy()[:n].copy()))
+    assert out[0][0] == out[1][0] and np.array_equal(out[0][1], out[1][1])
+    xg = out[0][1]
+    assert np.linalg.norm(xg - ref.x) <= 1e-10 * np.linalg.norm(ref.x)
+    assert abs(out[0][0] - ref.iters) <= max(5, ref.iters // 4), (out[0][0], ref.iters)
