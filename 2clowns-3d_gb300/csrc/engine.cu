@@ -237,6 +237,7 @@ struct EngLayout {
     size_t o_blk_group, o_grp_blk0, o_grp_nblk, o_mem_grp0, o_mem_ngrp, o_gticket, o_gpartials;
     size_t o_in, o_S, o_partials, o_bar, o_al, o_ll, o_d, o_vec[8], o_W, o_x64, o_r64, o_s64, o_t64;
     size_t o_wave, o_wbuf[kWaveBufs];
+    size_t o_baltab = 0;   // ensembles: block tables of the balanced kernels
     size_t total = 0;
 };
 
@@ -299,6 +300,7 @@ static EngLayout eng_layout(int M, const int* n, int mixed, int wave = -1) {
         L.o_wave = 0;
         for (int k = 0; k < kWaveBufs; k++) L.o_wbuf[k] = 0;
     }
+    if (M > 1) L.o_baltab = take(sizeof(BalBlock) * 16 * (size_t)kBalTabMax);
     L.total = o;
     return L;
 }
@@ -346,6 +348,7 @@ static Eng<T> eng_bind(void* work, const EngLayout& L) {
     }
     E.wave = L.wave ? (WaveCtl*)(b + L.o_wave) : nullptr;
     for (int k = 0; k < kWaveBufs; k++) E.w[k] = L.wave ? (T*)(b + L.o_wbuf[k]) : nullptr;
+    E.baltab = nullptr;       // set once the tables are uploaded (upload_bal_tables)
     return E;
 }
 
@@ -602,35 +605,87 @@ static void prepare_bal(int bal) {
     else if (bal) bal_grids<T, 4>();
 }
 
+// Kernel kinds of the balanced iteration, in the order of BalGrids and of the
+// ensembles' block tables (table of rows-per-thread R and kind k at index
+// (R == 8 ? 8 : 0) + k).
+enum BalKind { kBalAx, kBalSw, kBalS2, kBalR1, kBalR2, kBalEu, kBalXr, kBalPu, kBalKinds };
+
+static int bal_grid_of(const BalGrids& g, int kind) {
+    const int v[kBalKinds] = {g.ax, g.sw, g.s2, g.r1, g.r2, g.eu, g.xr, g.pu};
+    return v[kind];
+}
+
+// Ensembles: split each balanced launch's blocks over the members in
+// proportion to their rows, one block at least each -- member m takes blocks
+// [C_m, C_m+1) with C_m = m + floor((G - M) rows_before_m / rows_total) -- and
+// upload the 16 tables (both rows-per-thread settings, every kernel kind).
+// *ok is false (nothing uploaded) when a launch has fewer blocks than members.
+template <typename T>
+static int upload_bal_tables(void* work, const EngLayout& L, const int* n, cudaStream_t s, bool* ok) {
+    *ok = false;
+    const int M = L.M;
+    if (M <= 1 || !L.o_baltab) return CLOWNS_OK;
+    long total = 0;
+    for (int m = 0; m < M; m++) total += n[m];
+    std::vector<BalBlock> tab(16 * (size_t)kBalTabMax, BalBlock{0, 0, 1, 0});
+    for (int ri = 0; ri < 2; ri++) {
+        const BalGrids& g = ri ? bal_grids<T, 8>() : bal_grids<T, 4>();
+        for (int k = 0; k < kBalKinds; k++) {
+            const int G = std::min(bal_grid_of(g, k), L.nblk);
+            if (G < M || G > kBalTabMax) return CLOWNS_OK;
+            BalBlock* t = tab.data() + (size_t)(ri * 8 + k) * kBalTabMax;
+            long before = 0;
+            for (int m = 0; m < M; m++) {
+                const int c0 = m + (int)((long)(G - M) * before / std::max(total, 1L));
+                before += n[m];
+                const int c1 = m + 1 + (int)((long)(G - M) * before / std::max(total, 1L));
+                for (int b = c0; b < c1; b++) t[b] = BalBlock{m, b - c0, c1 - c0, c0};
+            }
+        }
+    }
+    CLOWNS_CUDA_TRY(cudaMemcpyAsync((char*)work + L.o_baltab, tab.data(), sizeof(BalBlock) * tab.size(),
+                                    cudaMemcpyHostToDevice, s));
+    CLOWNS_CUDA_TRY(cudaStreamSynchronize(s));
+    *ok = true;
+    return CLOWNS_OK;
+}
+
 template <typename T, int R>
 static void g_iteration_bal(bool pdl, const Eng<T>& E, const Shape& sh, cudaStream_t s) {
     const int B = kEngBlock, n = E.nblk;
     const BalGrids& G = bal_grids<T, R>();
-    const int g_ax = G.ax, g_sw = G.sw, g_s2 = G.s2, g_r1 = G.r1, g_r2 = G.r2, g_eu = G.eu, g_xr = G.xr, g_pu = G.pu;
-    auto apply = [&](const T* in, T* out, int mode) {
-        klaunch(pdl, k_bal_axsub<T, R>, std::min(g_ax, n), B, s, E, in, E.t);
-        if (sh.fuse) {
-            klaunch(pdl, k_bal_sweep2<T, R>, std::min(g_s2, n), B, s, E, 0, (const T*)E.t, out);
-            klaunch(pdl, k_bal_sweep2<T, R>, std::min(g_s2, n), B, s, E, 2, (const T*)out, E.t);
-        } else {
-            klaunch(pdl, k_bal_sweep<T, R>, std::min(g_sw, n), B, s, E, 0, (const T*)E.t, out);
-            klaunch(pdl, k_bal_sweep<T, R>, std::min(g_sw, n), B, s, E, 1, (const T*)out, E.t);
-            klaunch(pdl, k_bal_sweep<T, R>, std::min(g_sw, n), B, s, E, 2, (const T*)E.t, out);
-            klaunch(pdl, k_bal_sweep<T, R>, std::min(g_sw, n), B, s, E, 3, (const T*)out, E.t);
-        }
-        if (mode == 1) klaunch(pdl, k_bal_sweep56<T, 1, R>, std::min(g_r1, n), B, s, E, (const T*)E.t, out);
-        else klaunch(pdl, k_bal_sweep56<T, 2, R>, std::min(g_r2, n), B, s, E, (const T*)E.t, out);
+    auto grid = [&](int k) { return std::min(bal_grid_of(G, k), n); };
+    auto tab = [&](int k) -> const BalBlock* {
+        return E.M == 1 ? nullptr : E.baltab + (size_t)((R == 8 ? 8 : 0) + k) * kBalTabMax;
     };
-    apply((const T*)E.p, E.q, 1);                                        // q = PM A p ; RQ ; ALP
-    klaunch(pdl, k_bal_eupdate<T, R>, std::min(g_eu, n), B, s, E);      // e = r - ALP q
-    apply((const T*)E.e, E.v, 2);                                        // v = PM A e ; AMU
-    klaunch(pdl, k_bal_xrupdate<T, R>, std::min(g_xr, n), B, s, E);     // x, r ; RN, C1 ; stop tests
-    klaunch(pdl, k_bal_pupdate<T, R>, std::min(g_pu, n), B, s, E);      // p
+    auto apply = [&](const T* in, T* out, int mode) {
+        klaunch(pdl, k_bal_axsub<T, R>, grid(kBalAx), B, s, E, tab(kBalAx), in, E.t);
+        if (sh.fuse) {
+            klaunch(pdl, k_bal_sweep2<T, R>, grid(kBalS2), B, s, E, tab(kBalS2), 0, (const T*)E.t, out);
+            klaunch(pdl, k_bal_sweep2<T, R>, grid(kBalS2), B, s, E, tab(kBalS2), 2, (const T*)out, E.t);
+        } else {
+            klaunch(pdl, k_bal_sweep<T, R>, grid(kBalSw), B, s, E, tab(kBalSw), 0, (const T*)E.t, out);
+            klaunch(pdl, k_bal_sweep<T, R>, grid(kBalSw), B, s, E, tab(kBalSw), 1, (const T*)out, E.t);
+            klaunch(pdl, k_bal_sweep<T, R>, grid(kBalSw), B, s, E, tab(kBalSw), 2, (const T*)E.t, out);
+            klaunch(pdl, k_bal_sweep<T, R>, grid(kBalSw), B, s, E, tab(kBalSw), 3, (const T*)out, E.t);
+        }
+        if (mode == 1) klaunch(pdl, k_bal_sweep56<T, 1, R>, grid(kBalR1), B, s, E, tab(kBalR1), (const T*)E.t, out);
+        else klaunch(pdl, k_bal_sweep56<T, 2, R>, grid(kBalR2), B, s, E, tab(kBalR2), (const T*)E.t, out);
+    };
+    apply((const T*)E.p, E.q, 1);                                                    // q = PM A p ; RQ ; ALP
+    klaunch(pdl, k_bal_eupdate<T, R>, grid(kBalEu), B, s, E, tab(kBalEu));          // e = r - ALP q
+    apply((const T*)E.e, E.v, 2);                                                    // v = PM A e ; AMU
+    klaunch(pdl, k_bal_xrupdate<T, R>, grid(kBalXr), B, s, E, tab(kBalXr));         // x, r ; RN, C1 ; stop tests
+    klaunch(pdl, k_bal_pupdate<T, R>, grid(kBalPu), B, s, E, tab(kBalPu));          // p
 }
+
+// Balanced kernels serve single systems, and ensembles whose tables are uploaded.
+template <typename T>
+static bool bal_usable(const Eng<T>& E) { return E.M == 1 || E.baltab != nullptr; }
 
 template <typename T>
 static void g_iteration(bool pdl, const Eng<T>& E, const Shape& sh, cudaStream_t s) {
-    if (sh.bal && E.M == 1) {
+    if (sh.bal && bal_usable(E)) {
         if (sh.bal == 8) g_iteration_bal<T, 8>(pdl, E, sh, s);
         else g_iteration_bal<T, 4>(pdl, E, sh, s);
         return;
@@ -842,7 +897,7 @@ static int tune_loop(Eng<T> E, const void* work, GridBar* gb, long key_nv, int k
         const char* rz = getenv("CLOWNS_REDUCE_BLOCK");   // forced executions: 128 unless "64"
         sh.rblock = (rz && !strcmp(rz, "64")) ? 64 : kStepBlock;
         const char* bz = getenv("CLOWNS_BALANCED_ROWS");  // forced executions: tile kernels unless 4 or 8
-        sh.bal = E.M != 1 || !bz ? 0 : !strcmp(bz, "8") ? 8 : !strcmp(bz, "4") ? 4 : 0;
+        sh.bal = !bal_usable(E) || !bz ? 0 : !strcmp(bz, "8") ? 8 : !strcmp(bz, "4") ? 4 : 0;
         *out = sh;
         return CLOWNS_OK;
     }
@@ -922,8 +977,8 @@ static int tune_loop(Eng<T> E, const void* work, GridBar* gb, long key_nv, int k
                 gsh.rblock = rb;
                 cands.push_back(gsh);
             }
-        // single systems: the balanced one-wave kernels, 4 or 8 rows per thread per step
-        if (E.M == 1)
+        // the balanced one-wave kernels, 4 or 8 rows per thread per step
+        if (bal_usable(E))
             for (int fuse : {1, 0})
                 for (int rows : {4, 8}) {
                     LoopShape gsh;
@@ -1096,6 +1151,10 @@ int engine_solve_plain(int M, const MemberIn* ins, double eps, double parm, int 
     rc = eng_upload_tables(work, L, n.data(), ins, s);
     if (rc) return rc;
     Eng<double> E = eng_bind<double>(work, L);
+    bool bal_ok = false;
+    rc = upload_bal_tables<double>(work, L, n.data(), s, &bal_ok);
+    if (rc) return rc;
+    if (bal_ok) E.baltab = (const BalBlock*)((const char*)work + L.o_baltab);
     GridBar* gb = (GridBar*)((char*)work + L.o_bar);
     const int gs = std::min(L.nblk * 2, kEngMaxGrid * 4);
     auto prime = [&](cudaStream_t cs, double e, int it) {
@@ -1160,6 +1219,10 @@ int engine_solve_mixed(int M, const MemberIn* ins, double eps, double parm, doub
     rc = eng_upload_tables(work, L, n.data(), ins, s);
     if (rc) return rc;
     Eng<float> E = eng_bind<float>(work, L);
+    bool bal_ok = false;
+    rc = upload_bal_tables<float>(work, L, n.data(), s, &bal_ok);
+    if (rc) return rc;
+    if (bal_ok) E.baltab = (const BalBlock*)((const char*)work + L.o_baltab);
     GridBar* gb = (GridBar*)((char*)work + L.o_bar);
     const int gs = std::min(L.nblk * 2, kEngMaxGrid * 4);
     const Shape ksh;                               // standalone FP64 refinement kernels

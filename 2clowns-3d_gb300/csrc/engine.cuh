@@ -68,6 +68,13 @@ struct MemberIn {
     int na, n, nl, pad;
 };
 
+// Block of a balanced launch: member m, index j among the member's gm blocks,
+// the member's first block b0.
+struct BalBlock {
+    int m, j, gm, b0;
+};
+constexpr int kBalTabMax = kNumSMs * 16;   // entries of one block table (one wave at most)
+
 template <typename T>
 struct Eng {
     long NV;                  // rows of the concatenated space (multiple of kTile)
@@ -102,6 +109,7 @@ struct Eng {
     double* partials;         // 2 per block
     unsigned* ticket;         // one per member
     int* ctrl;                // [0] loop-body count, [1] max ITER over members, [2] bodies of earlier sweeps
+    const BalBlock* baltab;   // ensembles: 16 block tables of the balanced kernels (nullptr: none)
 };
 
 // ---------------------------------------------------------------------------
@@ -833,19 +841,23 @@ __global__ void __launch_bounds__(kEngBlock) k_eng_initres(Eng<T> E) {
 }
 
 // ---------------------------------------------------------------------------
-// Balanced kernels (single systems).  The iteration's kernels can instead run
-// as exactly one wave each: G = (resident blocks per SM) x SMs blocks, block b
-// owning the rows [n b / G, n (b+1) / G) and walking them R rows per thread
-// per step.  Every block then does the same work and all retire together, and
+// Balanced kernels.  The iteration's kernels can instead run as exactly one
+// wave each: G = (resident blocks per SM) x SMs blocks, block b owning the
+// rows [n b / G, n (b+1) / G) and walking them R rows per thread per step.  An
+// ensemble splits the G blocks over its members in proportion to their rows,
+// at least one block each, by a table the host writes (BalBlock per block);
+// blocks of a stopped member return before loading anything.  Every block then does the same work and all retire together, and
 // the per-block costs -- launch, the stop-flag and scalar loads, the reduction
 // tail -- are paid G times per kernel instead of once per 512-row tile (5517
 // times at 2.8 M rows).  The per-row arithmetic is the tile kernels'; dot
 // products are reduced once per block: the block's partial goes to
-// partials[b], and the last block to finish sums the G partials in index order
-// (deterministic for a given G) and finalises the scalars.  Callers keep G at
-// most nblk (the partials hold two values per tile).
+// partials[b], and the last block of a member to finish sums the member's
+// partials in index order (deterministic for a given G) and finalises its
+// scalars.  Callers keep G at most nblk (the partials hold two values per
+// tile) and at least the number of members.
 //
-// Only the kernels whose results outlive a stop test read the stop flag:
+// For a single system only the kernels whose results outlive a stop test read
+// the stop flag:
 // sweep56 (its reduction and finalisation) and xrupdate (x, r and the stop
 // tests); after a stop the other kernels of the body write scratch vectors (t,
 // q, e, v, p) the finished solve no longer reads, and the loop guard ends the
@@ -854,18 +866,39 @@ __global__ void __launch_bounds__(kEngBlock) k_eng_initres(Eng<T> E) {
 // barrier; each thread loads them, and the load overlaps its data loads.)
 // FP64 kernels at 4 rows per thread are held to 85 registers (3 blocks per SM).
 
-__device__ __forceinline__ void bal_range(long n, long& lo, long& hi) {
-    lo = n * (long)blockIdx.x / (long)gridDim.x;
-    hi = n * (long)(blockIdx.x + 1) / (long)gridDim.x;
+// This block's member and rows.  tab == nullptr: a single system, every block
+// belongs to member 0.  Returns false for a block of an ensemble member that
+// has stopped.
+template <typename T>
+__device__ __forceinline__ bool bal_block(const Eng<T>& E, const BalBlock* __restrict__ tab, BalBlock& bb,
+                                          long& lo, long& hi) {
+    long off, n;
+    if (!tab) {
+        bb.m = 0;
+        bb.j = blockIdx.x;
+        bb.gm = gridDim.x;
+        bb.b0 = 0;
+        off = 0;
+        n = E.n1;
+    } else {
+        bb = tab[blockIdx.x];
+        off = E.mem_off[bb.m];
+        n = E.mem_n[bb.m];
+    }
+    lo = off + n * (long)bb.j / (long)bb.gm;
+    hi = off + n * (long)(bb.j + 1) / (long)bb.gm;
+    return !tab || !sld(&E.S[bb.m].done);
 }
 
 template <typename T, int R>
 constexpr int kBalMinBlocks = sizeof(T) == 8 && R == 4 ? 3 : 1;
 
-// Block partial of (v0, v1), then the last block sums all partials; true in
-// every thread of that block, with the totals in tot[] of warp 0.
+// Block partial of (v0, v1), then the last block of the member sums the
+// member's partials; true in every thread of that block, with the totals in
+// tot[] of warp 0.
 template <typename T, typename A>
-__device__ __forceinline__ bool bal_reduce(const Eng<T>& E, A v0, A v1, double* red, double (&tot)[2]) {
+__device__ __forceinline__ bool bal_reduce(const Eng<T>& E, const BalBlock& bb, A v0, A v1, double* red,
+                                           double (&tot)[2]) {
     __shared__ int s_last;
     const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5, nw = blockDim.x >> 5;
     const A w = warp_pair_sum(v0, v1);
@@ -879,15 +912,15 @@ __device__ __forceinline__ bool bal_reduce(const Eng<T>& E, A v0, A v1, double* 
         if (lane == 16) E.partials[2L * blockIdx.x + 1] = s;
         if (lane == 0 || lane == 16) __threadfence();
         __syncwarp();
-        if (lane == 0) s_last = atomicAdd(&E.ticket[0], 1u) == gridDim.x - 1u;
+        if (lane == 0) s_last = atomicAdd(&E.ticket[bb.m], 1u) == (unsigned)bb.gm - 1u;
     }
     __syncthreads();
     if (!s_last) return false;
     __threadfence();
     double a = 0.0, b = 0.0;
-    for (int q = threadIdx.x; q < (int)gridDim.x; q += blockDim.x) {
-        a += __ldcg(E.partials + 2L * q + 0);
-        b += __ldcg(E.partials + 2L * q + 1);
+    for (int q = threadIdx.x; q < bb.gm; q += blockDim.x) {
+        a += __ldcg(E.partials + 2L * (bb.b0 + q) + 0);
+        b += __ldcg(E.partials + 2L * (bb.b0 + q) + 1);
     }
     const double w2 = warp_pair_sum(a, b);
     __syncthreads();                          // every warp has read red[] above
@@ -905,11 +938,12 @@ __device__ __forceinline__ bool bal_reduce(const Eng<T>& E, A v0, A v1, double* 
 }
 
 template <typename T, int R>
-__global__ void __launch_bounds__(kEngBlock, kBalMinBlocks<T, R>) k_bal_axsub(Eng<T> E, const T* __restrict__ in, T* __restrict__ out) {
+__global__ void __launch_bounds__(kEngBlock, kBalMinBlocks<T, R>) k_bal_axsub(Eng<T> E, const BalBlock* __restrict__ tab, const T* __restrict__ in, T* __restrict__ out) {
     pdl_enter();
     const long NV = E.NV;
     long lo, hi;
-    bal_range(E.n1, lo, hi);
+    BalBlock bb;
+    if (!bal_block(E, tab, bb, lo, hi)) return;
     for (long base = lo + threadIdx.x; base < hi; base += (long)blockDim.x * R) {
         T s[R];
         bool ok[R];
@@ -940,14 +974,15 @@ __global__ void __launch_bounds__(kEngBlock, kBalMinBlocks<T, R>) k_bal_axsub(En
 }
 
 template <typename T, int R>
-__global__ void __launch_bounds__(kEngBlock, kBalMinBlocks<T, R>) k_bal_sweep(Eng<T> E, int k, const T* __restrict__ in,
+__global__ void __launch_bounds__(kEngBlock, kBalMinBlocks<T, R>) k_bal_sweep(Eng<T> E, const BalBlock* __restrict__ tab, int k, const T* __restrict__ in,
                                                         T* __restrict__ out) {
     pdl_enter();
     const long NV = E.NV;
     const T* __restrict__ a = E.al + k * NV;
     const int* __restrict__ c = E.ll + k * NV;
     long lo, hi;
-    bal_range(E.n1, lo, hi);
+    BalBlock bb;
+    if (!bal_block(E, tab, bb, lo, hi)) return;
     for (long base = lo + threadIdx.x; base < hi; base += (long)blockDim.x * R) {
         T av[R], xv[R], gv[R];
         int cv[R];
@@ -971,7 +1006,7 @@ __global__ void __launch_bounds__(kEngBlock, kBalMinBlocks<T, R>) k_bal_sweep(En
 
 // the fused pair of sweeps k, k+1 (as tl_sweep2)
 template <typename T, int R>
-__global__ void __launch_bounds__(kEngBlock, kBalMinBlocks<T, R>) k_bal_sweep2(Eng<T> E, int k, const T* __restrict__ in,
+__global__ void __launch_bounds__(kEngBlock, kBalMinBlocks<T, R>) k_bal_sweep2(Eng<T> E, const BalBlock* __restrict__ tab, int k, const T* __restrict__ in,
                                                          T* __restrict__ out) {
     pdl_enter();
     const long NV = E.NV;
@@ -980,7 +1015,8 @@ __global__ void __launch_bounds__(kEngBlock, kBalMinBlocks<T, R>) k_bal_sweep2(E
     const T* __restrict__ a1 = a0 + NV;
     const int* __restrict__ c1 = c0 + NV;
     long lo, hi;
-    bal_range(E.n1, lo, hi);
+    BalBlock bb;
+    if (!bal_block(E, tab, bb, lo, hi)) return;
     for (long base = lo + threadIdx.x; base < hi; base += (long)blockDim.x * R) {
         T x[R], aa[R], ab[R], xj[R], aj[R];
         int ca[R], cb[R], cj[R];
@@ -1016,7 +1052,7 @@ __global__ void __launch_bounds__(kEngBlock, kBalMinBlocks<T, R>) k_bal_sweep2(E
 
 // sweeps 5, 6 with the RQ (MODE 1) or AMU (MODE 2) reduction (as tl_sweep56)
 template <typename T, int MODE, int R>
-__global__ void __launch_bounds__(kEngBlock, kBalMinBlocks<T, R>) k_bal_sweep56(Eng<T> E, const T* __restrict__ in, T* __restrict__ out) {
+__global__ void __launch_bounds__(kEngBlock, kBalMinBlocks<T, R>) k_bal_sweep56(Eng<T> E, const BalBlock* __restrict__ tab, const T* __restrict__ in, T* __restrict__ out) {
     pdl_enter();
     __shared__ double red[64];
     const long NV = E.NV;
@@ -1024,10 +1060,11 @@ __global__ void __launch_bounds__(kEngBlock, kBalMinBlocks<T, R>) k_bal_sweep56(
     const T* __restrict__ a6 = E.al + 5 * NV;
     const int* __restrict__ c5 = E.ll + 4 * NV;
     const int* __restrict__ c6 = E.ll + 5 * NV;
-    const int done = sld(&E.S[0].done);
-    T acc0 = T(0), acc1 = T(0);
     long lo, hi;
-    bal_range(E.n1, lo, hi);
+    BalBlock bb;
+    if (!bal_block(E, tab, bb, lo, hi)) return;
+    const int done = sld(&E.S[bb.m].done);
+    T acc0 = T(0), acc1 = T(0);
     for (long base = lo + threadIdx.x; base < hi; base += (long)blockDim.x * R) {
         T a5v[R], a6v[R], xv[R], g5[R], g6[R];
         int c5v[R], c6v[R];
@@ -1060,20 +1097,21 @@ __global__ void __launch_bounds__(kEngBlock, kBalMinBlocks<T, R>) k_bal_sweep56(
     }
     if (MODE == 0 || done) return;
     double tot[2];
-    if (!bal_reduce(E, acc0, acc1, red, tot)) return;
+    if (!bal_reduce(E, bb, acc0, acc1, red, tot)) return;
     if (threadIdx.x == 0) {
-        E.ticket[0] = 0;
-        finish_sweep56<MODE>(E.S, tot);
+        E.ticket[bb.m] = 0;
+        finish_sweep56<MODE>(E.S + bb.m, tot);
         __threadfence();
     }
 }
 
 template <typename T, int R>
-__global__ void __launch_bounds__(kEngBlock, kBalMinBlocks<T, R>) k_bal_eupdate(Eng<T> E) {
+__global__ void __launch_bounds__(kEngBlock, kBalMinBlocks<T, R>) k_bal_eupdate(Eng<T> E, const BalBlock* __restrict__ tab) {
     pdl_enter();
-    const T ALP = T(sld(&E.S[0].ALP));
     long lo, hi;
-    bal_range(E.n1, lo, hi);
+    BalBlock bb;
+    if (!bal_block(E, tab, bb, lo, hi)) return;
+    const T ALP = T(sld(&E.S[bb.m].ALP));
     for (long base = lo + threadIdx.x; base < hi; base += (long)blockDim.x * R) {
         T rv[R], qv[R];
 #pragma unroll
@@ -1092,14 +1130,15 @@ __global__ void __launch_bounds__(kEngBlock, kBalMinBlocks<T, R>) k_bal_eupdate(
 }
 
 template <typename T, int R>
-__global__ void __launch_bounds__(kEngBlock, kBalMinBlocks<T, R>) k_bal_xrupdate(Eng<T> E) {
+__global__ void __launch_bounds__(kEngBlock, kBalMinBlocks<T, R>) k_bal_xrupdate(Eng<T> E, const BalBlock* __restrict__ tab) {
     pdl_enter();
     __shared__ double red[64];
-    const int done = sld(&E.S[0].done);
-    const T ALP = T(sld(&E.S[0].ALP)), AMU = T(sld(&E.S[0].AMU));
-    T acc0 = T(0), acc1 = T(0);
     long lo, hi;
-    bal_range(E.n1, lo, hi);
+    BalBlock bb;
+    if (!bal_block(E, tab, bb, lo, hi)) return;
+    const int done = sld(&E.S[bb.m].done);
+    const T ALP = T(sld(&E.S[bb.m].ALP)), AMU = T(sld(&E.S[bb.m].AMU));
+    T acc0 = T(0), acc1 = T(0);
     for (long base = lo + threadIdx.x; base < hi; base += (long)blockDim.x * R) {
         T ev[R], xv[R], pv[R], vv[R], r0v[R];
 #pragma unroll
@@ -1125,20 +1164,21 @@ __global__ void __launch_bounds__(kEngBlock, kBalMinBlocks<T, R>) k_bal_xrupdate
     }
     if (done) return;
     double tot[2];
-    if (!bal_reduce(E, acc0, acc1, red, tot)) return;
+    if (!bal_reduce(E, bb, acc0, acc1, red, tot)) return;
     if (threadIdx.x == 0) {
-        E.ticket[0] = 0;
-        finish_xrupdate(E.S, tot);
+        E.ticket[bb.m] = 0;
+        finish_xrupdate(E.S + bb.m, tot);
         __threadfence();
     }
 }
 
 template <typename T, int R>
-__global__ void __launch_bounds__(kEngBlock, kBalMinBlocks<T, R>) k_bal_pupdate(Eng<T> E) {
+__global__ void __launch_bounds__(kEngBlock, kBalMinBlocks<T, R>) k_bal_pupdate(Eng<T> E, const BalBlock* __restrict__ tab) {
     pdl_enter();
-    const T BETA = T(sld(&E.S[0].BETA)), AMU = T(sld(&E.S[0].AMU));
     long lo, hi;
-    bal_range(E.n1, lo, hi);
+    BalBlock bb;
+    if (!bal_block(E, tab, bb, lo, hi)) return;
+    const T BETA = T(sld(&E.S[bb.m].BETA)), AMU = T(sld(&E.S[bb.m].AMU));
     for (long base = lo + threadIdx.x; base < hi; base += (long)blockDim.x * R) {
         T rv[R], pv[R], qv[R];
 #pragma unroll

@@ -126,8 +126,18 @@ def test_mixed_true_residual(gpu, ora, systems):
     assert np.linalg.norm(b - A @ xg) <= 1e-10 * np.linalg.norm(b)
 
 
-def test_batched_fp64_matches_single(gpu, systems):
+def _force_balanced(monkeypatch, balanced):
+    """"auto": the autotuner decides; "0", "4", "8": the graph loop with the tile
+    kernels or the balanced kernels at 4 or 8 rows per thread."""
+    if balanced != "auto":
+        monkeypatch.setenv("CLOWNS_LOOP_MODE", "graph")
+        monkeypatch.setenv("CLOWNS_BALANCED_ROWS", balanced)
+
+
+@pytest.mark.parametrize("balanced", ["auto", "0", "4", "8"])
+def test_batched_fp64_matches_single(gpu, systems, monkeypatch, balanced):
     import torch
+    _force_balanced(monkeypatch, balanced)
     sys_list = [(ds.alu, ds.llu, ds.de, ds.b) for (_, _, _, ds) in systems]
     sizes = [ds.mnoe for (_, _, _, ds) in systems]
     xs = [_x(ds) for (_, _, _, ds) in systems]
@@ -143,7 +153,9 @@ def test_batched_fp64_matches_single(gpu, systems):
     torch.cuda.synchronize()
 
 
-def test_batched_mixed_converges_per_member(gpu, ora, systems):
+@pytest.mark.parametrize("balanced", ["auto", "4", "8"])
+def test_batched_mixed_converges_per_member(gpu, ora, systems, monkeypatch, balanced):
+    _force_balanced(monkeypatch, balanced)
     sys_list = [(ds.alu, ds.llu, ds.de, ds.b) for (_, _, _, ds) in systems]
     sizes = [ds.mnoe for (_, _, _, ds) in systems]
     xs = [_x(ds) for (_, _, _, ds) in systems]
@@ -159,9 +171,12 @@ def test_batched_mixed_converges_per_member(gpu, ora, systems):
         assert np.linalg.norm(xg - xd) / nd <= max(1e-9, 2 * err_oracle), label
 
 
-def test_batched_member_fault_is_isolated(gpu, systems):
-    """A NaN right-hand side (injected on the host) stops only its own member."""
+@pytest.mark.parametrize("balanced", ["auto", "4", "8"])
+def test_batched_member_fault_is_isolated(gpu, systems, monkeypatch, balanced):
+    """A NaN right-hand side (injected on the host) stops only its own member,
+    with the tile kernels and with the balanced kernels' block tables."""
     import torch
+    _force_balanced(monkeypatch, balanced)
     sys_list = []
     for k, (_, _, _, ds) in enumerate(systems):
         b = ds.b.clone()
