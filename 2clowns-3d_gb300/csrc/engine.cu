@@ -238,6 +238,7 @@ struct EngLayout {
     size_t o_in, o_S, o_partials, o_bar, o_al, o_ll, o_d, o_vec[8], o_W, o_x64, o_r64, o_s64, o_t64;
     size_t o_wave, o_wbuf[kWaveBufs];
     size_t o_baltab = 0;   // ensembles: block tables of the balanced kernels
+    size_t o_balg = 0;     // ensembles: blocks of each table's launch
     size_t total = 0;
 };
 
@@ -300,7 +301,10 @@ static EngLayout eng_layout(int M, const int* n, int mixed, int wave = -1) {
         L.o_wave = 0;
         for (int k = 0; k < kWaveBufs; k++) L.o_wbuf[k] = 0;
     }
-    if (M > 1) L.o_baltab = take(sizeof(BalBlock) * 16 * (size_t)kBalTabMax);
+    if (M > 1) {
+        L.o_baltab = take(sizeof(BalBlock) * 16 * (size_t)kBalTabMax);
+        L.o_balg = take(sizeof(int) * 16);
+    }
     L.total = o;
     return L;
 }
@@ -348,7 +352,8 @@ static Eng<T> eng_bind(void* work, const EngLayout& L) {
     }
     E.wave = L.wave ? (WaveCtl*)(b + L.o_wave) : nullptr;
     for (int k = 0; k < kWaveBufs; k++) E.w[k] = L.wave ? (T*)(b + L.o_wbuf[k]) : nullptr;
-    E.baltab = nullptr;       // set once the tables are uploaded (upload_bal_tables)
+    E.baltab = nullptr;       // set once the launch sizes are uploaded (upload_bal_tables)
+    E.balg = L.o_balg ? (const int*)(b + L.o_balg) : nullptr;
     return E;
 }
 
@@ -615,36 +620,27 @@ static int bal_grid_of(const BalGrids& g, int kind) {
     return v[kind];
 }
 
-// Ensembles: split each balanced launch's blocks over the members in
-// proportion to their rows, one block at least each -- member m takes blocks
-// [C_m, C_m+1) with C_m = m + floor((G - M) rows_before_m / rows_total) -- and
-// upload the 16 tables (both rows-per-thread settings, every kernel kind).
-// *ok is false (nothing uploaded) when a launch has fewer blocks than members.
+// Ensembles: the blocks of each balanced launch (both rows-per-thread settings,
+// every kernel kind), which the block tables are built for on the device
+// (bal_rebuild: before each loop, and by the loop guard whenever members
+// stop).  *ok is false (nothing uploaded) when a launch has fewer blocks than
+// members: the ensemble then keeps the tile kernels.
 template <typename T>
 static int upload_bal_tables(void* work, const EngLayout& L, const int* n, cudaStream_t s, bool* ok) {
+    (void)n;
     *ok = false;
     const int M = L.M;
     if (M <= 1 || !L.o_baltab) return CLOWNS_OK;
-    long total = 0;
-    for (int m = 0; m < M; m++) total += n[m];
-    std::vector<BalBlock> tab(16 * (size_t)kBalTabMax, BalBlock{0, 0, 1, 0});
+    int g16[16];
     for (int ri = 0; ri < 2; ri++) {
         const BalGrids& g = ri ? bal_grids<T, 8>() : bal_grids<T, 4>();
         for (int k = 0; k < kBalKinds; k++) {
             const int G = std::min(bal_grid_of(g, k), L.nblk);
             if (G < M || G > kBalTabMax) return CLOWNS_OK;
-            BalBlock* t = tab.data() + (size_t)(ri * 8 + k) * kBalTabMax;
-            long before = 0;
-            for (int m = 0; m < M; m++) {
-                const int c0 = m + (int)((long)(G - M) * before / std::max(total, 1L));
-                before += n[m];
-                const int c1 = m + 1 + (int)((long)(G - M) * before / std::max(total, 1L));
-                for (int b = c0; b < c1; b++) t[b] = BalBlock{m, b - c0, c1 - c0, c0};
-            }
+            g16[ri * 8 + k] = G;
         }
     }
-    CLOWNS_CUDA_TRY(cudaMemcpyAsync((char*)work + L.o_baltab, tab.data(), sizeof(BalBlock) * tab.size(),
-                                    cudaMemcpyHostToDevice, s));
+    CLOWNS_CUDA_TRY(cudaMemcpyAsync((char*)work + L.o_balg, g16, sizeof(g16), cudaMemcpyHostToDevice, s));
     CLOWNS_CUDA_TRY(cudaStreamSynchronize(s));
     *ok = true;
     return CLOWNS_OK;
@@ -752,7 +748,8 @@ static int build_loop_graph(const Eng<T>& E, bool pdl, int fuse, int rblock, int
     sh.rblock = rblock;
     sh.bal = bal;
     g_iteration(pdl, E, sh, g_cap);
-    klaunch(pdl, k_eng_guard, 1, 256, g_cap, E.S, E.M, E.ctrl, h);
+    BalBlock* tabs = bal && E.M > 1 && E.baltab ? (BalBlock*)E.baltab : nullptr;
+    klaunch(pdl, k_eng_guard, 1, 256, g_cap, E.S, E.M, E.ctrl, h, (const int*)E.mem_n, tabs, E.balg);
     cudaGraph_t captured;
     cudaError_t ec = cudaStreamEndCapture(g_cap, &captured);
     if (ec != cudaSuccess) {
@@ -809,6 +806,12 @@ static long loop_launches(const LoopShape& sh, long bodies) {
 
 template <typename T>
 static int run_loop(Eng<T> E, const void* work, GridBar* gb, int prec, const LoopShape& sh, cudaStream_t s) {
+    if (sh.bal && E.M > 1 && E.baltab && (sh.graph == 1 || sh.graph == 2)) {
+        // ensembles on the balanced kernels: block tables over the members that iterate
+        k_bal_rebuild<<<1, kBalScanThreads, 0, s>>>(E.S, E.M, E.mem_n, (BalBlock*)E.baltab, E.balg, E.ctrl + 4);
+        CLOWNS_CUDA_TRY(cudaGetLastError());
+        t_launches += 1;
+    }
     if (sh.graph == 2) {
         CLOWNS_CUDA_TRY(cudaMemsetAsync(gb, 0, sizeof(GridBar), s));
         Shape ksh;

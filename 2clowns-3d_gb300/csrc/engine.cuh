@@ -110,6 +110,7 @@ struct Eng {
     unsigned* ticket;         // one per member
     int* ctrl;                // [0] loop-body count, [1] max ITER over members, [2] bodies of earlier sweeps
     const BalBlock* baltab;   // ensembles: 16 block tables of the balanced kernels (nullptr: none)
+    const int* balg;          // ensembles: the blocks of each table's launch (16)
 };
 
 // ---------------------------------------------------------------------------
@@ -1200,13 +1201,73 @@ __global__ void __launch_bounds__(kEngBlock, kBalMinBlocks<T, R>) k_bal_pupdate(
 // Graph mode: the last node of the WHILE body and the only writer of the loop
 // condition.  Continue while any member iterates; as a backstop no correct
 // run reaches, stop after max ITER + 2 bodies.
-static __global__ void k_eng_guard(MemberScalars* S, int M, int* ctrl, cudaGraphConditionalHandle h) {
+// Ensembles with the balanced kernels: rebuild the 16 block tables over the
+// members still iterating -- member m (active) takes blocks [C_m, C_m+1) of a
+// launch of G blocks, C_m = A_m + floor((G - NA) R_m / RT), A_m and R_m the
+// active members and their rows before m, NA and RT their totals -- so that
+// blocks go to members that still work.  Skipped while NA equals the count of
+// the last rebuild (*last_na), unless force.  One block; NA <= M <= G holds
+// for every table (the host uploads G only then).
+constexpr int kBalScanThreads = 256;
+__device__ __forceinline__ void bal_rebuild(const MemberScalars* S, int M, const int* mem_n, BalBlock* tab,
+                                            const int* balg, int* last_na, bool force) {
+    __shared__ int s_cnt[kBalScanThreads + 1];
+    __shared__ long long s_rows[kBalScanThreads + 1];
+    const int t = threadIdx.x, nt = blockDim.x;
+    const int per = (M + nt - 1) / nt, m0 = min(M, t * per), m1 = min(M, m0 + per);
+    int c = 0;
+    long long r = 0;
+    for (int m = m0; m < m1; m++)
+        if (!sld(&S[m].done)) { c++; r += mem_n[m]; }
+    s_cnt[t + 1] = c;
+    s_rows[t + 1] = r;
+    __syncthreads();
+    if (t == 0) {                         // exclusive prefix over the threads' chunks (nt <= 256)
+        s_cnt[0] = 0;
+        s_rows[0] = 0;
+        for (int q = 1; q <= nt; q++) {
+            s_cnt[q] += s_cnt[q - 1];
+            s_rows[q] += s_rows[q - 1];
+        }
+    }
+    __syncthreads();
+    const int NA = s_cnt[nt];
+    const long long RT = s_rows[nt];
+    if (NA == 0 || (!force && NA == *last_na)) return;
+    __syncthreads();
+    if (t == 0) *last_na = NA;
+    for (int k = 0; k < 16; k++) {
+        const int G = balg[k];
+        BalBlock* tk = tab + (size_t)k * kBalTabMax;
+        int a = s_cnt[t];
+        long long rb = s_rows[t];
+        for (int m = m0; m < m1; m++) {
+            if (sld(&S[m].done)) continue;
+            const int c0 = a + (int)((long long)(G - NA) * rb / RT);
+            rb += mem_n[m];
+            const int c1 = a + 1 + (int)((long long)(G - NA) * rb / RT);
+            for (int b = c0; b < c1; b++) tk[b] = BalBlock{m, b - c0, c1 - c0, c0};
+            a++;
+        }
+    }
+}
+
+// Standalone rebuild before a loop starts (every member active again).
+static __global__ void k_bal_rebuild(const MemberScalars* S, int M, const int* mem_n, BalBlock* tab,
+                                     const int* balg, int* last_na) {
+    bal_rebuild(S, M, mem_n, tab, balg, last_na, true);
+}
+
+static __global__ void k_eng_guard(MemberScalars* S, int M, int* ctrl, cudaGraphConditionalHandle h,
+                                   const int* mem_n, BalBlock* baltab, const int* balg) {
     pdl_enter();
     __shared__ int any;
     if (threadIdx.x == 0) any = 0;
     __syncthreads();
     for (int m = threadIdx.x; m < M; m += blockDim.x)
         if (!sld(&S[m].done)) atomicOr(&any, 1);
+    __syncthreads();
+    if (baltab) bal_rebuild(S, M, mem_n, baltab, balg, ctrl + 4, false);
     __syncthreads();
     if (threadIdx.x == 0) {
         ctrl[0] += 1;
