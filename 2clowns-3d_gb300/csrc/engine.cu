@@ -881,10 +881,11 @@ static int check_abort(GridBar* gb, cudaStream_t s) {
 }
 
 // Autotuner: time kTuneIters iterations of the loop for each candidate -- the
-// graph with fused and with single sweep pairs, the persistent kernel and the
-// wavefront kernel -- on the actual row space, in four rounds over all
-// candidates (the first warms up and builds the graphs); cache the candidate
-// with the smallest best-of-three time per (row-space size, precision).
+// wavefront kernel, the persistent kernel, the graph of tile kernels with fused
+// or single sweep pairs, and the graph of balanced kernels -- on the actual row
+// space, in four rounds over all candidates (the first warms up and builds the
+// graphs); cache, per (row-space size, precision), the first candidate whose
+// best-of-three time is within 1 % of the fastest.
 // `prime` re-creates the state the loop starts from.
 constexpr int kTuneIters = 24;
 template <typename T, typename Prime>
@@ -1019,10 +1020,15 @@ static int tune_loop(Eng<T> E, const void* work, GridBar* gb, long key_nv, int k
             if (round > 0) best_of[c] = std::min(best_of[c], ms);
         }
     }
-    LoopShape best = cands[0];
+    // The first candidate (in the fixed order above) within 1 % of the fastest:
+    // candidates closer than the timing noise would otherwise swap from run to
+    // run, and with them the summation order and the iteration count.
     float best_ms = 1e30f;
     for (size_t c = 0; c < cands.size(); c++)
-        if (!failed[c] && best_of[c] < best_ms) { best_ms = best_of[c]; best = cands[c]; }
+        if (!failed[c]) best_ms = std::min(best_ms, best_of[c]);
+    LoopShape best = cands[0];
+    for (size_t c = 0; c < cands.size(); c++)
+        if (!failed[c] && best_of[c] <= best_ms * 1.01f) { best = cands[c]; break; }
     cudaEventDestroy(e0);
     cudaEventDestroy(e1);
     std::lock_guard<std::mutex> lk(g_loop_mu);
