@@ -130,7 +130,7 @@ int clowns_pcgpme_dev(const double* al, int nl, int na, const int* ll, const dou
  * FP32.  An FP64 outer loop forms r = W (b - A x) from the caller's original FP64
  * matrix, measures ERR = ||PM r|| / ||PM W b|| (the reference's EPS definition)
  * in FP64, solves PM W A d = PM r / ||PM r|| in FP32 to the relative residual
- * max(inner_tol, eps / (2 ERR)) (inner_tol <= 0: 1.6e-2) -- no further than the
+ * max(inner_tol, eps / (2 ERR)) (inner_tol <= 0: 3e-2) -- no further than the
  * outer tolerance still needs -- and accumulates x += ||PM r|| d in FP64, until
  * ERR <= eps.  info->iter counts
  * inner iterations, info->outer the refinement sweeps; IER = 3000 after
