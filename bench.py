@@ -56,8 +56,8 @@ def measured_peaks():
 # accumulation; 96 B for the FP64 -> FP32 conversion).
 # Measured DRAM bytes per row and iteration of the loop graph (ncu, the graph as
 # one unit, beach_256x256x96): profiles/pcgpme_loop_dram_beach_256x256x96.md.
-TRAFFIC_ROW_ITER_FP64 = 448.8
-TRAFFIC_ROW_ITER_MIXED = 251.6
+TRAFFIC_ROW_ITER_FP64 = 448.7
+TRAFFIC_ROW_ITER_MIXED = 252.1
 
 
 def bytes_solve_fp64(n: int, iters: int) -> float:
