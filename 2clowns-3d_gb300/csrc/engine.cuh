@@ -845,12 +845,13 @@ __global__ void __launch_bounds__(kEngBlock) k_eng_initres(Eng<T> E) {
 // Balanced kernels.  The iteration's kernels can instead run as exactly one
 // wave each: G = (resident blocks per SM) x SMs blocks, block b owning the
 // rows [n b / G, n (b+1) / G) and walking them R rows per thread per step.  An
-// ensemble splits the G blocks over its members in proportion to their rows,
-// at least one block each, by a table the host writes (BalBlock per block);
-// blocks of a stopped member return before loading anything.  Every block then does the same work and all retire together, and
-// the per-block costs -- launch, the stop-flag and scalar loads, the reduction
-// tail -- are paid G times per kernel instead of once per 512-row tile (5517
-// times at 2.8 M rows).  The per-row arithmetic is the tile kernels'; dot
+// ensemble splits the G blocks over its members still iterating in proportion
+// to their rows, at least one block each, by a table (BalBlock per block) that
+// bal_rebuild writes on the device; blocks of a stopped member return before
+// loading anything.  Every block then does the same work and all retire
+// together, and the per-block costs -- launch, the stop-flag and scalar loads,
+// the reduction tail -- are paid G times per kernel instead of once per
+// 512-row tile (5517 times at 2.8 M rows).  The per-row arithmetic is the tile kernels'; dot
 // products are reduced once per block: the block's partial goes to
 // partials[b], and the last block of a member to finish sums the member's
 // partials in index order (deterministic for a given G) and finalises its
@@ -858,9 +859,8 @@ __global__ void __launch_bounds__(kEngBlock) k_eng_initres(Eng<T> E) {
 // tile) and at least the number of members.
 //
 // For a single system only the kernels whose results outlive a stop test read
-// the stop flag:
-// sweep56 (its reduction and finalisation) and xrupdate (x, r and the stop
-// tests); after a stop the other kernels of the body write scratch vectors (t,
+// the stop flag: sweep56 (its reduction and finalisation) and xrupdate (x, r
+// and the stop tests); after a stop the other kernels of the body write scratch vectors (t,
 // q, e, v, p) the finished solve no longer reads, and the loop guard ends the
 // graph at the end of the body.  (A flag load in every kernel cost 2-4 us per
 // kernel at 2.8 M rows, as did reading the scalars once per block behind a
