@@ -355,6 +355,7 @@ def run_will(args):
             "e2e": {"value": 1.0 / e2e_s, "unit": "solves/s",
                     "h2d_bytes_per_step": n * (4 * 8 + 4 * 4 + 2 * 8), "d2h_bytes_per_step": n * 8},
             "rel_l2_vs_oracle": float(np.linalg.norm(bg - bo) / np.linalg.norm(bo)),
+            "tuned_shape": pkg.tuned_shape([n], 0),
             "cpu_baseline": {"value": 1.0 / t_cpu, "unit": "solves/s", "cores": threads, "kind": "port",
                              "cpu_model": cpu_model(),
                              "sample": f"one solve, OpenMP restatement of pcgpme_2DH.f90 on {threads} threads"}}
