@@ -353,6 +353,7 @@ static Eng<T> eng_bind(void* work, const EngLayout& L) {
     E.wave = L.wave ? (WaveCtl*)(b + L.o_wave) : nullptr;
     for (int k = 0; k < kWaveBufs; k++) E.w[k] = L.wave ? (T*)(b + L.o_wbuf[k]) : nullptr;
     E.baltab = nullptr;       // set once the launch sizes are uploaded (upload_bal_tables)
+    E.nl = 6;                 // set by the solve from its members' NL
     E.balg = L.o_balg ? (const int*)(b + L.o_balg) : nullptr;
     return E;
 }
@@ -1160,6 +1161,7 @@ int engine_solve_plain(int M, const MemberIn* ins, double eps, double parm, int 
     rc = eng_upload_tables(work, L, n.data(), ins, s);
     if (rc) return rc;
     Eng<double> E = eng_bind<double>(work, L);
+    E.nl = nl;
     bool bal_ok = false;
     rc = upload_bal_tables<double>(work, L, n.data(), s, &bal_ok);
     if (rc) return rc;
@@ -1229,6 +1231,7 @@ int engine_solve_mixed(int M, const MemberIn* ins, double eps, double parm, doub
     rc = eng_upload_tables(work, L, n.data(), ins, s);
     if (rc) return rc;
     Eng<float> E = eng_bind<float>(work, L);
+    E.nl = nl;
     bool bal_ok = false;
     rc = upload_bal_tables<float>(work, L, n.data(), s, &bal_ok);
     if (rc) return rc;

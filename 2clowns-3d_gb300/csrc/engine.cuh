@@ -111,6 +111,7 @@ struct Eng {
     int* ctrl;                // [0] loop-body count, [1] max ITER over members, [2] bodies of earlier sweeps
     const BalBlock* baltab;   // ensembles: 16 block tables of the balanced kernels (nullptr: none)
     const int* balg;          // ensembles: the blocks of each table's launch (16)
+    int nl;                   // columns the members' matrices fill: 6 (3D) or 4 (2DH); the rest are empty
 };
 
 // ---------------------------------------------------------------------------
@@ -957,6 +958,7 @@ __global__ void __launch_bounds__(kEngBlock, kBalMinBlocks<T, R>) k_bal_axsub(En
         }
 #pragma unroll
         for (int k = 0; k < 6; k++) {
+            if (k >= E.nl) break;                     // empty columns: zero coefficients at the zero row
             T a[R];
             int c[R];
 #pragma unroll
@@ -1070,27 +1072,32 @@ __global__ void __launch_bounds__(kEngBlock, kBalMinBlocks<T, R>) k_bal_sweep56(
         T a5v[R], a6v[R], xv[R], g5[R], g6[R];
         int c5v[R], c6v[R];
         bool ok[R];
+        const bool six = E.nl == 6;                   // NL = 4: sweeps 5 and 6 are empty, out = in
 #pragma unroll
         for (int u = 0; u < R; u++) {
             const long r = base + (long)u * blockDim.x;
             ok[u] = r < hi;
             const long i = ok[u] ? r : lo;
-            a5v[u] = ld_stream(a5 + i);
-            a6v[u] = ld_stream(a6 + i);
-            c5v[u] = ld_stream(c5 + i);
-            c6v[u] = ld_stream(c6 + i);
             xv[u] = ldg2(in + i);
+            if (six) {
+                a5v[u] = ld_stream(a5 + i);
+                a6v[u] = ld_stream(a6 + i);
+                c5v[u] = ld_stream(c5 + i);
+                c6v[u] = ld_stream(c6 + i);
+            }
         }
+        if (six) {
 #pragma unroll
-        for (int u = 0; u < R; u++) {
-            g5[u] = ldg2(in + c5v[u]);
-            g6[u] = ldg2(in + c6v[u]);
+            for (int u = 0; u < R; u++) {
+                g5[u] = ldg2(in + c5v[u]);
+                g6[u] = ldg2(in + c6v[u]);
+            }
         }
 #pragma unroll
         for (int u = 0; u < R; u++) {
             if (!ok[u] || done) continue;
             const long i = base + (long)u * blockDim.x;
-            const T y = fnma(a6v[u], g6[u], fnma(a5v[u], g5[u], xv[u]));
+            const T y = six ? fnma(a6v[u], g6[u], fnma(a5v[u], g5[u], xv[u])) : xv[u];
             out[i] = y;
             if (MODE == 1) acc0 += ldg2(E.r0 + i) * y;
             if (MODE == 2) { acc0 += ldg2(E.e + i) * y; acc1 += y * y; }
