@@ -598,9 +598,9 @@ struct BalGrids {
 // The balanced kernels' one-wave grids (queried once; before any capture)
 template <typename T, int R>
 static const BalGrids& bal_grids() {
-    static const BalGrids g = {bal_grid(k_bal_axsub<T, R>, INT_MAX), bal_grid(k_bal_sweep<T, R>, INT_MAX),
-                               bal_grid(k_bal_sweep2<T, R>, INT_MAX), bal_grid(k_bal_sweep56<T, 1, R>, INT_MAX),
-                               bal_grid(k_bal_sweep56<T, 2, R>, INT_MAX), bal_grid(k_bal_eupdate<T, R>, INT_MAX),
+    static const BalGrids g = {bal_grid(k_bal_axsub<T, R, 6>, INT_MAX), bal_grid(k_bal_sweep<T, R>, INT_MAX),
+                               bal_grid(k_bal_sweep2<T, R>, INT_MAX), bal_grid(k_bal_sweep56<T, 1, R, 6>, INT_MAX),
+                               bal_grid(k_bal_sweep56<T, 2, R, 6>, INT_MAX), bal_grid(k_bal_eupdate<T, R>, INT_MAX),
                                bal_grid(k_bal_xrupdate<T, R>, INT_MAX), bal_grid(k_bal_pupdate<T, R>, INT_MAX)};
     return g;
 }
@@ -647,7 +647,7 @@ static int upload_bal_tables(void* work, const EngLayout& L, const int* n, cudaS
     return CLOWNS_OK;
 }
 
-template <typename T, int R>
+template <typename T, int R, int NL>
 static void g_iteration_bal(bool pdl, const Eng<T>& E, const Shape& sh, cudaStream_t s) {
     const int B = kEngBlock, n = E.nblk;
     const BalGrids& G = bal_grids<T, R>();
@@ -656,7 +656,7 @@ static void g_iteration_bal(bool pdl, const Eng<T>& E, const Shape& sh, cudaStre
         return E.M == 1 ? nullptr : E.baltab + (size_t)((R == 8 ? 8 : 0) + k) * kBalTabMax;
     };
     auto apply = [&](const T* in, T* out, int mode) {
-        klaunch(pdl, k_bal_axsub<T, R>, grid(kBalAx), B, s, E, tab(kBalAx), in, E.t);
+        klaunch(pdl, k_bal_axsub<T, R, NL>, grid(kBalAx), B, s, E, tab(kBalAx), in, E.t);
         if (sh.fuse) {
             klaunch(pdl, k_bal_sweep2<T, R>, grid(kBalS2), B, s, E, tab(kBalS2), 0, (const T*)E.t, out);
             klaunch(pdl, k_bal_sweep2<T, R>, grid(kBalS2), B, s, E, tab(kBalS2), 2, (const T*)out, E.t);
@@ -666,8 +666,8 @@ static void g_iteration_bal(bool pdl, const Eng<T>& E, const Shape& sh, cudaStre
             klaunch(pdl, k_bal_sweep<T, R>, grid(kBalSw), B, s, E, tab(kBalSw), 2, (const T*)E.t, out);
             klaunch(pdl, k_bal_sweep<T, R>, grid(kBalSw), B, s, E, tab(kBalSw), 3, (const T*)out, E.t);
         }
-        if (mode == 1) klaunch(pdl, k_bal_sweep56<T, 1, R>, grid(kBalR1), B, s, E, tab(kBalR1), (const T*)E.t, out);
-        else klaunch(pdl, k_bal_sweep56<T, 2, R>, grid(kBalR2), B, s, E, tab(kBalR2), (const T*)E.t, out);
+        if (mode == 1) klaunch(pdl, k_bal_sweep56<T, 1, R, NL>, grid(kBalR1), B, s, E, tab(kBalR1), (const T*)E.t, out);
+        else klaunch(pdl, k_bal_sweep56<T, 2, R, NL>, grid(kBalR2), B, s, E, tab(kBalR2), (const T*)E.t, out);
     };
     apply((const T*)E.p, E.q, 1);                                                    // q = PM A p ; RQ ; ALP
     klaunch(pdl, k_bal_eupdate<T, R>, grid(kBalEu), B, s, E, tab(kBalEu));          // e = r - ALP q
@@ -683,8 +683,13 @@ static bool bal_usable(const Eng<T>& E) { return E.M == 1 || E.baltab != nullptr
 template <typename T>
 static void g_iteration(bool pdl, const Eng<T>& E, const Shape& sh, cudaStream_t s) {
     if (sh.bal && bal_usable(E)) {
-        if (sh.bal == 8) g_iteration_bal<T, 8>(pdl, E, sh, s);
-        else g_iteration_bal<T, 4>(pdl, E, sh, s);
+        if (E.nl == 4) {
+            if (sh.bal == 8) g_iteration_bal<T, 8, 4>(pdl, E, sh, s);
+            else g_iteration_bal<T, 4, 4>(pdl, E, sh, s);
+        } else {
+            if (sh.bal == 8) g_iteration_bal<T, 8, 6>(pdl, E, sh, s);
+            else g_iteration_bal<T, 4, 6>(pdl, E, sh, s);
+        }
         return;
     }
     const int g = grid_of(sh, E.nblk), b = sh.block;
@@ -699,10 +704,10 @@ static void g_iteration(bool pdl, const Eng<T>& E, const Shape& sh, cudaStream_t
 struct GraphKey {
     const void* work;
     long NV;
-    int M, prec, fuse, rblock, bal;
+    int M, prec, fuse, rblock, bal, nl;
     bool operator<(const GraphKey& o) const {
-        return std::tie(work, NV, M, prec, fuse, rblock, bal) <
-               std::tie(o.work, o.NV, o.M, o.prec, o.fuse, o.rblock, o.bal);
+        return std::tie(work, NV, M, prec, fuse, rblock, bal, nl) <
+               std::tie(o.work, o.NV, o.M, o.prec, o.fuse, o.rblock, o.bal, o.nl);
     }
 };
 static std::mutex g_graph_mu;
@@ -775,7 +780,7 @@ template <typename T>
 static int loop_graph(const Eng<T>& E, const void* work, int prec, int fuse, int rblock, int bal,
                       cudaGraphExec_t* out) {
     std::lock_guard<std::mutex> lk(g_graph_mu);
-    GraphKey key{work, E.NV, E.M, prec, fuse, rblock, bal};
+    GraphKey key{work, E.NV, E.M, prec, fuse, rblock, bal, E.nl};
     auto it = g_graphs.find(key);
     if (it != g_graphs.end()) { *out = it->second; return CLOWNS_OK; }
     cudaGraphExec_t ex;

@@ -939,7 +939,9 @@ __device__ __forceinline__ bool bal_reduce(const Eng<T>& E, const BalBlock& bb, 
     return true;
 }
 
-template <typename T, int R>
+// NL: the columns the matrix fills (6, or 4 for a 2DH system, whose two empty
+// columns hold zero coefficients at the zero row and are not read).
+template <typename T, int R, int NL>
 __global__ void __launch_bounds__(kEngBlock, kBalMinBlocks<T, R>) k_bal_axsub(Eng<T> E, const BalBlock* __restrict__ tab, const T* __restrict__ in, T* __restrict__ out) {
     pdl_enter();
     const long NV = E.NV;
@@ -957,8 +959,7 @@ __global__ void __launch_bounds__(kEngBlock, kBalMinBlocks<T, R>) k_bal_axsub(En
             s[u] = ldg2(in + i) * ld_stream(E.d + i);
         }
 #pragma unroll
-        for (int k = 0; k < 6; k++) {
-            if (k >= E.nl) break;                     // empty columns: zero coefficients at the zero row
+        for (int k = 0; k < NL; k++) {
             T a[R];
             int c[R];
 #pragma unroll
@@ -1053,8 +1054,9 @@ __global__ void __launch_bounds__(kEngBlock, kBalMinBlocks<T, R>) k_bal_sweep2(E
     }
 }
 
-// sweeps 5, 6 with the RQ (MODE 1) or AMU (MODE 2) reduction (as tl_sweep56)
-template <typename T, int MODE, int R>
+// sweeps 5, 6 with the RQ (MODE 1) or AMU (MODE 2) reduction (as tl_sweep56);
+// NL = 4: a copy with the reduction
+template <typename T, int MODE, int R, int NL>
 __global__ void __launch_bounds__(kEngBlock, kBalMinBlocks<T, R>) k_bal_sweep56(Eng<T> E, const BalBlock* __restrict__ tab, const T* __restrict__ in, T* __restrict__ out) {
     pdl_enter();
     __shared__ double red[64];
@@ -1072,19 +1074,19 @@ __global__ void __launch_bounds__(kEngBlock, kBalMinBlocks<T, R>) k_bal_sweep56(
         T a5v[R], a6v[R], xv[R], g5[R], g6[R];
         int c5v[R], c6v[R];
         bool ok[R];
-        const bool six = E.nl == 6;                   // NL = 4: sweeps 5 and 6 are empty, out = in
+        constexpr bool six = NL == 6;                 // NL = 4: sweeps 5 and 6 are empty, out = in
 #pragma unroll
         for (int u = 0; u < R; u++) {
             const long r = base + (long)u * blockDim.x;
             ok[u] = r < hi;
             const long i = ok[u] ? r : lo;
-            xv[u] = ldg2(in + i);
             if (six) {
                 a5v[u] = ld_stream(a5 + i);
                 a6v[u] = ld_stream(a6 + i);
                 c5v[u] = ld_stream(c5 + i);
                 c6v[u] = ld_stream(c6 + i);
             }
+            xv[u] = ldg2(in + i);
         }
         if (six) {
 #pragma unroll
