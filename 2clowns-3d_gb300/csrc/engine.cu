@@ -627,8 +627,7 @@ static int bal_grid_of(const BalGrids& g, int kind) {
 // stop).  *ok is false (nothing uploaded) when a launch has fewer blocks than
 // members: the ensemble then keeps the tile kernels.
 template <typename T>
-static int upload_bal_tables(void* work, const EngLayout& L, const int* n, cudaStream_t s, bool* ok) {
-    (void)n;
+static int upload_bal_tables(void* work, const EngLayout& L, cudaStream_t s, bool* ok) {
     *ok = false;
     const int M = L.M;
     if (M <= 1 || !L.o_baltab) return CLOWNS_OK;
@@ -1168,7 +1167,7 @@ int engine_solve_plain(int M, const MemberIn* ins, double eps, double parm, int 
     Eng<double> E = eng_bind<double>(work, L);
     E.nl = nl;
     bool bal_ok = false;
-    rc = upload_bal_tables<double>(work, L, n.data(), s, &bal_ok);
+    rc = upload_bal_tables<double>(work, L, s, &bal_ok);
     if (rc) return rc;
     if (bal_ok) E.baltab = (const BalBlock*)((const char*)work + L.o_baltab);
     GridBar* gb = (GridBar*)((char*)work + L.o_bar);
@@ -1238,7 +1237,7 @@ int engine_solve_mixed(int M, const MemberIn* ins, double eps, double parm, doub
     Eng<float> E = eng_bind<float>(work, L);
     E.nl = nl;
     bool bal_ok = false;
-    rc = upload_bal_tables<float>(work, L, n.data(), s, &bal_ok);
+    rc = upload_bal_tables<float>(work, L, s, &bal_ok);
     if (rc) return rc;
     if (bal_ok) E.baltab = (const BalBlock*)((const char*)work + L.o_baltab);
     GridBar* gb = (GridBar*)((char*)work + L.o_bar);
