@@ -278,3 +278,22 @@ def test_reader_rounds_spacings_like_the_reference(ing, ora, pkg, tmp_path):
     _, _, s1 = ora.prepare(r)
     assert np.array_equal(s0.alu.view(np.int64), s1.alu.view(np.int64))
     assert np.array_equal(s0.b.view(np.int64), s1.b.view(np.int64))
+
+
+def test_missing_fdata_and_nsdata_defaults(ing, pkg, tmp_path):
+    """Without .fdata every face of cells 1..inne is open with porosity 1 (faces
+    of the obstacle-surface cells closed); without .nsdata every surface
+    position is the -1e4 marker; dt falls back to the trailing record when
+    t0 > 0, else to the argument."""
+    import os
+    c = pkg.workload.make_case(10, 8, 6, dz=0.1, seed=2)
+    ing.write_case(tmp_path / "c", c, sparse=True, t=1.5, dt=2e-3)
+    os.remove(tmp_path / "c.fdata")
+    os.remove(tmp_path / "c.nsdata")
+    got = ing.read_case(tmp_path / "c")
+    r = got.case
+    assert np.all(r.a[1:r.inne + 1] == 1.0) and np.all(r.fb[1:r.inne + 1] == 1.0)
+    assert np.all(r.a[r.inne + 1:] == 0.0)
+    assert np.all(r.sp[0] == ing.SDUM)
+    assert got.dt0 == 2e-3 and r.dt == 2e-3 and got.t0 == 1.5
+    assert ing.read_case(tmp_path / "c", dt=5e-4).case.dt == 5e-4
