@@ -106,6 +106,7 @@ _SIGS = {
     "clowns_tuned_shape": (C.c_int, [C.c_int, C.c_void_p, C.c_int, C.c_void_p, C.c_void_p, C.c_void_p,
                                      C.c_void_p, C.c_void_p]),
     "clowns_last_kernel_launches": (C.c_long, []),
+    "clowns_test_arm_wait_timeout": (C.c_int, [C.c_long, C.c_int]),
     "clowns_session_create": (C.c_int, [C.c_void_p, C.c_void_p, C.c_int, C.c_int, C.c_int] + [C.c_void_p] * 7),
     "clowns_session_set_fields": (C.c_int, [C.c_void_p] * 9),
     "clowns_session_classify": (C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p]),

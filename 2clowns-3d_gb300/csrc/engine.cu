@@ -47,7 +47,7 @@ __global__ void __launch_bounds__(kEngBlock) k_mx_residual(Eng<T> E) {
             double s = in.d[li] * E.x64[i];
             for (int k = 0; k < in.nl; k++) {
                 const int c = in.ll[k * (long)in.na + li];
-                if (c > 0 && c <= in.n) s += in.al[k * (long)in.na + li] * E.x64[off + c - 1];
+                if (c > 0 && c <= in.n) s = fma_rn(in.al[k * (long)in.na + li], E.x64[off + c - 1], s);
             }
             E.r64[i] = E.W[i] * (in.b[li] - s);
         }
@@ -67,12 +67,13 @@ __global__ void __launch_bounds__(kEngBlock) k_mx_sweep(Eng<T> E, int k, const d
         if (!tile_outer(E, blk, m, row0, rows)) continue;
         for (int r = threadIdx.x; r < rows; r += blockDim.x) {
             const long i = row0 + r;
-            out[i] = in[i] - (double)a[i] * in[c[i]];
+            out[i] = fnma((double)a[i], in[c[i]], in[i]);
         }
     }
 }
 
-// Last sweep on FP64 vectors with the squared norm of the result per member.
+// Last sweep on FP64 vectors with the squared norm of the result per member
+// (the canonical reduction: warp w takes the tile's chunks w, w + nw, ...).
 //   PHASE 0: BN64 = ||PM W b||^2
 //   PHASE 1: ERR64 = sqrt(||PM r||^2 / BN64); stop the member at the outer
 //            tolerance or sweep cap, else arm its inner solve (mode 1) with
@@ -83,85 +84,101 @@ template <typename T, int PHASE>
 __global__ void __launch_bounds__(kEngBlock) k_mx_sweep56(Eng<T> E, const double* __restrict__ in,
                                                          double* __restrict__ out, double inner_tol,
                                                          int inner_max) {
-    __shared__ double red[64];
     const long NV = E.NV;
     const T* __restrict__ a5 = E.al + 4 * NV;
     const T* __restrict__ a6 = E.al + 5 * NV;
     const int* __restrict__ c5 = E.ll + 4 * NV;
     const int* __restrict__ c6 = E.ll + 5 * NV;
+    const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5, nw = blockDim.x >> 5;
     for (int blk = blockIdx.x; blk < E.nblk; blk += gridDim.x) {
         int m, rows;
         long row0;
         if (!tile_outer(E, blk, m, row0, rows)) continue;
-        double acc = 0.0;
-        for (int r = threadIdx.x; r < rows; r += blockDim.x) {
-            const long i = row0 + r;
-            const double y = in[i] - (double)a5[i] * in[c5[i]] - (double)a6[i] * in[c6[i]];
-            out[i] = y;
-            acc += y * y;
+        for (int q = wid; q < kTileChunks; q += nw) {
+            const int cr = q * kChunk;
+            if (cr >= rows) break;
+            double acc[1] = {0.0};
+#pragma unroll
+            for (int u = 0; u < kChunkRows; u++) {
+                const int r = cr + 32 * u + lane;
+                if (r >= rows) continue;
+                const long i = row0 + r;
+                const double y = fnma((double)a6[i], in[c6[i]], fnma((double)a5[i], in[c5[i]], in[i]));
+                out[i] = y;
+                acc[0] = fma_rn(y, y, acc[0]);
+            }
+            chunk_total(E, (row0 + cr) / kChunk, acc);
         }
+        int c0, c1;
+        tile_chunks(E, m, row0, rows, c0, c1);
         double tot[2];
-        if (!member_reduce(E, blk, m, acc, 0.0, red, tot)) continue;
-        if (threadIdx.x == 0) {
-            MemberScalars* S = E.S + m;
-            E.ticket[m] = 0;
-            if (PHASE == 0) {
-                S->BN64 = tot[0];
+        if (!account_chunks(E, m, c0, c1, tot) || lane != 0) continue;
+        MemberScalars* S = E.S + m;
+        E.ticket[m] = 0;
+        if (PHASE == 0) {
+            S->BN64 = tot[0];
+        } else {
+            const double err = sqrt(tot[0] / S->BN64);
+            S->ERR64 = err;
+            if (!isfinite(err)) {
+                S->odone = 1;
+                stop_member(S, CLOWNS_STOP_NONFINITE, CLOWNS_IER_NONFINITE);
+            } else if (err <= S->EPS64) {
+                S->odone = 1;
+                stop_member(S, CLOWNS_STOP_TOL, 0);
+            } else if (S->outer >= S->OITER) {
+                S->odone = 1;
+                stop_member(S, CLOWNS_STOP_MAXITER, CLOWNS_IER_MAXITER);
             } else {
-                const double err = sqrt(tot[0] / S->BN64);
-                S->ERR64 = err;
-                if (!isfinite(err)) {
-                    S->odone = 1;
-                    stop_member(S, CLOWNS_STOP_NONFINITE, CLOWNS_IER_NONFINITE);
-                } else if (err <= S->EPS64) {
-                    S->odone = 1;
-                    stop_member(S, CLOWNS_STOP_TOL, 0);
-                } else if (S->outer >= S->OITER) {
-                    S->odone = 1;
-                    stop_member(S, CLOWNS_STOP_MAXITER, CLOWNS_IER_MAXITER);
-                } else {
-                    S->outer += 1;
-                    S->SIGMA = sqrt(tot[0]);
-                    S->K = 0;
-                    S->ERRP = 0.0;
-                    S->done = 0;
-                    S->mode = 1;
-                    S->EPS = fmax(inner_tol, 0.5 * S->EPS64 / err);
-                    S->ITER = inner_max;
-                }
+                S->outer += 1;
+                S->SIGMA = sqrt(tot[0]);
+                S->K = 0;
+                S->ERRP = 0.0;
+                S->done = 0;
+                S->mode = 1;
+                S->EPS = fmax(inner_tol, 0.5 * S->EPS64 / err);
+                S->ITER = inner_max;
             }
         }
-        __syncwarp();
+        __threadfence();
     }
 }
 
 // Inner right-hand side: r = p = r0 = T(PM r64 / sigma), xi = 0; BN = C1 = ||r||^2
 template <typename T>
 __global__ void __launch_bounds__(kEngBlock) k_mx_normalize(Eng<T> E) {
-    __shared__ double red[64];
+    const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5, nw = blockDim.x >> 5;
     for (int blk = blockIdx.x; blk < E.nblk; blk += gridDim.x) {
         int m, rows;
         long row0;
         if (!tile_outer(E, blk, m, row0, rows)) continue;
         const double inv = 1.0 / E.S[m].SIGMA;
-        double acc = 0.0;
-        for (int r = threadIdx.x; r < rows; r += blockDim.x) {
-            const long i = row0 + r;
-            const T v = T(E.r64[i] * inv);
-            E.r[i] = v;
-            E.p[i] = v;
-            E.r0[i] = v;
-            E.xi[i] = T(0);
-            acc += (double)v * (double)v;
+        for (int q = wid; q < kTileChunks; q += nw) {
+            const int cr = q * kChunk;
+            if (cr >= rows) break;
+            double acc[1] = {0.0};
+#pragma unroll
+            for (int u = 0; u < kChunkRows; u++) {
+                const int r = cr + 32 * u + lane;
+                if (r >= rows) continue;
+                const long i = row0 + r;
+                const T v = T(E.r64[i] * inv);
+                E.r[i] = v;
+                E.p[i] = v;
+                E.r0[i] = v;
+                E.xi[i] = T(0);
+                acc[0] = fma_rn((double)v, (double)v, acc[0]);
+            }
+            chunk_total(E, (row0 + cr) / kChunk, acc);
         }
+        int c0, c1;
+        tile_chunks(E, m, row0, rows, c0, c1);
         double tot[2];
-        if (!member_reduce(E, blk, m, acc, 0.0, red, tot)) continue;
-        if (threadIdx.x == 0) {
-            E.ticket[m] = 0;
-            E.S[m].BN = tot[0];
-            E.S[m].C1 = tot[0];
-        }
-        __syncwarp();
+        if (!account_chunks(E, m, c0, c1, tot) || lane != 0) continue;
+        E.ticket[m] = 0;
+        E.S[m].BN = tot[0];
+        E.S[m].C1 = tot[0];
+        __threadfence();
     }
 }
 
@@ -224,17 +241,17 @@ __global__ void k_eng_export(Eng<T> E, double* al_s, int* ll_s, double* d_s, dou
 // ---------------------------------------------------------------------------
 // Layout
 
-// Reduction groups of a member of n rows: kGroupTiles consecutive tiles each.
+// Reduction groups of a member of n rows: kGroupChunks consecutive 128-row chunks each.
 static inline int member_groups(int n) {
-    const int nblk = (n + kTile - 1) / kTile;
-    return (nblk + kGroupTiles - 1) / kGroupTiles;
+    const int nc = (n + kChunk - 1) / kChunk;
+    return (nc + kGroupChunks - 1) / kGroupChunks;
 }
 
 struct EngLayout {
     long NV = 0;
     int M = 0, nblk = 0, ngrp = 0, mixed = 0, tsize = 8, wave = 0, nchunk = 0, n1 = 0;
     size_t o_blk_member, o_blk_rows, o_mem_off, o_mem_n, o_mem_nblk, o_mem_blk0, o_ticket, o_ctrl;
-    size_t o_blk_group, o_grp_blk0, o_grp_nblk, o_mem_grp0, o_mem_ngrp, o_gticket, o_gpartials;
+    size_t o_mem_grp0, o_mem_ngrp, o_gticket, o_gpartials;
     size_t o_in, o_S, o_partials, o_bar, o_al, o_ll, o_d, o_vec[8], o_W, o_x64, o_r64, o_s64, o_t64;
     size_t o_wave, o_wbuf[kWaveBufs];
     size_t o_baltab = 0;   // ensembles: block tables of the balanced kernels
@@ -268,9 +285,6 @@ static EngLayout eng_layout(int M, const int* n, int mixed, int wave = -1) {
     L.o_mem_nblk = take(sizeof(int) * M);
     L.o_mem_blk0 = take(sizeof(int) * M);
     L.o_ticket = take(sizeof(unsigned) * M);
-    L.o_blk_group = take(sizeof(int) * L.nblk);
-    L.o_grp_blk0 = take(sizeof(int) * ngrp);
-    L.o_grp_nblk = take(sizeof(int) * ngrp);
     L.o_mem_grp0 = take(sizeof(int) * M);
     L.o_mem_ngrp = take(sizeof(int) * M);
     L.o_gticket = take(sizeof(unsigned) * ngrp);
@@ -278,7 +292,7 @@ static EngLayout eng_layout(int M, const int* n, int mixed, int wave = -1) {
     L.o_ctrl = take(sizeof(int) * 8);
     L.o_in = take(sizeof(MemberIn) * M);
     L.o_S = take(sizeof(MemberScalars) * M);
-    L.o_partials = take(sizeof(double) * 2 * L.nblk);
+    L.o_partials = take(sizeof(double) * 2 * (NV / kChunk));
     L.o_bar = take(sizeof(GridBar));
     L.o_al = take((size_t)L.tsize * 6 * NV);
     L.o_ll = take(sizeof(int) * 6 * NV);
@@ -324,9 +338,6 @@ static Eng<T> eng_bind(void* work, const EngLayout& L) {
     E.mem_nblk = (const int*)(b + L.o_mem_nblk);
     E.mem_blk0 = (const int*)(b + L.o_mem_blk0);
     E.ticket = (unsigned*)(b + L.o_ticket);
-    E.blk_group = (const int*)(b + L.o_blk_group);
-    E.grp_blk0 = (const int*)(b + L.o_grp_blk0);
-    E.grp_nblk = (const int*)(b + L.o_grp_nblk);
     E.mem_grp0 = (const int*)(b + L.o_mem_grp0);
     E.mem_ngrp = (const int*)(b + L.o_mem_ngrp);
     E.gticket = (unsigned*)(b + L.o_gticket);
@@ -358,21 +369,14 @@ static Eng<T> eng_bind(void* work, const EngLayout& L) {
     return E;
 }
 
-// Reduction-group tables: group q of member m covers its real tiles
-// blk0 + q*kGroupTiles .. (at most kGroupTiles of them).  Callers size the
-// arrays: blk_group[nblk] (pre-filled with -1), grp_blk0/grp_nblk[ngrp],
-// mem_grp0/mem_ngrp[M].
-static void fill_groups(int M, const int* blk0, const int* nblk, int* blk_group, int* grp_blk0, int* grp_nblk,
-                        int* mem_grp0, int* mem_ngrp) {
+// Reduction groups: member m's groups are mem_grp0[m] .. mem_grp0[m] +
+// mem_ngrp[m] - 1 (kGroupChunks chunks of 128 rows each).
+static void fill_groups(int M, const int* n, int* mem_grp0, int* mem_ngrp) {
     int g = 0;
     for (int m = 0; m < M; m++) {
         mem_grp0[m] = g;
-        mem_ngrp[m] = (nblk[m] + kGroupTiles - 1) / kGroupTiles;
-        for (int q = 0; q < mem_ngrp[m]; q++, g++) {
-            grp_blk0[g] = blk0[m] + q * kGroupTiles;
-            grp_nblk[g] = std::min(kGroupTiles, nblk[m] - q * kGroupTiles);
-            for (int t = 0; t < grp_nblk[g]; t++) blk_group[grp_blk0[g] + t] = g;
-        }
+        mem_ngrp[m] = member_groups(n[m]);
+        g += mem_ngrp[m];
     }
 }
 
@@ -395,9 +399,8 @@ static int eng_upload_tables(void* work, const EngLayout& L, const int* n, const
         }
         o += R;
     }
-    std::vector<int> blk_group(L.nblk, -1), grp_blk0(L.ngrp), grp_nblk(L.ngrp), mem_grp0(M), mem_ngrp(M);
-    fill_groups(M, blk0.data(), nblk.data(), blk_group.data(), grp_blk0.data(), grp_nblk.data(), mem_grp0.data(),
-                mem_ngrp.data());
+    std::vector<int> mem_grp0(M), mem_ngrp(M);
+    fill_groups(M, n, mem_grp0.data(), mem_ngrp.data());
     std::vector<unsigned> zeros(std::max(M, L.ngrp), 0u);
     char* b = (char*)work;
     CLOWNS_CUDA_TRY(cudaMemcpyAsync(b + L.o_blk_member, blk_member.data(), sizeof(int) * L.nblk, cudaMemcpyHostToDevice, s));
@@ -407,9 +410,6 @@ static int eng_upload_tables(void* work, const EngLayout& L, const int* n, const
     CLOWNS_CUDA_TRY(cudaMemcpyAsync(b + L.o_mem_nblk, nblk.data(), sizeof(int) * M, cudaMemcpyHostToDevice, s));
     CLOWNS_CUDA_TRY(cudaMemcpyAsync(b + L.o_mem_blk0, blk0.data(), sizeof(int) * M, cudaMemcpyHostToDevice, s));
     CLOWNS_CUDA_TRY(cudaMemcpyAsync(b + L.o_ticket, zeros.data(), sizeof(unsigned) * M, cudaMemcpyHostToDevice, s));
-    CLOWNS_CUDA_TRY(cudaMemcpyAsync(b + L.o_blk_group, blk_group.data(), sizeof(int) * L.nblk, cudaMemcpyHostToDevice, s));
-    CLOWNS_CUDA_TRY(cudaMemcpyAsync(b + L.o_grp_blk0, grp_blk0.data(), sizeof(int) * L.ngrp, cudaMemcpyHostToDevice, s));
-    CLOWNS_CUDA_TRY(cudaMemcpyAsync(b + L.o_grp_nblk, grp_nblk.data(), sizeof(int) * L.ngrp, cudaMemcpyHostToDevice, s));
     CLOWNS_CUDA_TRY(cudaMemcpyAsync(b + L.o_mem_grp0, mem_grp0.data(), sizeof(int) * M, cudaMemcpyHostToDevice, s));
     CLOWNS_CUDA_TRY(cudaMemcpyAsync(b + L.o_mem_ngrp, mem_ngrp.data(), sizeof(int) * M, cudaMemcpyHostToDevice, s));
     CLOWNS_CUDA_TRY(cudaMemcpyAsync(b + L.o_gticket, zeros.data(), sizeof(unsigned) * L.ngrp, cudaMemcpyHostToDevice, s));
@@ -525,7 +525,9 @@ static const void* wave_fn(int minb) {
 }
 
 static std::mutex g_loop_mu;
-static std::map<std::tuple<long, int, int>, LoopShape> g_loop_shapes;   // (row space, precision, wave)
+// (row space, precision, wave loop available, forced execution or -1): a forced
+// execution is tuned among its own shapes and never served an automatic pick.
+static std::map<std::tuple<long, int, int, int>, LoopShape> g_loop_shapes;
 
 template <typename T>
 static int loop_max_grid(int block, int minb, int* out, bool wave = false) {
@@ -809,8 +811,41 @@ static long loop_launches(const LoopShape& sh, long bodies) {
     return 1;
 }
 
+// Test hook of the bounded device waits (clowns_test_arm_wait_timeout): the
+// next solve whose loop runs as one cooperative kernel gives every wait
+// `limit` polls and makes block `absent` leave without arriving.  One use.
+struct WaitFault {
+    long limit = kBarSpinLimit;
+    int absent = -1;
+    bool armed = false;
+};
+static std::mutex g_fault_mu;
+static WaitFault g_fault;
+
+void engine_arm_wait_fault(long limit, int absent) {
+    std::lock_guard<std::mutex> lk(g_fault_mu);
+    g_fault.limit = limit;
+    g_fault.absent = absent;
+    g_fault.armed = true;
+}
+
+// Wait parameters of a cooperative launch: the armed fault (once) when `take`.
+static void wait_params(bool take, long* limit, int* absent) {
+    *limit = kBarSpinLimit;
+    *absent = -1;
+    if (!take) return;
+    std::lock_guard<std::mutex> lk(g_fault_mu);
+    if (!g_fault.armed) return;
+    *limit = g_fault.limit;
+    *absent = g_fault.absent;
+    g_fault = WaitFault();
+}
+
+// take_fault: this run is a solve's (not a tuning trial's), so an armed wait
+// fault applies to it.
 template <typename T>
-static int run_loop(Eng<T> E, const void* work, GridBar* gb, int prec, const LoopShape& sh, cudaStream_t s) {
+static int run_loop(Eng<T> E, const void* work, GridBar* gb, int prec, const LoopShape& sh, cudaStream_t s,
+                    bool take_fault = false) {
     if (sh.bal && E.M > 1 && E.baltab && (sh.graph == 1 || sh.graph == 2)) {
         // ensembles on the balanced kernels: block tables over the members that iterate
         k_bal_rebuild<<<1, kBalScanThreads, 0, s>>>(E.S, E.M, E.mem_n, (BalBlock*)E.baltab, E.balg, E.ctrl + 4);
@@ -852,7 +887,10 @@ static int run_loop(Eng<T> E, const void* work, GridBar* gb, int prec, const Loo
         CLOWNS_CUDA_TRY(cudaMemsetAsync(&E.wave->alp, 0, 3 * sizeof(unsigned), s));
         CLOWNS_CUDA_TRY(cudaMemsetAsync(E.wave + 1, 0, sizeof(unsigned) * 12 * (size_t)nchunk, s));
         int K = sh.wk, slack = sh.wslack;
-        void* args[] = {(void*)&E, (void*)&gb, (void*)&K, (void*)&slack};
+        long lim;
+        int absent;
+        wait_params(take_fault, &lim, &absent);
+        void* args[] = {(void*)&E, (void*)&gb, (void*)&K, (void*)&slack, (void*)&lim, (void*)&absent};
         CLOWNS_CUDA_TRY(cudaLaunchCooperativeKernel(wave_fn<T>(sh.minb), dim3(sh.grid), dim3(kStepBlock), args, 0, s));
         t_launches += 1;
         return CLOWNS_OK;
@@ -868,7 +906,10 @@ static int run_loop(Eng<T> E, const void* work, GridBar* gb, int prec, const Loo
     int grid = std::max(1, std::min(sh.grid, E.nblk));
     CLOWNS_CUDA_TRY(cudaMemsetAsync(gb, 0, sizeof(GridBar), s));
     int init = 0;
-    void* args[] = {(void*)&E, (void*)&gb, (void*)&init};
+    long lim;
+    int absent;
+    wait_params(take_fault, &lim, &absent);
+    void* args[] = {(void*)&E, (void*)&gb, (void*)&init, (void*)&lim, (void*)&absent};
     CLOWNS_CUDA_TRY(cudaLaunchCooperativeKernel(loop_fn<T>(sh.minb), dim3(grid), dim3(sh.block), args, 0, s));
     t_launches += 1;
     return CLOWNS_OK;
@@ -910,7 +951,7 @@ static int tune_loop(Eng<T> E, const void* work, GridBar* gb, long key_nv, int k
         *out = sh;
         return CLOWNS_OK;
     }
-    const auto key = std::make_tuple(key_nv, key_prec, (int)wave_ok);
+    const auto key = std::make_tuple(key_nv, key_prec, (int)wave_ok, forced);
     // CLOWNS_WAVE_PARAMS="K,slack,minb,frac" pins the wavefront candidate (tuning sweeps; read on every call)
     const char* wp = getenv("CLOWNS_WAVE_PARAMS");
     int pk = 0, ps = 0, pm = 0, pf = 0;
@@ -1047,7 +1088,7 @@ static int tune_loop(Eng<T> E, const void* work, GridBar* gb, long key_nv, int k
 // one-wave kernels (bit 3: 8 rows per thread per step, else 4)
 int engine_tuned_shape(long nv, int prec, int single, int* mode, int* block, int* grid, int* minb, int* fuse) {
     std::lock_guard<std::mutex> lk(g_loop_mu);
-    auto it = g_loop_shapes.find(std::make_tuple(nv, prec, single));
+    auto it = g_loop_shapes.find(std::make_tuple(nv, prec, single, forced_loop_mode()));
     if (it == g_loop_shapes.end()) return CLOWNS_ERR_ARG;
     const LoopShape& sh = it->second;
     *mode = sh.graph;
@@ -1194,7 +1235,7 @@ int engine_solve_plain(int M, const MemberIn* ins, double eps, double parm, int 
     start(s);
     t_launches += 2 + 8;
     CLOWNS_CUDA_TRY(cudaGetLastError());
-    rc = run_loop(E, work, gb, 0, sh, s);
+    rc = run_loop(E, work, gb, 0, sh, s, true);
     if (rc) return rc;
     k_eng_copy_out<double><<<gs, kEngBlock, 0, s>>>(E);
     t_launches += 1;
@@ -1414,11 +1455,10 @@ static int static_upload_tables(void* work, const EngLayout& L, int n, const Mem
         blk_rows[b] = (int)std::max(0L, std::min((long)kTile, rows));
     }
     const int off = 0, nblk = (n + kTile - 1) / kTile, blk0 = 0;
-    constexpr int kStaticMaxGrp = (kStaticMaxBlk + kGroupTiles - 1) / kGroupTiles;
-    int blk_group[kStaticMaxBlk], grp_blk0[kStaticMaxGrp], grp_nblk[kStaticMaxGrp], mem_grp0 = 0, mem_ngrp = 0;
+    constexpr int kStaticMaxGrp = (kStaticMaxBlk * kTileChunks + kGroupChunks - 1) / kGroupChunks;
+    int mem_grp0 = 0, mem_ngrp = 0;
     const unsigned zeros[kStaticMaxGrp] = {};
-    for (int q = 0; q < L.nblk; q++) blk_group[q] = -1;
-    fill_groups(1, &blk0, &nblk, blk_group, grp_blk0, grp_nblk, &mem_grp0, &mem_ngrp);
+    fill_groups(1, &n, &mem_grp0, &mem_ngrp);
     const unsigned zero = 0u;
     char* b = (char*)work;
     CLOWNS_CUDA_TRY(cudaMemcpyAsync(b + L.o_blk_member, blk_member, sizeof(int) * L.nblk, cudaMemcpyHostToDevice, s));
@@ -1428,9 +1468,6 @@ static int static_upload_tables(void* work, const EngLayout& L, int n, const Mem
     CLOWNS_CUDA_TRY(cudaMemcpyAsync(b + L.o_mem_nblk, &nblk, sizeof(int), cudaMemcpyHostToDevice, s));
     CLOWNS_CUDA_TRY(cudaMemcpyAsync(b + L.o_mem_blk0, &blk0, sizeof(int), cudaMemcpyHostToDevice, s));
     CLOWNS_CUDA_TRY(cudaMemcpyAsync(b + L.o_ticket, &zero, sizeof(unsigned), cudaMemcpyHostToDevice, s));
-    CLOWNS_CUDA_TRY(cudaMemcpyAsync(b + L.o_blk_group, blk_group, sizeof(int) * L.nblk, cudaMemcpyHostToDevice, s));
-    CLOWNS_CUDA_TRY(cudaMemcpyAsync(b + L.o_grp_blk0, grp_blk0, sizeof(int) * L.ngrp, cudaMemcpyHostToDevice, s));
-    CLOWNS_CUDA_TRY(cudaMemcpyAsync(b + L.o_grp_nblk, grp_nblk, sizeof(int) * L.ngrp, cudaMemcpyHostToDevice, s));
     CLOWNS_CUDA_TRY(cudaMemcpyAsync(b + L.o_mem_grp0, &mem_grp0, sizeof(int), cudaMemcpyHostToDevice, s));
     CLOWNS_CUDA_TRY(cudaMemcpyAsync(b + L.o_mem_ngrp, &mem_ngrp, sizeof(int), cudaMemcpyHostToDevice, s));
     CLOWNS_CUDA_TRY(cudaMemcpyAsync(b + L.o_gticket, zeros, sizeof(unsigned) * L.ngrp, cudaMemcpyHostToDevice, s));

@@ -2,28 +2,53 @@
 // src2LOWNS/pcgpme_para.F90:1-354) over a concatenation of independent systems.
 //
 // One solve of the reference is a batch of one member.  Members occupy disjoint,
-// tile-aligned row ranges of one row space; every kernel walks tiles of kTile
-// rows, looks up the tile's member, skips members whose solve has stopped, and
-// reduces dot products per member: the last tile of a member to finish sums
-// that member's tile partials in tile order (deterministic) and finalises its
-// scalars on the device.  Coefficients and Krylov vectors are stored as T
-// (double for the plain path, float for the inner solve of the mixed path);
-// all dot products and scalars are double.
+// tile-aligned row ranges of one row space; every kernel serves all members and
+// skips members whose solve has stopped.  Coefficients and Krylov vectors are
+// stored as T (double for the plain path, float for the inner solve of the
+// mixed path); all scalars are double.
+//
+// Dot products follow ONE summation tree, whichever kernel computes them (tile
+// or balanced kernels, 4 or 8 rows per thread, 64 or 128 threads per tile, the
+// persistent or the wavefront loop, a single system or a member of an
+// ensemble), so that a solve's iteration count and pressure do not depend on
+// the launch shape the autotuner picks:
+//   - chunk c of a member is its rows [128 c, 128 c + 128); lane l of the chunk
+//     folds the rows 128 c + 32 u + l, u = 0..3, in that order, with fused
+//     multiply-adds into a value of T's precision (rows past the member's end
+//     are not folded);
+//   - the chunk total is the xor butterfly of the 32 lane values (offsets 16,
+//     8, 4, 2, 1), converted to double;
+//   - group g is the chunks [64 g, 64 g + 64): lane l adds the totals of chunks
+//     l and l + 32 that exist, then the butterfly;
+//   - the member total: lane l sums the group totals l, l + 32, ... in order,
+//     then the butterfly.
+// Each add of a butterfly is commutative, so every lane ends with the same
+// bits, and a warp that reduces several chunks at once (a transposed butterfly,
+// warp_tsum) forms the same tree for each.  Whoever accounts the last chunk of a
+// group (a ticket per group) sums the group; whoever sums a member's last group
+// sums the member and finalises its scalars on the device.
 #pragma once
 
 #include "common.cuh"
 
 namespace clowns {
 
-constexpr int kTile = 512;           // rows per tile (multiple of kEngBlock)
+constexpr int kTile = 512;           // rows per tile (member ranges are tile-aligned)
 constexpr int kEngBlock = 256;
 constexpr int kRowsPerThread = 4;   // rows a thread handles per step (explicit ILP)
 constexpr int kStepBlock = kTile / kRowsPerThread;   // threads covering one tile in one step
 constexpr int kEngMaxGrid = kNumSMs * 8;
-constexpr int kGroupTiles = 64;    // tiles per first-level reduction group
+constexpr int kChunk = 128;         // rows of a reduction chunk: 32 lanes x 4 rows
+constexpr int kChunkRows = kChunk / 32;
+constexpr int kTileChunks = kTile / kChunk;
+constexpr int kGroupChunks = 64;    // chunks per reduction group
 constexpr int kWaveChunk = 16;     // tiles per completion counter of the wavefront loop
 constexpr int kWaveStages = 7;     // stages of each of the wavefront loop's two apply segments
 constexpr int kWaveBufs = 5;       // intermediate vectors of one operator application
+
+// Polls a device-wide wait makes before it gives up (seconds; no correct run
+// comes near it: a phase lasts microseconds to milliseconds).
+constexpr long kBarSpinLimit = 1L << 24;
 
 // Control block of the wavefront loop (single system).  D: the largest
 // distance, in tiles, between a row and a real (non-zero-row) neighbour it
@@ -89,25 +114,22 @@ struct Eng {
     double* r64;              // FP64 work vectors (mixed path)
     double* s64;
     double* t64;
-    const int* blk_member;    // member of each block (-1: none)
-    const int* blk_rows;      // real rows in each block (0: pad only)
-    const int* mem_off;       // first row of each member
+    const int* blk_member;    // member of each tile (-1: none)
+    const int* blk_rows;      // real rows in each tile (0: pad only)
+    const int* mem_off;       // first row of each member (a multiple of kTile)
     const int* mem_n;         // rows of each member
-    const int* mem_nblk;      // blocks with real rows per member
-    const int* mem_blk0;      // first block of each member
-    const int* blk_group;     // reduction group of each block with real rows
-    const int* grp_blk0;      // first block of each group
-    const int* grp_nblk;      // blocks in each group
-    const int* mem_grp0;      // first group of each member
-    const int* mem_ngrp;      // groups of each member
-    unsigned* gticket;        // one per group
+    const int* mem_nblk;      // tiles with real rows per member
+    const int* mem_blk0;      // first tile of each member
+    const int* mem_grp0;      // first reduction group of each member
+    const int* mem_ngrp;      // reduction groups of each member
+    unsigned* gticket;        // chunks accounted, one per group
     double* gpartials;        // 2 per group
     T* w[kWaveBufs];          // wavefront loop: intermediates of one application (single system)
     WaveCtl* wave;            // wavefront loop control (nullptr: not available)
     const MemberIn* in;       // per-member inputs (device copy of the table)
     MemberScalars* S;
-    double* partials;         // 2 per block
-    unsigned* ticket;         // one per member
+    double* partials;         // 2 per chunk of the row space (chunk totals)
+    unsigned* ticket;         // groups summed, one per member
     int* ctrl;                // [0] loop-body count, [1] max ITER over members, [2] bodies of earlier sweeps
     const BalBlock* baltab;   // ensembles: 16 block tables of the balanced kernels (nullptr: none)
     const int* balg;          // ensembles: the blocks of each table's launch (16)
@@ -120,18 +142,141 @@ struct Eng {
 // kernel boundary or by grid_sync, whose gpu-scope fence orders the block's
 // later loads after the other blocks' stores (the L1 is not a source of stale
 // lines across it).  Scalars and reduction partials, which can be written by
-// the last block of a member within the same phase, are read through L2
-// (ld.global.cg).
+// other blocks within the same phase, are read through L2 (ld.global.cg).
 
 template <typename V>
 __device__ __forceinline__ V ldg2(const V* p) { return *p; }
 
-// c - a b with one rounding (the sweeps' update, written out so that fused and
-// separate sweeps round identically)
-__device__ __forceinline__ double fnma(double a, double b, double c) { return __fma_rn(-a, b, c); }
-__device__ __forceinline__ float fnma(float a, float b, float c) { return __fmaf_rn(-a, b, c); }
+// Per-row arithmetic with explicit single roundings, so that every kernel that
+// evaluates a formula (tile, balanced, fused or not) rounds it identically.
+__device__ __forceinline__ double fma_rn(double a, double b, double c) { return __fma_rn(a, b, c); }
+__device__ __forceinline__ float fma_rn(float a, float b, float c) { return __fmaf_rn(a, b, c); }
+// c - a b with one rounding
+template <typename V>
+__device__ __forceinline__ V fnma(V a, V b, V c) { return fma_rn(-a, b, c); }
 __device__ __forceinline__ double sld(const double* p) { return __ldcg(p); }
 __device__ __forceinline__ int sld(const int* p) { return __ldcg(p); }
+
+// ---------------------------------------------------------------------------
+// The canonical reduction
+
+// Transposed xor butterfly of V values per lane (V a power of two <= 32): value
+// q of every lane is summed over the warp with the butterfly tree 16, 8, 4, 2, 1,
+// and each lane returns one of the V totals, number `idx` (from the lane's bits
+// 4, 3, ... : the same total sits in 32 / V lanes).  V = 1 is the plain
+// butterfly; V = 2 the pair sum (lanes 0-15: value 0, lanes 16-31: value 1).
+template <typename A, int V>
+__device__ __forceinline__ A warp_tsum(A (&v)[V], int& idx) {
+    const int lane = threadIdx.x & 31;
+    idx = 0;
+    int off = 16;
+#pragma unroll
+    for (int h = V / 2; h >= 1; h /= 2) {          // h values remain after this level
+        const bool hi = (lane & off) != 0;
+#pragma unroll
+        for (int j = 0; j < h; j++) {
+            const A keep = hi ? v[h + j] : v[j];
+            const A send = hi ? v[j] : v[h + j];
+            v[j] = keep + __shfl_xor_sync(0xffffffffu, send, off);
+        }
+        idx = 2 * idx + (hi ? 1 : 0);
+        off >>= 1;
+    }
+    A s = v[0];
+#pragma unroll
+    for (; off > 0; off >>= 1) s += __shfl_xor_sync(0xffffffffu, s, off);
+    return s;
+}
+
+// Record a chunk total (global chunk index gc, value k of NV) -- by one lane.
+template <typename T>
+__device__ __forceinline__ void put_chunk(const Eng<T>& E, long gc, int k, double v) {
+    E.partials[2 * gc + k] = v;
+    __threadfence();
+}
+
+// Reduce one chunk's lane values (NV = 1 or 2 per lane) and record its totals.
+// Every lane of the warp calls it.
+template <typename T, typename A, int NV>
+__device__ __forceinline__ void chunk_total(const Eng<T>& E, long gc, A (&v)[NV]) {
+    int idx;
+    const A s = warp_tsum<A, NV>(v, idx);
+    if ((threadIdx.x & (32 / NV - 1)) == 0) put_chunk(E, gc, idx, (double)s);
+}
+
+// Called by EVERY thread of the block once the block's writers recorded (and
+// fenced) the totals of member m's chunks [c0, c1) (member-relative; empty
+// allowed).  Accounts the chunks to their groups; the block that completes a
+// group sums it in one warp, and the warp that completes the member's last group
+// sums the member.  Returns true in all lanes of that warp, with the member
+// totals in tot[] (every lane); false elsewhere.
+template <typename T>
+__device__ __noinline__ bool account_chunks(const Eng<T>& E, int m, int c0, int c1, double (&tot)[2]) {
+    constexpr int kList = 256;
+    __shared__ int s_list[kList];
+    __shared__ int s_n;
+    const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5, nw = blockDim.x >> 5;
+    const int n = E.mem_n[m];
+    const int nc = (n + kChunk - 1) / kChunk;
+    const long gc0 = E.mem_off[m] / kChunk;
+    const int G0 = E.mem_grp0[m], ng = E.mem_ngrp[m];
+    bool fin = false;
+    const int g_lo = c1 > c0 ? c0 / kGroupChunks : 0;
+    const int g_hi = c1 > c0 ? (c1 - 1) / kGroupChunks : -1;
+    __syncthreads();                              // the block's chunk totals are written and fenced
+    for (int gb = g_lo; gb <= g_hi || gb == g_lo; gb += kList) {
+        if (threadIdx.x == 0) s_n = 0;
+        __syncthreads();
+        for (int g = gb + threadIdx.x; g <= g_hi && g < gb + kList; g += blockDim.x) {
+            const int cnt = min(c1, (g + 1) * kGroupChunks) - max(c0, g * kGroupChunks);
+            const int need = min(kGroupChunks, nc - g * kGroupChunks);
+            const unsigned old = atomicAdd(&E.gticket[G0 + g], (unsigned)cnt);
+            if (old + (unsigned)cnt == (unsigned)need) s_list[atomicAdd(&s_n, 1)] = g;
+        }
+        __syncthreads();
+        const int nd = s_n;
+        for (int q = wid; q < nd; q += nw) {
+            const int g = s_list[q];
+            __threadfence();
+            const long p0 = 2 * (gc0 + (long)g * kGroupChunks);
+            const int cg = min(kGroupChunks, nc - g * kGroupChunks);
+            double a = 0.0, b = 0.0;
+            if (lane < cg) {
+                a = __ldcg(E.partials + p0 + 2 * lane);
+                b = __ldcg(E.partials + p0 + 2 * lane + 1);
+            }
+            if (lane + 32 < cg) {
+                a += __ldcg(E.partials + p0 + 2 * (lane + 32));
+                b += __ldcg(E.partials + p0 + 2 * (lane + 32) + 1);
+            }
+            double s = warp_pair_sum(a, b);
+            if (lane == 0) E.gpartials[2L * (G0 + g) + 0] = s;
+            if (lane == 16) E.gpartials[2L * (G0 + g) + 1] = s;
+            if (lane == 0 || lane == 16) __threadfence();
+            __syncwarp();
+            unsigned last = 0;
+            if (lane == 0) {
+                E.gticket[G0 + g] = 0;
+                last = atomicAdd(&E.ticket[m], 1u) == (unsigned)ng - 1u;
+            }
+            if (__shfl_sync(0xffffffffu, last, 0)) {
+                __threadfence();
+                a = b = 0.0;
+                for (int j = lane; j < ng; j += 32) {
+                    a += __ldcg(E.gpartials + 2L * (G0 + j) + 0);
+                    b += __ldcg(E.gpartials + 2L * (G0 + j) + 1);
+                }
+                s = warp_pair_sum(a, b);
+                tot[0] = __shfl_sync(0xffffffffu, s, 0);
+                tot[1] = __shfl_sync(0xffffffffu, s, 16);
+                fin = true;
+            }
+        }
+        if (g_hi < gb + kList) break;
+        __syncthreads();                          // s_list is reused by the next round
+    }
+    return fin;
+}
 
 // ---------------------------------------------------------------------------
 // Tile walk helpers
@@ -159,73 +304,12 @@ __device__ __forceinline__ bool tile_active(const Eng<T>& E, int blk, int& m, lo
     return E.M == 1 || !done;
 }
 
-// Reduce (v0, v1) over the block and record the block's partial.  Two levels of
-// "last one sums": the last block of a group of kGroupTiles tiles sums the
-// group's partials, and the last group of member m sums the member's group
-// partials.  Per-thread values are summed over the warp in their own type A
-// (float for the FP32 inner solve, whose FP64 pipe is scarce on this GPU) and
-// across warps and blocks in double.  After the block-wide step only warp 0
-// continues (the other warps retire); returns true in warp 0 of the block that
-// completed member m, with tot[] holding the member totals in all its lanes.
-// Every sum uses a fixed assignment of terms to lanes and a fixed tree, so the
-// result is deterministic for a given layout and block size.  `red` holds 64
-// doubles.
-template <typename T, typename A>
-__device__ __forceinline__ bool member_reduce(const Eng<T>& E, int blk, int m, A v0, A v1, double* red,
-                                              double (&tot)[2]) {
-    const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5, nw = blockDim.x >> 5;
-    const A w = warp_pair_sum(v0, v1);
-    if (lane == 0) red[wid] = (double)w;
-    if (lane == 16) red[32 + wid] = (double)w;
-    __syncthreads();
-    double a = 0.0, b = 0.0;
-    if (wid == 0 && lane < nw) {
-        a = red[lane];
-        b = red[32 + lane];
-    }
-    __syncthreads();                       // red is free for the next tile
-    if (wid != 0) return false;
-    double s = warp_pair_sum(a, b);
-    const int g = E.blk_group[blk];
-    unsigned last = 0;
-    if (lane == 0) E.partials[2L * blk + 0] = s;
-    if (lane == 16) E.partials[2L * blk + 1] = s;
-    if (lane == 0 || lane == 16) __threadfence();
-    __syncwarp();
-    if (lane == 0) last = atomicAdd(&E.gticket[g], 1u) == (unsigned)E.grp_nblk[g] - 1u;
-    if (!__shfl_sync(0xffffffffu, last, 0)) return false;
-    __threadfence();
-    {
-        const int b0 = E.grp_blk0[g], nb = E.grp_nblk[g];
-        a = b = 0.0;
-        for (int q = lane; q < nb; q += 32) {
-            a += __ldcg(E.partials + 2L * (b0 + q) + 0);
-            b += __ldcg(E.partials + 2L * (b0 + q) + 1);
-        }
-        s = warp_pair_sum(a, b);
-        if (lane == 0) E.gpartials[2L * g + 0] = s;
-        if (lane == 16) E.gpartials[2L * g + 1] = s;
-        if (lane == 0 || lane == 16) __threadfence();
-        __syncwarp();
-        if (lane == 0) {
-            E.gticket[g] = 0;
-            last = atomicAdd(&E.ticket[m], 1u) == (unsigned)E.mem_ngrp[m] - 1u;
-        }
-    }
-    if (!__shfl_sync(0xffffffffu, last, 0)) return false;
-    __threadfence();
-    {
-        const int g0 = E.mem_grp0[m], ng = E.mem_ngrp[m];
-        a = b = 0.0;
-        for (int q = lane; q < ng; q += 32) {
-            a += __ldcg(E.gpartials + 2L * (g0 + q) + 0);
-            b += __ldcg(E.gpartials + 2L * (g0 + q) + 1);
-        }
-        s = warp_pair_sum(a, b);
-        tot[0] = __shfl_sync(0xffffffffu, s, 0);
-        tot[1] = __shfl_sync(0xffffffffu, s, 16);
-    }
-    return true;
+// Member-relative chunk range of a tile's real rows.
+template <typename T>
+__device__ __forceinline__ void tile_chunks(const Eng<T>& E, int m, long row0, int rows, int& c0, int& c1) {
+    const long off = E.M == 1 ? 0L : (long)E.mem_off[m];
+    c0 = (int)((row0 - off) / kChunk);
+    c1 = c0 + (rows + kChunk - 1) / kChunk;
 }
 
 __device__ __forceinline__ void stop_member(MemberScalars* S, int reason, int ier) {
@@ -444,7 +528,7 @@ __device__ __forceinline__ void tl_axsub(const Eng<T>& E, int blk, const T* __re
                     c[u] = ld_stream(E.ll + k * NV + i);
                 }
 #pragma unroll
-                for (int u = 0; u < R; u++) s[u] += a[u] * ldg2(in + c[u]);
+                for (int u = 0; u < R; u++) s[u] = fma_rn(a[u], ldg2(in + c[u]), s[u]);
             }
 #pragma unroll
             for (int u = 0; u < R; u++)
@@ -558,71 +642,80 @@ __device__ __forceinline__ void ph_sweep2(const Eng<T>& E, int k, const T* __res
     for (int blk = blockIdx.x; blk < E.nblk; blk += gridDim.x) tl_sweep2(E, blk, k, in, out);
 }
 
+// Rows of one chunk as lanes see them: warp-wide lane l takes rows
+// 32 u + l (u = 0..kChunkRows-1) of the chunk starting at tile row cr.
+
 // Last sweep (J=5,6, 306-318) with an optional fused per-member reduction:
 //   MODE 0 none; 1: RQ = (r0,out) -> ALP = C1/RQ; 2: AMU = (e,out)/(out,out)
-// Returns true in warp 0 of the block that finalised the member's scalars.
+// Warp w of the block takes the tile's chunks w, w + nw, ...  Returns true in
+// the one thread that finalised the member's scalars.
 template <typename T, int MODE>
-__device__ __forceinline__ bool tl_sweep56(const Eng<T>& E, int blk, const T* __restrict__ in, T* __restrict__ out,
-                                           double* red) {
+__device__ __forceinline__ bool tl_sweep56(const Eng<T>& E, int blk, const T* __restrict__ in, T* __restrict__ out) {
     const long NV = E.NV;
     const T* __restrict__ a5 = E.al + 4 * NV;
     const T* __restrict__ a6 = E.al + 5 * NV;
     const int* __restrict__ c5 = E.ll + 4 * NV;
     const int* __restrict__ c6 = E.ll + 5 * NV;
-    {
-        int m, rows;
-        long row0;
-        int done;
-        if (!tile_active(E, blk, m, row0, rows, done)) return false;
-        constexpr int R = kRowsPerThread;
-        T acc0 = T(0), acc1 = T(0);
-        for (int base = threadIdx.x; base < rows; base += blockDim.x * R) {
-            T a5v[R], a6v[R], xv[R], g5[R], g6[R];
-            int c5v[R], c6v[R];
-            bool ok[R];
+    int m, rows;
+    long row0;
+    int done;
+    if (!tile_active(E, blk, m, row0, rows, done)) return false;
+    constexpr int U = kChunkRows;
+    constexpr int NVAL = MODE == 2 ? 2 : 1;
+    const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5, nw = blockDim.x >> 5;
+    for (int q = wid; q < kTileChunks; q += nw) {
+        const int cr = q * kChunk;
+        if (cr >= rows) break;
+        T a5v[U], a6v[U], xv[U], g5[U], g6[U];
+        int c5v[U], c6v[U];
+        bool ok[U];
 #pragma unroll
-            for (int u = 0; u < R; u++) {
-                const int r = base + u * blockDim.x;
-                ok[u] = r < rows;
-                const long i = row0 + (ok[u] ? r : 0);
-                a5v[u] = ld_stream(a5 + i);
-                a6v[u] = ld_stream(a6 + i);
-                c5v[u] = ld_stream(c5 + i);
-                c6v[u] = ld_stream(c6 + i);
-                xv[u] = ldg2(in + i);
-            }
+        for (int u = 0; u < U; u++) {
+            const int r = cr + 32 * u + lane;
+            ok[u] = r < rows;
+            const long i = row0 + (ok[u] ? r : cr);
+            a5v[u] = ld_stream(a5 + i);
+            a6v[u] = ld_stream(a6 + i);
+            c5v[u] = ld_stream(c5 + i);
+            c6v[u] = ld_stream(c6 + i);
+            xv[u] = ldg2(in + i);
+        }
 #pragma unroll
-            for (int u = 0; u < R; u++) {
-                g5[u] = ldg2(in + c5v[u]);
-                g6[u] = ldg2(in + c6v[u]);
-            }
+        for (int u = 0; u < U; u++) {
+            g5[u] = ldg2(in + c5v[u]);
+            g6[u] = ldg2(in + c6v[u]);
+        }
+        T acc[NVAL];
 #pragma unroll
-            for (int u = 0; u < R; u++) {
-                if (!ok[u] || done) continue;
-                const long i = row0 + base + u * blockDim.x;
-                const T y = fnma(a6v[u], g6[u], fnma(a5v[u], g5[u], xv[u]));
-                out[i] = y;
-                if (MODE == 1) acc0 += ldg2(E.r0 + i) * y;
-                if (MODE == 2) { acc0 += ldg2(E.e + i) * y; acc1 += y * y; }
+        for (int k = 0; k < NVAL; k++) acc[k] = T(0);
+#pragma unroll
+        for (int u = 0; u < U; u++) {
+            if (!ok[u] || done) continue;
+            const long i = row0 + cr + 32 * u + lane;
+            const T y = fnma(a6v[u], g6[u], fnma(a5v[u], g5[u], xv[u]));
+            out[i] = y;
+            if (MODE == 1) acc[0] = fma_rn(ldg2(E.r0 + i), y, acc[0]);
+            if (MODE == 2) {
+                acc[0] = fma_rn(ldg2(E.e + i), y, acc[0]);
+                acc[NVAL - 1] = fma_rn(y, y, acc[NVAL - 1]);
             }
         }
-        if (MODE == 0 || done) return false;
-        double tot[2];
-        if (!member_reduce(E, blk, m, acc0, acc1, red, tot)) return false;
-        if (threadIdx.x == 0) {
-            E.ticket[m] = 0;
-            finish_sweep56<MODE>(E.S + m, tot);
-            __threadfence();
-        }
-        __syncwarp();
-        return true;
+        if (MODE != 0 && !done) chunk_total(E, (row0 + cr) / kChunk, acc);
     }
+    if (MODE == 0 || done) return false;
+    int c0, c1;
+    tile_chunks(E, m, row0, rows, c0, c1);
+    double tot[2];
+    if (!account_chunks(E, m, c0, c1, tot) || lane != 0) return false;
+    E.ticket[m] = 0;
+    finish_sweep56<MODE>(E.S + m, tot);
+    __threadfence();
+    return true;
 }
 
 template <typename T, int MODE>
 __device__ __forceinline__ void ph_sweep56(const Eng<T>& E, const T* __restrict__ in, T* __restrict__ out) {
-    __shared__ double red[64];
-    for (int blk = blockIdx.x; blk < E.nblk; blk += gridDim.x) tl_sweep56<T, MODE>(E, blk, in, out, red);
+    for (int blk = blockIdx.x; blk < E.nblk; blk += gridDim.x) tl_sweep56<T, MODE>(E, blk, in, out);
 }
 
 // E = R - ALP Q  (171-175)
@@ -647,7 +740,7 @@ __device__ __forceinline__ void tl_eupdate(const Eng<T>& E, int blk) {
 #pragma unroll
             for (int u = 0; u < R; u++) {
                 const int r = base + u * blockDim.x;
-                if (r < rows && !done) E.e[row0 + r] = rv[u] - ALP * qv[u];
+                if (r < rows && !done) E.e[row0 + r] = fnma(ALP, qv[u], rv[u]);
             }
         }
     }
@@ -659,59 +752,60 @@ __device__ __forceinline__ void ph_eupdate(const Eng<T>& E) {
 }
 
 // X += ALP P + AMU E ; R = E - AMU V ; RN = (R,R) ; C1 = (R0,R)  (199-213),
-// then ERR and the stop tests (215-241).
-// Returns true in warp 0 of the block that finalised the member's scalars.
+// then ERR and the stop tests (215-241).  Warp w takes the tile's chunks w,
+// w + nw, ...  Returns true in the one thread that finalised the member's
+// scalars.
 template <typename T>
-__device__ __forceinline__ bool tl_xrupdate(const Eng<T>& E, int blk, double* red) {
-    {
-        int m, rows;
-        long row0;
-        int done;
-        if (!tile_active(E, blk, m, row0, rows, done)) return false;
-        const T ALP = T(sld(&E.S[m].ALP)), AMU = T(sld(&E.S[m].AMU));
-        T acc0 = T(0), acc1 = T(0);
-        constexpr int R = kRowsPerThread;
-        for (int base = threadIdx.x; base < rows; base += blockDim.x * R) {
-            T ev[R], xv[R], pv[R], vv[R], r0v[R];
+__device__ __forceinline__ bool tl_xrupdate(const Eng<T>& E, int blk) {
+    int m, rows;
+    long row0;
+    int done;
+    if (!tile_active(E, blk, m, row0, rows, done)) return false;
+    const T ALP = T(sld(&E.S[m].ALP)), AMU = T(sld(&E.S[m].AMU));
+    constexpr int U = kChunkRows;
+    const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5, nw = blockDim.x >> 5;
+    for (int q = wid; q < kTileChunks; q += nw) {
+        const int cr = q * kChunk;
+        if (cr >= rows) break;
+        T ev[U], xv[U], pv[U], vv[U], r0v[U];
 #pragma unroll
-            for (int u = 0; u < R; u++) {
-                const int r = base + u * blockDim.x;
-                const long i = row0 + (r < rows ? r : 0);
-                ev[u] = ldg2(E.e + i);
-                xv[u] = ldg2(E.xi + i);
-                pv[u] = ldg2(E.p + i);
-                vv[u] = ldg2(E.v + i);
-                r0v[u] = ldg2(E.r0 + i);
-            }
+        for (int u = 0; u < U; u++) {
+            const int r = cr + 32 * u + lane;
+            const long i = row0 + (r < rows ? r : cr);
+            ev[u] = ldg2(E.e + i);
+            xv[u] = ldg2(E.xi + i);
+            pv[u] = ldg2(E.p + i);
+            vv[u] = ldg2(E.v + i);
+            r0v[u] = ldg2(E.r0 + i);
+        }
+        T acc[2] = {T(0), T(0)};
 #pragma unroll
-            for (int u = 0; u < R; u++) {
-                const int r = base + u * blockDim.x;
-                if (r >= rows || done) continue;
-                const long i = row0 + r;
-                E.xi[i] = xv[u] + ALP * pv[u] + AMU * ev[u];
-                const T rn = ev[u] - AMU * vv[u];
-                E.r[i] = rn;
-                acc0 += rn * rn;
-                acc1 += rn * r0v[u];
-            }
+        for (int u = 0; u < U; u++) {
+            const int r = cr + 32 * u + lane;
+            if (r >= rows || done) continue;
+            const long i = row0 + r;
+            E.xi[i] = fma_rn(AMU, ev[u], fma_rn(ALP, pv[u], xv[u]));
+            const T rn = fnma(AMU, vv[u], ev[u]);
+            E.r[i] = rn;
+            acc[0] = fma_rn(rn, rn, acc[0]);
+            acc[1] = fma_rn(rn, r0v[u], acc[1]);
         }
-        if (done) return false;
-        double tot[2];
-        if (!member_reduce(E, blk, m, acc0, acc1, red, tot)) return false;
-        if (threadIdx.x == 0) {
-            E.ticket[m] = 0;
-            finish_xrupdate(E.S + m, tot);
-            __threadfence();
-        }
-        __syncwarp();
-        return true;
+        if (!done) chunk_total(E, (row0 + cr) / kChunk, acc);
     }
+    if (done) return false;
+    int c0, c1;
+    tile_chunks(E, m, row0, rows, c0, c1);
+    double tot[2];
+    if (!account_chunks(E, m, c0, c1, tot) || lane != 0) return false;
+    E.ticket[m] = 0;
+    finish_xrupdate(E.S + m, tot);
+    __threadfence();
+    return true;
 }
 
 template <typename T>
 __device__ __forceinline__ void ph_xrupdate(const Eng<T>& E) {
-    __shared__ double red[64];
-    for (int blk = blockIdx.x; blk < E.nblk; blk += gridDim.x) tl_xrupdate(E, blk, red);
+    for (int blk = blockIdx.x; blk < E.nblk; blk += gridDim.x) tl_xrupdate(E, blk);
 }
 
 // P = R + BETA (P - AMU Q)  (242-246)
@@ -737,7 +831,7 @@ __device__ __forceinline__ void tl_pupdate(const Eng<T>& E, int blk) {
 #pragma unroll
             for (int u = 0; u < R; u++) {
                 const int r = base + u * blockDim.x;
-                if (r < rows && !done) E.p[row0 + r] = rv[u] + BETA * (pv[u] - AMU * qv[u]);
+                if (r < rows && !done) E.p[row0 + r] = fma_rn(BETA, fnma(AMU, qv[u], pv[u]), rv[u]);
             }
         }
     }
@@ -749,35 +843,42 @@ __device__ __forceinline__ void ph_pupdate(const Eng<T>& E) {
 }
 
 // BN = (b^,b^); R = b^ - q; C1 = (R,R); P = R0 = R  (129-145).  p holds b^ = PM W b
-// and q holds PM A x0 on entry.
+// and q holds PM A x0 on entry.  Warp w takes the tile's chunks w, w + nw, ...
 template <typename T>
 __device__ __forceinline__ void ph_initres(const Eng<T>& E) {
-    __shared__ double red[64];
+    const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5, nw = blockDim.x >> 5;
     for (int blk = blockIdx.x; blk < E.nblk; blk += gridDim.x) {
         int m, rows;
         long row0;
         int done;
         if (!tile_active(E, blk, m, row0, rows, done) || done) continue;
-        T acc0 = T(0), acc1 = T(0);
-        for (int r = threadIdx.x; r < rows; r += blockDim.x) {
-            const long i = row0 + r;
-            T temp = ldg2(E.p + i);
-            acc0 += temp * temp;
-            temp = temp - ldg2(E.q + i);
-            E.r[i] = temp;
-            acc1 += temp * temp;
-            E.p[i] = temp;
-            E.r0[i] = temp;
+        for (int q = wid; q < kTileChunks; q += nw) {
+            const int cr = q * kChunk;
+            if (cr >= rows) break;
+            T acc[2] = {T(0), T(0)};
+#pragma unroll
+            for (int u = 0; u < kChunkRows; u++) {
+                const int r = cr + 32 * u + lane;
+                if (r >= rows) continue;
+                const long i = row0 + r;
+                T temp = ldg2(E.p + i);
+                acc[0] = fma_rn(temp, temp, acc[0]);
+                temp = temp - ldg2(E.q + i);
+                E.r[i] = temp;
+                acc[1] = fma_rn(temp, temp, acc[1]);
+                E.p[i] = temp;
+                E.r0[i] = temp;
+            }
+            chunk_total(E, (row0 + cr) / kChunk, acc);
         }
+        int c0, c1;
+        tile_chunks(E, m, row0, rows, c0, c1);
         double tot[2];
-        if (!member_reduce(E, blk, m, acc0, acc1, red, tot)) continue;
-        if (threadIdx.x == 0) {
-            E.ticket[m] = 0;
-            E.S[m].BN = tot[0];
-            E.S[m].C1 = tot[1];
-            __threadfence();
-        }
-        __syncwarp();
+        if (!account_chunks(E, m, c0, c1, tot) || lane != 0) continue;
+        E.ticket[m] = 0;
+        E.S[m].BN = tot[0];
+        E.S[m].C1 = tot[1];
+        __threadfence();
     }
 }
 
@@ -845,19 +946,17 @@ __global__ void __launch_bounds__(kEngBlock) k_eng_initres(Eng<T> E) {
 // ---------------------------------------------------------------------------
 // Balanced kernels.  The iteration's kernels can instead run as exactly one
 // wave each: G = (resident blocks per SM) x SMs blocks, block b owning the
-// rows [n b / G, n (b+1) / G) and walking them R rows per thread per step.  An
+// chunks [nc b / G, nc (b+1) / G) of its member (nc = its 128-row chunks).  An
 // ensemble splits the G blocks over its members still iterating in proportion
 // to their rows, at least one block each, by a table (BalBlock per block) that
 // bal_rebuild writes on the device; blocks of a stopped member return before
 // loading anything.  Every block then does the same work and all retire
 // together, and the per-block costs -- launch, the stop-flag and scalar loads,
 // the reduction tail -- are paid G times per kernel instead of once per
-// 512-row tile (5517 times at 2.8 M rows).  The per-row arithmetic is the tile kernels'; dot
-// products are reduced once per block: the block's partial goes to
-// partials[b], and the last block of a member to finish sums the member's
-// partials in index order (deterministic for a given G) and finalises its
-// scalars.  Callers keep G at most nblk (the partials hold two values per
-// tile) and at least the number of members.
+// 512-row tile (5517 times at 2.8 M rows).  The per-row arithmetic is the tile
+// kernels'.  The dot-product kernels give warp w the block's chunks w, w + 8, ...
+// (R / 4 adjacent chunks per step), fold them as the canonical reduction
+// prescribes, and sum four chunks at a time with one transposed butterfly.
 //
 // For a single system only the kernels whose results outlive a stop test read
 // the stop flag: sweep56 (its reduction and finalisation) and xrupdate (x, r
@@ -868,13 +967,12 @@ __global__ void __launch_bounds__(kEngBlock) k_eng_initres(Eng<T> E) {
 // barrier; each thread loads them, and the load overlaps its data loads.)
 // FP64 kernels at 4 rows per thread are held to 85 registers (3 blocks per SM).
 
-// This block's member and rows.  tab == nullptr: a single system, every block
-// belongs to member 0.  Returns false for a block of an ensemble member that
-// has stopped.
+// This block's member, the member's first row and rows, and its chunk range.
+// tab == nullptr: a single system, every block belongs to member 0.  Returns
+// false for a block of an ensemble member that has stopped.
 template <typename T>
 __device__ __forceinline__ bool bal_block(const Eng<T>& E, const BalBlock* __restrict__ tab, BalBlock& bb,
-                                          long& lo, long& hi) {
-    long off, n;
+                                          long& off, int& n, int& c0, int& c1) {
     if (!tab) {
         bb.m = 0;
         bb.j = blockIdx.x;
@@ -887,57 +985,38 @@ __device__ __forceinline__ bool bal_block(const Eng<T>& E, const BalBlock* __res
         off = E.mem_off[bb.m];
         n = E.mem_n[bb.m];
     }
-    lo = off + n * (long)bb.j / (long)bb.gm;
-    hi = off + n * (long)(bb.j + 1) / (long)bb.gm;
+    const long nc = (n + kChunk - 1) / kChunk;
+    c0 = (int)(nc * bb.j / bb.gm);
+    c1 = (int)(nc * (bb.j + 1) / bb.gm);
     return !tab || !sld(&E.S[bb.m].done);
 }
 
-template <typename T, int R>
-constexpr int kBalMinBlocks = sizeof(T) == 8 && R == 4 ? 3 : 1;
-
-// Block partial of (v0, v1), then the last block of the member sums the
-// member's partials; true in every thread of that block, with the totals in
-// tot[] of warp 0.
-template <typename T, typename A>
-__device__ __forceinline__ bool bal_reduce(const Eng<T>& E, const BalBlock& bb, A v0, A v1, double* red,
-                                           double (&tot)[2]) {
-    __shared__ int s_last;
-    const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5, nw = blockDim.x >> 5;
-    const A w = warp_pair_sum(v0, v1);
-    if (lane == 0) red[wid] = (double)w;
-    if (lane == 16) red[32 + wid] = (double)w;
-    __syncthreads();
-    if (wid == 0) {
-        const double a = lane < nw ? red[lane] : 0.0, b = lane < nw ? red[32 + lane] : 0.0;
-        const double s = warp_pair_sum(a, b);
-        if (lane == 0) E.partials[2L * blockIdx.x + 0] = s;
-        if (lane == 16) E.partials[2L * blockIdx.x + 1] = s;
-        if (lane == 0 || lane == 16) __threadfence();
-        __syncwarp();
-        if (lane == 0) s_last = atomicAdd(&E.ticket[bb.m], 1u) == (unsigned)bb.gm - 1u;
-    }
-    __syncthreads();
-    if (!s_last) return false;
-    __threadfence();
-    double a = 0.0, b = 0.0;
-    for (int q = threadIdx.x; q < bb.gm; q += blockDim.x) {
-        a += __ldcg(E.partials + 2L * (bb.b0 + q) + 0);
-        b += __ldcg(E.partials + 2L * (bb.b0 + q) + 1);
-    }
-    const double w2 = warp_pair_sum(a, b);
-    __syncthreads();                          // every warp has read red[] above
-    if (lane == 0) red[wid] = w2;
-    if (lane == 16) red[32 + wid] = w2;
-    __syncthreads();
-    if (wid == 0) {
-        a = lane < nw ? red[lane] : 0.0;
-        b = lane < nw ? red[32 + lane] : 0.0;
-        const double s = warp_pair_sum(a, b);
-        tot[0] = __shfl_sync(0xffffffffu, s, 0);
-        tot[1] = __shfl_sync(0xffffffffu, s, 16);
-    }
-    return true;
+// Row range of the same block.
+template <typename T>
+__device__ __forceinline__ bool bal_rows(const Eng<T>& E, const BalBlock* __restrict__ tab, BalBlock& bb, long& lo,
+                                         long& hi) {
+    long off;
+    int n, c0, c1;
+    const bool go = bal_block(E, tab, bb, off, n, c0, c1);
+    lo = off + (long)c0 * kChunk;
+    hi = off + min((long)n, (long)c1 * kChunk);
+    return go;
 }
+
+template <typename T, int R>
+constexpr int kBalMinBlocks = R == 4 ? (sizeof(T) == 8 ? 3 : 4) : 1;
+
+// Chunks per transposed butterfly in the balanced dot-product kernels: four
+// (2.25 additions per chunk and value pair instead of five), one for the FP64
+// x/r update at 4 rows per thread, whose loads already fill its 80 registers
+// (a batch of two spills).
+template <typename T, int R, int NVAL>
+constexpr int kBalBatch = (sizeof(T) == 8 && R == 4 && NVAL == 2) ? 1 : 4;
+
+// Keeps the compiler from hoisting the next step's loads above this step's
+// stores: each step keeps its own window of R rows in flight, as the kernels'
+// register budgets assume.
+__device__ __forceinline__ void step_fence() { asm volatile("" ::: "memory"); }
 
 // NL: the columns the matrix fills (6, or 4 for a 2DH system, whose two empty
 // columns hold zero coefficients at the zero row and are not read).
@@ -947,7 +1026,7 @@ __global__ void __launch_bounds__(kEngBlock, kBalMinBlocks<T, R>) k_bal_axsub(En
     const long NV = E.NV;
     long lo, hi;
     BalBlock bb;
-    if (!bal_block(E, tab, bb, lo, hi)) return;
+    if (!bal_rows(E, tab, bb, lo, hi)) return;
     for (long base = lo + threadIdx.x; base < hi; base += (long)blockDim.x * R) {
         T s[R];
         bool ok[R];
@@ -969,7 +1048,7 @@ __global__ void __launch_bounds__(kEngBlock, kBalMinBlocks<T, R>) k_bal_axsub(En
                 c[u] = ld_stream(E.ll + k * NV + i);
             }
 #pragma unroll
-            for (int u = 0; u < R; u++) s[u] += a[u] * ldg2(in + c[u]);
+            for (int u = 0; u < R; u++) s[u] = fma_rn(a[u], ldg2(in + c[u]), s[u]);
         }
 #pragma unroll
         for (int u = 0; u < R; u++)
@@ -986,7 +1065,7 @@ __global__ void __launch_bounds__(kEngBlock, kBalMinBlocks<T, R>) k_bal_sweep(En
     const int* __restrict__ c = E.ll + k * NV;
     long lo, hi;
     BalBlock bb;
-    if (!bal_block(E, tab, bb, lo, hi)) return;
+    if (!bal_rows(E, tab, bb, lo, hi)) return;
     for (long base = lo + threadIdx.x; base < hi; base += (long)blockDim.x * R) {
         T av[R], xv[R], gv[R];
         int cv[R];
@@ -1020,7 +1099,7 @@ __global__ void __launch_bounds__(kEngBlock, kBalMinBlocks<T, R>) k_bal_sweep2(E
     const int* __restrict__ c1 = c0 + NV;
     long lo, hi;
     BalBlock bb;
-    if (!bal_block(E, tab, bb, lo, hi)) return;
+    if (!bal_rows(E, tab, bb, lo, hi)) return;
     for (long base = lo + threadIdx.x; base < hi; base += (long)blockDim.x * R) {
         T x[R], aa[R], ab[R], xj[R], aj[R];
         int ca[R], cb[R], cj[R];
@@ -1054,65 +1133,96 @@ __global__ void __launch_bounds__(kEngBlock, kBalMinBlocks<T, R>) k_bal_sweep2(E
     }
 }
 
+// Sum the batch's lane values (kBalBatch chunks x NVAL values) with one
+// transposed butterfly and record the chunk totals.  Slot q of the batch is the
+// chunk c0 + (8 (s0 + q / CPS) + w) CPS + q % CPS of the block's member.
+template <typename T, int NVAL, int CPS, int B>
+__device__ __forceinline__ void bal_flush(const Eng<T>& E, T (&v)[B * NVAL], long gc_member, int c0,
+                                          int c1, int s0, int w, int nwarps) {
+    constexpr int V = B * NVAL;
+    int idx;
+    const T s = warp_tsum<T, V>(v, idx);
+    const int q = idx / NVAL, k = idx % NVAL;
+    const int cc = c0 + (nwarps * (s0 + q / CPS) + w) * CPS + q % CPS;
+    if ((threadIdx.x & (32 / V - 1)) == 0 && cc < c1) put_chunk(E, gc_member + cc, k, (double)s);
+}
+
 // sweeps 5, 6 with the RQ (MODE 1) or AMU (MODE 2) reduction (as tl_sweep56);
 // NL = 4: a copy with the reduction
 template <typename T, int MODE, int R, int NL>
 __global__ void __launch_bounds__(kEngBlock, kBalMinBlocks<T, R>) k_bal_sweep56(Eng<T> E, const BalBlock* __restrict__ tab, const T* __restrict__ in, T* __restrict__ out) {
     pdl_enter();
-    __shared__ double red[64];
     const long NV = E.NV;
     const T* __restrict__ a5 = E.al + 4 * NV;
     const T* __restrict__ a6 = E.al + 5 * NV;
     const int* __restrict__ c5 = E.ll + 4 * NV;
     const int* __restrict__ c6 = E.ll + 5 * NV;
-    long lo, hi;
     BalBlock bb;
-    if (!bal_block(E, tab, bb, lo, hi)) return;
+    long off;
+    int n, c0, c1;
+    if (!bal_block(E, tab, bb, off, n, c0, c1)) return;
     const int done = sld(&E.S[bb.m].done);
-    T acc0 = T(0), acc1 = T(0);
-    for (long base = lo + threadIdx.x; base < hi; base += (long)blockDim.x * R) {
-        T a5v[R], a6v[R], xv[R], g5[R], g6[R];
-        int c5v[R], c6v[R];
-        bool ok[R];
-        constexpr bool six = NL == 6;                 // NL = 4: sweeps 5 and 6 are empty, out = in
+    constexpr int CPS = R / kChunkRows;              // chunks per warp and step
+    constexpr int NVAL = MODE == 2 ? 2 : 1;
+    constexpr int B = kBalBatch<T, R, NVAL>;
+    constexpr int SPB = B / CPS;                     // steps per batch
+    constexpr bool six = NL == 6;                    // NL = 4: sweeps 5 and 6 are empty, out = in
+    const int lane = threadIdx.x & 31, w = threadIdx.x >> 5, nwarps = blockDim.x >> 5;
+    const long gcm = off / kChunk;
+    for (int s0 = 0; c0 + (nwarps * s0 + w) * CPS < c1; s0 += SPB) {
+        T v[B * NVAL];
 #pragma unroll
-        for (int u = 0; u < R; u++) {
-            const long r = base + (long)u * blockDim.x;
-            ok[u] = r < hi;
-            const long i = ok[u] ? r : lo;
-            if (six) {
-                a5v[u] = ld_stream(a5 + i);
-                a6v[u] = ld_stream(a6 + i);
-                c5v[u] = ld_stream(c5 + i);
-                c6v[u] = ld_stream(c6 + i);
-            }
-            xv[u] = ldg2(in + i);
-        }
-        if (six) {
+        for (int q = 0; q < B * NVAL; q++) v[q] = T(0);
+#pragma unroll
+        for (int st = 0; st < SPB; st++) {
+            const int cb = c0 + (nwarps * (s0 + st) + w) * CPS;
+            T a5v[R], a6v[R], xv[R], g5[R], g6[R];
+            int c5v[R], c6v[R];
+            bool ok[R];
 #pragma unroll
             for (int u = 0; u < R; u++) {
-                g5[u] = ldg2(in + c5v[u]);
-                g6[u] = ldg2(in + c6v[u]);
+                const int cc = cb + u / kChunkRows;
+                const long r = (long)cc * kChunk + 32 * (u % kChunkRows) + lane;
+                ok[u] = cc < c1 && r < n;
+                const long i = off + (ok[u] ? r : 0);
+                if (six) {
+                    a5v[u] = ld_stream(a5 + i);
+                    a6v[u] = ld_stream(a6 + i);
+                    c5v[u] = ld_stream(c5 + i);
+                    c6v[u] = ld_stream(c6 + i);
+                }
+                xv[u] = ldg2(in + i);
             }
-        }
+            if (six) {
 #pragma unroll
-        for (int u = 0; u < R; u++) {
-            if (!ok[u] || done) continue;
-            const long i = base + (long)u * blockDim.x;
-            const T y = six ? fnma(a6v[u], g6[u], fnma(a5v[u], g5[u], xv[u])) : xv[u];
-            out[i] = y;
-            if (MODE == 1) acc0 += ldg2(E.r0 + i) * y;
-            if (MODE == 2) { acc0 += ldg2(E.e + i) * y; acc1 += y * y; }
+                for (int u = 0; u < R; u++) {
+                    g5[u] = ldg2(in + c5v[u]);
+                    g6[u] = ldg2(in + c6v[u]);
+                }
+            }
+#pragma unroll
+            for (int u = 0; u < R; u++) {
+                if (!ok[u] || done) continue;
+                const long i = off + (long)(cb + u / kChunkRows) * kChunk + 32 * (u % kChunkRows) + lane;
+                const T y = six ? fnma(a6v[u], g6[u], fnma(a5v[u], g5[u], xv[u])) : xv[u];
+                out[i] = y;
+                const int q = (st * CPS + u / kChunkRows) * NVAL;
+                if (MODE == 1) v[q] = fma_rn(ldg2(E.r0 + i), y, v[q]);
+                if (MODE == 2) {
+                    v[q] = fma_rn(ldg2(E.e + i), y, v[q]);
+                    v[q + NVAL - 1] = fma_rn(y, y, v[q + NVAL - 1]);
+                }
+            }
+            step_fence();
         }
+        if (MODE != 0 && !done) bal_flush<T, NVAL, CPS, B>(E, v, gcm, c0, c1, s0, w, nwarps);
     }
     if (MODE == 0 || done) return;
     double tot[2];
-    if (!bal_reduce(E, bb, acc0, acc1, red, tot)) return;
-    if (threadIdx.x == 0) {
-        E.ticket[bb.m] = 0;
-        finish_sweep56<MODE>(E.S + bb.m, tot);
-        __threadfence();
-    }
+    if (!account_chunks(E, bb.m, c0, c1, tot) || lane != 0) return;
+    E.ticket[bb.m] = 0;
+    finish_sweep56<MODE>(E.S + bb.m, tot);
+    __threadfence();
 }
 
 template <typename T, int R>
@@ -1120,7 +1230,7 @@ __global__ void __launch_bounds__(kEngBlock, kBalMinBlocks<T, R>) k_bal_eupdate(
     pdl_enter();
     long lo, hi;
     BalBlock bb;
-    if (!bal_block(E, tab, bb, lo, hi)) return;
+    if (!bal_rows(E, tab, bb, lo, hi)) return;
     const T ALP = T(sld(&E.S[bb.m].ALP));
     for (long base = lo + threadIdx.x; base < hi; base += (long)blockDim.x * R) {
         T rv[R], qv[R];
@@ -1134,7 +1244,7 @@ __global__ void __launch_bounds__(kEngBlock, kBalMinBlocks<T, R>) k_bal_eupdate(
 #pragma unroll
         for (int u = 0; u < R; u++) {
             const long r = base + (long)u * blockDim.x;
-            if (r < hi) E.e[r] = rv[u] - ALP * qv[u];
+            if (r < hi) E.e[r] = fnma(ALP, qv[u], rv[u]);
         }
     }
 }
@@ -1142,44 +1252,59 @@ __global__ void __launch_bounds__(kEngBlock, kBalMinBlocks<T, R>) k_bal_eupdate(
 template <typename T, int R>
 __global__ void __launch_bounds__(kEngBlock, kBalMinBlocks<T, R>) k_bal_xrupdate(Eng<T> E, const BalBlock* __restrict__ tab) {
     pdl_enter();
-    __shared__ double red[64];
-    long lo, hi;
     BalBlock bb;
-    if (!bal_block(E, tab, bb, lo, hi)) return;
+    long off;
+    int n, c0, c1;
+    if (!bal_block(E, tab, bb, off, n, c0, c1)) return;
     const int done = sld(&E.S[bb.m].done);
     const T ALP = T(sld(&E.S[bb.m].ALP)), AMU = T(sld(&E.S[bb.m].AMU));
-    T acc0 = T(0), acc1 = T(0);
-    for (long base = lo + threadIdx.x; base < hi; base += (long)blockDim.x * R) {
-        T ev[R], xv[R], pv[R], vv[R], r0v[R];
+    constexpr int CPS = R / kChunkRows;
+    constexpr int B = kBalBatch<T, R, 2>;
+    constexpr int SPB = B / CPS;
+    const int lane = threadIdx.x & 31, w = threadIdx.x >> 5, nwarps = blockDim.x >> 5;
+    const long gcm = off / kChunk;
+    for (int s0 = 0; c0 + (nwarps * s0 + w) * CPS < c1; s0 += SPB) {
+        T v[B * 2];
 #pragma unroll
-        for (int u = 0; u < R; u++) {
-            const long r = base + (long)u * blockDim.x;
-            const long i = r < hi ? r : lo;
-            ev[u] = ldg2(E.e + i);
-            xv[u] = ldg2(E.xi + i);
-            pv[u] = ldg2(E.p + i);
-            vv[u] = ldg2(E.v + i);
-            r0v[u] = ldg2(E.r0 + i);
-        }
+        for (int q = 0; q < B * 2; q++) v[q] = T(0);
 #pragma unroll
-        for (int u = 0; u < R; u++) {
-            const long r = base + (long)u * blockDim.x;
-            if (r >= hi || done) continue;
-            E.xi[r] = xv[u] + ALP * pv[u] + AMU * ev[u];
-            const T rn = ev[u] - AMU * vv[u];
-            E.r[r] = rn;
-            acc0 += rn * rn;
-            acc1 += rn * r0v[u];
+        for (int st = 0; st < SPB; st++) {
+            const int cb = c0 + (nwarps * (s0 + st) + w) * CPS;
+            T ev[R], xv[R], pv[R], vv[R], r0v[R];
+            bool ok[R];
+#pragma unroll
+            for (int u = 0; u < R; u++) {
+                const int cc = cb + u / kChunkRows;
+                const long r = (long)cc * kChunk + 32 * (u % kChunkRows) + lane;
+                ok[u] = cc < c1 && r < n;
+                const long i = off + (ok[u] ? r : 0);
+                ev[u] = ldg2(E.e + i);
+                xv[u] = ldg2(E.xi + i);
+                pv[u] = ldg2(E.p + i);
+                vv[u] = ldg2(E.v + i);
+                r0v[u] = ldg2(E.r0 + i);
+            }
+#pragma unroll
+            for (int u = 0; u < R; u++) {
+                if (!ok[u] || done) continue;
+                const long i = off + (long)(cb + u / kChunkRows) * kChunk + 32 * (u % kChunkRows) + lane;
+                E.xi[i] = fma_rn(AMU, ev[u], fma_rn(ALP, pv[u], xv[u]));
+                const T rn = fnma(AMU, vv[u], ev[u]);
+                E.r[i] = rn;
+                const int q = (st * CPS + u / kChunkRows) * 2;
+                v[q] = fma_rn(rn, rn, v[q]);
+                v[q + 1] = fma_rn(rn, r0v[u], v[q + 1]);
+            }
+            step_fence();
         }
+        if (!done) bal_flush<T, 2, CPS, B>(E, v, gcm, c0, c1, s0, w, nwarps);
     }
     if (done) return;
     double tot[2];
-    if (!bal_reduce(E, bb, acc0, acc1, red, tot)) return;
-    if (threadIdx.x == 0) {
-        E.ticket[bb.m] = 0;
-        finish_xrupdate(E.S + bb.m, tot);
-        __threadfence();
-    }
+    if (!account_chunks(E, bb.m, c0, c1, tot) || lane != 0) return;
+    E.ticket[bb.m] = 0;
+    finish_xrupdate(E.S + bb.m, tot);
+    __threadfence();
 }
 
 template <typename T, int R>
@@ -1187,7 +1312,7 @@ __global__ void __launch_bounds__(kEngBlock, kBalMinBlocks<T, R>) k_bal_pupdate(
     pdl_enter();
     long lo, hi;
     BalBlock bb;
-    if (!bal_block(E, tab, bb, lo, hi)) return;
+    if (!bal_rows(E, tab, bb, lo, hi)) return;
     const T BETA = T(sld(&E.S[bb.m].BETA)), AMU = T(sld(&E.S[bb.m].AMU));
     for (long base = lo + threadIdx.x; base < hi; base += (long)blockDim.x * R) {
         T rv[R], pv[R], qv[R];
@@ -1202,7 +1327,7 @@ __global__ void __launch_bounds__(kEngBlock, kBalMinBlocks<T, R>) k_bal_pupdate(
 #pragma unroll
         for (int u = 0; u < R; u++) {
             const long r = base + (long)u * blockDim.x;
-            if (r < hi) E.p[r] = rv[u] + BETA * (pv[u] - AMU * qv[u]);
+            if (r < hi) E.p[r] = fma_rn(BETA, fnma(AMU, qv[u], pv[u]), rv[u]);
         }
     }
 }
@@ -1296,9 +1421,9 @@ static __global__ void k_eng_guard(MemberScalars* S, int M, int* ctrl, cudaGraph
 // One cooperative launch runs the whole BiCGSTAB loop of every member: the 16
 // phases of an iteration are separated by grid barriers instead of kernel
 // boundaries.  Every barrier wait is bounded: a block that waits longer than
-// kBarSpinLimit polls (seconds) raises the abort flag, and every block leaves
-// the kernel at its next barrier; the host then reports CLOWNS_IER_DEVICE.  No
-// correct run comes near the bound (a phase lasts microseconds to milliseconds).
+// `limit` polls raises the abort flag, and every block leaves the kernel at its
+// next barrier; the host then reports the failure.  The limit is a kernel
+// argument (kBarSpinLimit in every solve; a test gives a short one).
 
 struct GridBar {
     unsigned count;
@@ -1307,9 +1432,7 @@ struct GridBar {
     int pad[29];
 };
 
-constexpr long kBarSpinLimit = 1L << 24;
-
-__device__ __forceinline__ bool grid_sync(GridBar* gb) {
+__device__ __forceinline__ bool grid_sync(GridBar* gb, long limit) {
     __shared__ int s_ok;
     __syncthreads();
     if (threadIdx.x == 0) {
@@ -1326,7 +1449,7 @@ __device__ __forceinline__ bool grid_sync(GridBar* gb) {
             long spins = 0;
             while (*genp == g0) {
                 if (*abortp) break;
-                if (++spins > kBarSpinLimit) {
+                if (++spins > limit) {
                     atomicExch(&gb->abort, 1);
                     break;
                 }
@@ -1341,33 +1464,37 @@ __device__ __forceinline__ bool grid_sync(GridBar* gb) {
 }
 
 template <typename T>
-__device__ __forceinline__ bool ph_apply(const Eng<T>& E, GridBar* gb, const T* in, T* out, T* tmp, int mode) {
+__device__ __forceinline__ bool ph_apply(const Eng<T>& E, GridBar* gb, long lim, const T* in, T* out, T* tmp,
+                                         int mode) {
     ph_axsub(E, in, tmp);
-    if (!grid_sync(gb)) return false;
+    if (!grid_sync(gb, lim)) return false;
     ph_sweep2(E, 0, tmp, out);
-    if (!grid_sync(gb)) return false;
+    if (!grid_sync(gb, lim)) return false;
     ph_sweep2(E, 2, out, tmp);
-    if (!grid_sync(gb)) return false;
+    if (!grid_sync(gb, lim)) return false;
     if (mode == 0) ph_sweep56<T, 0>(E, tmp, out);
     if (mode == 1) ph_sweep56<T, 1>(E, tmp, out);
     if (mode == 2) ph_sweep56<T, 2>(E, tmp, out);
-    return grid_sync(gb);
+    return grid_sync(gb, lim);
 }
 
-// init != 0: also run the start of PCGPME (b^ = PM W b, q = PM A x0, residuals)
+// init != 0: also run the start of PCGPME (b^ = PM W b, q = PM A x0, residuals).
+// lim: polls per barrier wait; absent >= 0: that block leaves at once without
+// arriving anywhere (a test of the bounded waits: the others give up).
 template <typename T, int MINB>
-__global__ void __launch_bounds__(kEngBlock, MINB) k_eng_loop(Eng<T> E, GridBar* gb, int init) {
+__global__ void __launch_bounds__(kEngBlock, MINB) k_eng_loop(Eng<T> E, GridBar* gb, int init, long lim, int absent) {
+    if ((int)blockIdx.x == absent) return;
     if (init) {
         // b^ = PM W b in place on p (sweeps p->t->q->t->q->p)
         ph_sweep2(E, 0, E.p, E.t);
-        if (!grid_sync(gb)) return;
+        if (!grid_sync(gb, lim)) return;
         ph_sweep2(E, 2, E.t, E.q);
-        if (!grid_sync(gb)) return;
+        if (!grid_sync(gb, lim)) return;
         ph_sweep56<T, 0>(E, E.q, E.p);
-        if (!grid_sync(gb)) return;
-        if (!ph_apply(E, gb, E.xi, E.q, E.t, 0)) return;      // q = PM A x0
+        if (!grid_sync(gb, lim)) return;
+        if (!ph_apply(E, gb, lim, E.xi, E.q, E.t, 0)) return;      // q = PM A x0
         ph_initres(E);
-        if (!grid_sync(gb)) return;
+        if (!grid_sync(gb, lim)) return;
     }
     const int cap = sld(E.ctrl + 1) + 2;
     for (int body = 0;; body++) {
@@ -1383,14 +1510,14 @@ __global__ void __launch_bounds__(kEngBlock, MINB) k_eng_loop(Eng<T> E, GridBar*
                         stop_member(E.S + m, CLOWNS_STOP_MAXITER, sld(&E.S[m].mode) == 0 ? CLOWNS_IER_MAXITER : 0);
             break;
         }
-        if (!ph_apply(E, gb, E.p, E.q, E.t, 1)) return;       // q = PM A p ; ALP
-        ph_eupdate(E);                                        // e = r - ALP q
-        if (!grid_sync(gb)) return;
-        if (!ph_apply(E, gb, E.e, E.v, E.t, 2)) return;       // v = PM A e ; AMU
-        ph_xrupdate(E);                                       // x, r ; stop tests
-        if (!grid_sync(gb)) return;
-        ph_pupdate(E);                                        // p
-        if (!grid_sync(gb)) return;
+        if (!ph_apply(E, gb, lim, E.p, E.q, E.t, 1)) return;       // q = PM A p ; ALP
+        ph_eupdate(E);                                             // e = r - ALP q
+        if (!grid_sync(gb, lim)) return;
+        if (!ph_apply(E, gb, lim, E.e, E.v, E.t, 2)) return;       // v = PM A e ; AMU
+        ph_xrupdate(E);                                            // x, r ; stop tests
+        if (!grid_sync(gb, lim)) return;
+        ph_pupdate(E);                                             // p
+        if (!grid_sync(gb, lim)) return;
     }
 }
 
@@ -1409,11 +1536,11 @@ __global__ void __launch_bounds__(kEngBlock, MINB) k_eng_loop(Eng<T> E, GridBar*
 // waits for, and the FP64-heavy axsub of one tile runs beside the memory-bound
 // sweeps of others.  Items are dealt round-robin to the co-resident blocks,
 // which take them in order; each waits on per-chunk completion counters
-// (monotone across iterations) and publishes its own.  The reductions keep the
-// engine's deterministic two-level "last block sums" scheme; their finalising
-// block publishes an epoch that the next segment waits for.  Every wait is
-// bounded (kBarSpinLimit polls): a block that gives up raises the abort flag,
-// every other block leaves at its next wait, and the host reports the error.
+// (monotone across iterations) and publishes its own.  The reductions are the
+// canonical ones; their finalising thread publishes an epoch that the next
+// segment waits for.  Every wait is bounded (`limit` polls): a block that gives
+// up raises the abort flag, every other block leaves at its next wait, and the
+// host reports the error.
 
 __device__ __forceinline__ unsigned ld_relaxed_u32(const unsigned* p) {
     unsigned v;
@@ -1429,7 +1556,7 @@ __device__ __forceinline__ int ld_relaxed_s32(const int* p) {
 // Warp 0 waits until the counters of chunks c0..c1 reach (it + 1) x (tiles of
 // the chunk); the whole block then proceeds.  False: abort raised.
 __device__ __forceinline__ bool wave_wait_counts(const unsigned* cnt, int c0, int c1, int it, int nblk,
-                                                 GridBar* gb) {
+                                                 GridBar* gb, long limit) {
     __shared__ int s_ok;
     if (threadIdx.x < 32) {
         bool ok = true;
@@ -1438,7 +1565,7 @@ __device__ __forceinline__ bool wave_wait_counts(const unsigned* cnt, int c0, in
             long spins = 0;
             while (ld_relaxed_u32(cnt + c) < need) {
                 if (ld_relaxed_s32(&gb->abort)) { ok = false; break; }
-                if (++spins > kBarSpinLimit) { atomicExch(&gb->abort, 1); ok = false; break; }
+                if (++spins > limit) { atomicExch(&gb->abort, 1); ok = false; break; }
                 __nanosleep(32);
             }
         }
@@ -1451,14 +1578,14 @@ __device__ __forceinline__ bool wave_wait_counts(const unsigned* cnt, int c0, in
 }
 
 // Thread 0 waits until *ep >= need.  False: abort raised.
-__device__ __forceinline__ bool wave_wait_epoch(const unsigned* ep, unsigned need, GridBar* gb) {
+__device__ __forceinline__ bool wave_wait_epoch(const unsigned* ep, unsigned need, GridBar* gb, long limit) {
     __shared__ int s_ok;
     if (threadIdx.x == 0) {
         bool ok = true;
         long spins = 0;
         while (ld_relaxed_u32(ep) < need) {
             if (ld_relaxed_s32(&gb->abort)) { ok = false; break; }
-            if (++spins > kBarSpinLimit) { atomicExch(&gb->abort, 1); ok = false; break; }
+            if (++spins > limit) { atomicExch(&gb->abort, 1); ok = false; break; }
             __nanosleep(64);
         }
         __threadfence();
@@ -1471,21 +1598,21 @@ __device__ __forceinline__ bool wave_wait_epoch(const unsigned* ep, unsigned nee
 // Stage s (0..6) of segment seg (0: A, 1: B) on tiles t0 .. t0+K-1 (K divides
 // kWaveChunk) in iteration it.
 template <typename T>
-__device__ __forceinline__ bool wave_item(const Eng<T>& E, GridBar* gb, unsigned* cnt, int nchunk, int seg, int s,
-                                          int t0, int K, int it, int D, double* red) {
+__device__ __forceinline__ bool wave_item(const Eng<T>& E, GridBar* gb, long lim, unsigned* cnt, int nchunk,
+                                          int seg, int s, int t0, int K, int it, int D) {
     const int nblk = E.nblk;
     const int t1 = min(nblk, t0 + K);
     if (s >= 1) {
         const int lo = max(0, t0 - D), hi = min(nblk - 1, t1 - 1 + D);
         if (!wave_wait_counts(cnt + (long)(seg * 6 + s - 1) * nchunk, lo / kWaveChunk, hi / kWaveChunk, it, nblk,
-                              gb))
+                              gb, lim))
             return false;
     }
     for (int t = t0; t < t1; t++) {
         if (s == 6) {
-            const bool fin = seg == 0 ? tl_sweep56<T, 1>(E, t, E.w[4], E.q, red)    // q = PM A p ; RQ ; ALP
-                                      : tl_sweep56<T, 2>(E, t, E.w[4], E.v, red);   // v = PM A e ; AMU
-            if (fin && threadIdx.x == 0) {
+            const bool fin = seg == 0 ? tl_sweep56<T, 1>(E, t, E.w[4], E.q)    // q = PM A p ; RQ ; ALP
+                                      : tl_sweep56<T, 2>(E, t, E.w[4], E.v);   // v = PM A e ; AMU
+            if (fin) {
                 __threadfence();
                 atomicAdd(seg == 0 ? &E.wave->alp : &E.wave->amu, 1u);
             }
@@ -1509,10 +1636,12 @@ __device__ __forceinline__ bool wave_item(const Eng<T>& E, GridBar* gb, unsigned
 }
 
 // K: tiles per item (divides kWaveChunk); slack: rounds of G items between an
-// item and the items it waits for, beyond the gather reach.
+// item and the items it waits for, beyond the gather reach.  lim and absent as
+// for k_eng_loop.
 template <typename T, int MINB>
-__global__ void __launch_bounds__(kStepBlock, MINB) k_eng_wave(Eng<T> E, GridBar* gb, int K, int slack) {
-    __shared__ double red[64];
+__global__ void __launch_bounds__(kStepBlock, MINB) k_eng_wave(Eng<T> E, GridBar* gb, int K, int slack, long lim,
+                                                               int absent) {
+    if ((int)blockIdx.x == absent) return;
     WaveCtl* W = E.wave;
     unsigned* cnt = (unsigned*)(W + 1);
     const int G = gridDim.x;
@@ -1526,7 +1655,7 @@ __global__ void __launch_bounds__(kStepBlock, MINB) k_eng_wave(Eng<T> E, GridBar
     const int cap = sld(E.ctrl + 1) + 2;
     MemberScalars* S = E.S;
     for (int it = 0;; it++) {
-        if (it > 0 && !wave_wait_epoch(&W->beta, (unsigned)it, gb)) return;
+        if (it > 0 && !wave_wait_epoch(&W->beta, (unsigned)it, gb, lim)) return;
         if (sld(&S->done)) return;
         if (it >= cap) {                        // backstop: ITER stops the member first
             if (blockIdx.x == 0 && threadIdx.x == 0)
@@ -1538,13 +1667,13 @@ __global__ void __launch_bounds__(kStepBlock, MINB) k_eng_wave(Eng<T> E, GridBar
                 const int s = (int)(q % kWaveStages);
                 const long u = q / kWaveStages - (long)s * L;
                 if (u < 0 || u >= nsup) continue;
-                if (!wave_item(E, gb, cnt, nchunk, seg, s, (int)u * K, K, it, D, red)) return;
+                if (!wave_item(E, gb, lim, cnt, nchunk, seg, s, (int)u * K, K, it, D)) return;
             }
-            if (!wave_wait_epoch(seg == 0 ? &W->alp : &W->amu, (unsigned)(it + 1), gb)) return;
+            if (!wave_wait_epoch(seg == 0 ? &W->alp : &W->amu, (unsigned)(it + 1), gb, lim)) return;
             if (sld(&S->done)) return;
         }
         for (int t = blockIdx.x; t < nblk; t += G) {
-            if (tl_xrupdate(E, t, red) && threadIdx.x == 0) {
+            if (tl_xrupdate(E, t)) {
                 __threadfence();
                 atomicAdd(&W->beta, 1u);
             }

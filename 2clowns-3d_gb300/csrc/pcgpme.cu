@@ -113,3 +113,12 @@ extern "C" int clowns_tuned_shape(int m, const int* n, int precision, int* mode,
 }
 
 extern "C" long clowns_last_kernel_launches(void) { return engine_last_launches(); }
+
+extern "C" int clowns_test_arm_wait_timeout(long polls, int absent_block) {
+    if (polls < 1 || absent_block < 0) {
+        set_last_error_msg("test_arm_wait_timeout: polls >= 1 and absent_block >= 0 required");
+        return CLOWNS_ERR_ARG;
+    }
+    engine_arm_wait_fault(polls, absent_block);
+    return CLOWNS_OK;
+}

@@ -184,6 +184,17 @@ int clowns_pcgpme_batched_dev(int m, const clowns_member* members, int precision
 int clowns_tuned_shape(int m, const int* n, int precision, int* mode, int* block, int* grid, int* regs,
                        int* fused);
 
+/* Test hook of failure detection (no counterpart in the reference): the next
+ * plain FP64 solve whose iteration loop runs as one cooperative kernel
+ * (CLOWNS_LOOP_PERSISTENT or CLOWNS_LOOP_WAVE, e.g. forced by
+ * CLOWNS_LOOP_MODE=persistent|wave) gives every device-wide wait `polls` polls
+ * instead of 2^24 and makes its block `absent_block` leave the kernel without
+ * arriving anywhere.  The other blocks' waits then run out: they raise the
+ * abort flag and return, nothing hangs or faults, and the solve reports
+ * CLOWNS_ERR_NOCONV (through pcgpme_gpu: IER = CLOWNS_IER_DEVICE).  Applies to
+ * one solve, then disarms; later solves on the same context run normally. */
+int clowns_test_arm_wait_timeout(long polls, int absent_block);
+
 /* Kernels the calling thread's last solve (plain or mixed, single or batched)
  * launched: host launches plus the kernel nodes its loop graphs executed
  * (16 per iteration), not counting the autotuner's one-time trial runs.

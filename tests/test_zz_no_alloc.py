@@ -1,11 +1,13 @@
 """The allocation-free solve (clowns_pcgpme_static_dev) against the workspace
-solve (clowns_pcgpme_dev), both called through the C ABI.
+solve (clowns_pcgpme_dev) and the oracle, called through the C ABI.
 
 Callers that cannot allocate device memory -- a host model whose device memory
 belongs to another runtime or to a fixed budget -- use the allocation-free
 entry point, whose scratch lives in a static device array (limit: 32768 rows).
-Two calls in a row must each match the workspace solve within the tolerance of
-the other solve tests (1e-10 relative L2 at ERR <= 1e-13), and the second call
+It runs the workspace solve's kernels and summation tree, so two calls in a
+row must each reproduce the workspace solve's iteration count and pressure
+bit for bit, lie within 1e-10 relative L2 of the oracle's pressure (both at
+ERR <= 1e-13, the tolerance of the other solve tests), and the second call
 must not change the device's free memory.  This file is collected last."""
 import ctypes as C
 
@@ -30,15 +32,17 @@ def _static_solve(gpu, ds, x, eps):
 
 
 @pytest.mark.parametrize("idx", [1, 2])
-def test_static_solve_matches_workspace_solve_twice(gpu, idx):
+def test_static_solve_matches_workspace_solve_twice(gpu, ora, idx):
     import torch
     label, case = small_cases()[idx]
+    cls, sm, sy = ora.prepare(case)
     dc, ds = gpu.prepare_dev(case)
     n = ds.mnoe
     assert n <= 32768
     xw = torch.zeros(ds.mm2, dtype=torch.float64, device="cuda")
     iw = gpu.Solver(n).solve(ds.alu, ds.llu, ds.de, ds.b, xw, eps=1e-13)
     ref = xw[:n].cpu().numpy()
+    oracle = ora.pcgpme(sy.alu, sy.llu, sy.de[1:], sy.b[1:], n, eps=1e-13)
     free_after_first = None
     for call in range(2):
         xs = torch.zeros(ds.mm2, dtype=torch.float64, device="cuda")
@@ -51,8 +55,9 @@ def test_static_solve_matches_workspace_solve_twice(gpu, idx):
             assert free_after == free_before, "the allocation-free solve changed free device memory"
         got = xs[:n].cpu().numpy()
         assert info.ier == iw.ier == 0
-        assert np.linalg.norm(got - ref) <= 1e-10 * np.linalg.norm(ref), (label, call)
-        assert abs(info.iter - iw.iter) <= max(5, iw.iter // 4)
+        assert (info.iter, info.eps) == (iw.iter, iw.eps), (label, call)
+        assert np.array_equal(got, ref), (label, call)
+        assert np.linalg.norm(got - oracle.x) <= 1e-10 * np.linalg.norm(oracle.x), (label, call)
         free_after_first = free_after
     assert free_after_first is not None
 
