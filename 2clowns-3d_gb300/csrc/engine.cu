@@ -10,6 +10,7 @@
 #include <cstring>
 #include <map>
 #include <mutex>
+#include <string>
 #include <tuple>
 #include <vector>
 
@@ -701,16 +702,33 @@ static void g_iteration(bool pdl, const Eng<T>& E, const Shape& sh, cudaStream_t
     klaunch(pdl, k_eng_pupdate<T>, g, b, s, E);
 }
 
-// Graph cache: one instantiated loop graph per (workspace, row space, precision)
+// Graph cache: one instantiated loop graph per engine state and kernel shape.
+// The captured kernels take the Eng struct by value -- its row counts, member
+// tables and workspace pointers -- so the key holds all of its fields: two
+// systems of the same row space but different sizes (or ensembles with
+// different members) must not share a graph.
 struct GraphKey {
-    const void* work;
-    long NV;
-    int M, prec, fuse, rblock, bal, nl;
+    std::string eng;
+    int prec, fuse, rblock, bal;
     bool operator<(const GraphKey& o) const {
-        return std::tie(work, NV, M, prec, fuse, rblock, bal, nl) <
-               std::tie(o.work, o.NV, o.M, o.prec, o.fuse, o.rblock, o.bal, o.nl);
+        return std::tie(eng, prec, fuse, rblock, bal) < std::tie(o.eng, o.prec, o.fuse, o.rblock, o.bal);
     }
 };
+
+// Every field of E, field by field (no padding bytes).
+template <typename T>
+static std::string eng_key(const Eng<T>& E) {
+    std::string k;
+    auto put = [&](const auto& v) { k.append((const char*)&v, sizeof(v)); };
+    put(E.NV); put(E.M); put(E.nblk); put(E.n1); put(E.nl);
+    put(E.al); put(E.ll); put(E.d); put(E.r); put(E.p); put(E.r0); put(E.q); put(E.e); put(E.v); put(E.t);
+    put(E.xi); put(E.W); put(E.x64); put(E.r64); put(E.s64); put(E.t64);
+    put(E.blk_member); put(E.blk_rows); put(E.mem_off); put(E.mem_n); put(E.mem_nblk); put(E.mem_blk0);
+    put(E.mem_grp0); put(E.mem_ngrp); put(E.gticket); put(E.gpartials);
+    for (int i = 0; i < kWaveBufs; i++) put(E.w[i]);
+    put(E.wave); put(E.in); put(E.S); put(E.partials); put(E.ticket); put(E.ctrl); put(E.baltab); put(E.balg);
+    return k;
+}
 static std::mutex g_graph_mu;
 static std::map<GraphKey, cudaGraphExec_t> g_graphs;
 static cudaStream_t g_cap = nullptr;
@@ -719,18 +737,6 @@ void release_all_graphs() {
     std::lock_guard<std::mutex> lk(g_graph_mu);
     for (auto& kv : g_graphs) cudaGraphExecDestroy(kv.second);
     g_graphs.clear();
-}
-
-void release_graphs_for(const void* work) {
-    std::lock_guard<std::mutex> lk(g_graph_mu);
-    for (auto it = g_graphs.begin(); it != g_graphs.end();) {
-        if (it->first.work == work) {
-            cudaGraphExecDestroy(it->second);
-            it = g_graphs.erase(it);
-        } else {
-            ++it;
-        }
-    }
 }
 
 // WHILE { iteration ; guard } captured into a fresh graph
@@ -781,7 +787,8 @@ template <typename T>
 static int loop_graph(const Eng<T>& E, const void* work, int prec, int fuse, int rblock, int bal,
                       cudaGraphExec_t* out) {
     std::lock_guard<std::mutex> lk(g_graph_mu);
-    GraphKey key{work, E.NV, E.M, prec, fuse, rblock, bal, E.nl};
+    (void)work;
+    GraphKey key{eng_key(E), prec, fuse, rblock, bal};
     auto it = g_graphs.find(key);
     if (it != g_graphs.end()) { *out = it->second; return CLOWNS_OK; }
     cudaGraphExec_t ex;
@@ -1160,11 +1167,7 @@ static int check_members(int M, const MemberIn* ins, std::vector<int>& n, int* n
             set_last_error_msg("pcgpme: invalid member arguments");
             return CLOWNS_ERR_ARG;
         }
-        if (nl >= 0 && in.nl != nl) {
-            set_last_error_msg("pcgpme: all members must share nl");
-            return CLOWNS_ERR_ARG;
-        }
-        nl = in.nl;
+        nl = std::max(nl, in.nl);          // 2DV (4) and 3D (6) members may share a batch
         n[m] = in.n;
     }
     long tot = 0;

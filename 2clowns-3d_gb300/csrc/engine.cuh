@@ -189,10 +189,11 @@ __device__ __forceinline__ A warp_tsum(A (&v)[V], int& idx) {
 }
 
 // Record a chunk total (global chunk index gc, value k of NV) -- by one lane.
+// Plain store: account_chunks fences every thread's stores once, before the
+// block's tickets.
 template <typename T>
 __device__ __forceinline__ void put_chunk(const Eng<T>& E, long gc, int k, double v) {
     E.partials[2 * gc + k] = v;
-    __threadfence();
 }
 
 // Reduce one chunk's lane values (NV = 1 or 2 per lane) and record its totals.
@@ -204,9 +205,8 @@ __device__ __forceinline__ void chunk_total(const Eng<T>& E, long gc, A (&v)[NV]
     if ((threadIdx.x & (32 / NV - 1)) == 0) put_chunk(E, gc, idx, (double)s);
 }
 
-// Called by EVERY thread of the block once the block's writers recorded (and
-// fenced) the totals of member m's chunks [c0, c1) (member-relative; empty
-// allowed).  Accounts the chunks to their groups; the block that completes a
+// Called by EVERY thread of the block once the block's writers recorded the
+// totals of member m's chunks [c0, c1) (member-relative; empty allowed).  Accounts the chunks to their groups; the block that completes a
 // group sums it in one warp, and the warp that completes the member's last group
 // sums the member.  Returns true in all lanes of that warp, with the member
 // totals in tot[] (every lane); false elsewhere.
@@ -223,7 +223,8 @@ __device__ __noinline__ bool account_chunks(const Eng<T>& E, int m, int c0, int 
     bool fin = false;
     const int g_lo = c1 > c0 ? c0 / kGroupChunks : 0;
     const int g_hi = c1 > c0 ? (c1 - 1) / kGroupChunks : -1;
-    __syncthreads();                              // the block's chunk totals are written and fenced
+    __threadfence();                              // this thread's chunk totals are visible device-wide
+    __syncthreads();                              // ... before any ticket of the block
     for (int gb = g_lo; gb <= g_hi || gb == g_lo; gb += kList) {
         if (threadIdx.x == 0) s_n = 0;
         __syncthreads();
@@ -388,7 +389,11 @@ __device__ __forceinline__ void finish_xrupdate(MemberScalars* S, const double (
 // exchange sort (pcgpme_para.F90:77-112).  Explicitly rounded arithmetic so the
 // sort decisions equal an IEEE evaluation of the source.  For rows beyond a
 // member's n (its pad rows) all vectors are zeroed and slots point at the
-// member's zero row.  init_x: copy the member's initial guess into xi / x64.
+// member's zero row.  NL: the batch's widest matrix; a member with fewer
+// columns (a 2DV member, 4, beside 3D ones) reads only its own, and its other
+// slots are empty -- zero coefficients never move ahead of others in the
+// exchange sort (strict <), so its first columns sort exactly as a sort of its
+// own columns would.  init_x: copy the member's initial guess into xi / x64.
 template <typename T, int NL>
 __global__ void __launch_bounds__(kEngBlock) k_eng_setup(Eng<T> E, double P1, double P2, int mixed) {
     int reach = 0;    // gather distance in tiles (wavefront loop), real neighbours only
@@ -419,7 +424,7 @@ __global__ void __launch_bounds__(kEngBlock) k_eng_setup(Eng<T> E, double P1, do
         double s = 0.0;
 #pragma unroll
         for (int k = 0; k < 6; k++) {
-            if (k < NL) {
+            if (k < NL && k < in.nl) {
                 a[k] = in.al[k * (long)in.na + li];
                 int cc = in.ll[k * (long)in.na + li];
                 if (cc < 0 || cc > n) {

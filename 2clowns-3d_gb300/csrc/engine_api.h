@@ -27,7 +27,6 @@ void release_all_graphs();
 int engine_tuned_shape(long nv, int prec, int single, int* mode, int* block, int* grid, int* minb, int* fuse);
 long engine_row_space(int M, const int* n, int mixed);
 long engine_last_launches();
-void release_graphs_for(const void* work);
 // Test hook: the next plain solve's cooperative loop kernel waits at most
 // `limit` polls per device-wide wait and its block `absent` leaves at once.
 void engine_arm_wait_fault(long limit, int absent);
