@@ -114,7 +114,8 @@ _SIGS = {
                                      + [C.c_void_p] * 5),
     "clowns_session_get_fields": (C.c_int, [C.c_void_p] * 7),
     "clowns_session_destroy": (C.c_int, [C.c_void_p]),
-    "clowns_transpose_dev": (C.c_int, [C.c_int, C.c_int] + [C.c_void_p] * 8),
+    "clowns_transpose_dev": (C.c_int, [C.c_int, C.c_int, C.c_int] + [C.c_void_p] * 8),
+    "clowns_grid_nl": (C.c_int, [C.c_void_p]),
     "clowns_face_grad_dev": (C.c_int, [C.c_void_p, C.c_int, C.c_int, C.c_int] + [C.c_void_p] * 13),
     "clowns_correct_dev": (C.c_int, [C.c_void_p, C.c_int, C.c_int] + [C.c_void_p] * 8
                            + [C.c_double, C.c_int] + [C.c_void_p] * 6),
@@ -260,7 +261,7 @@ class DeviceSystem:
     fln: object          # int32 (ifln,) == fln(1:ifln)
     sfn: object
     mp: object           # f64 (1,)
-    alu_c: object        # (6, inne)
+    alu_c: object        # (nl, inne)
     ll_c: object
     de_c: object
     mm2: int
@@ -271,8 +272,8 @@ class DeviceSystem:
     b: object            # (mm2,) == b(1:mm2)
     xe: object           # (mm2+1,) == xe(0:mm2)
     de: object           # (mm2,)
-    alu: object          # (6, mm2)
-    llu: object          # (6, mm2)
+    alu: object          # (nl, mm2)
+    llu: object          # (nl, mm2)
 
 
 def set_nflag_dev(dc: DeviceCase):
@@ -294,13 +295,23 @@ def set_nflag_dev(dc: DeviceCase):
     return fln[:ifln.value], ifln.value, sfn[:isfn.value], isfn.value, passes.value
 
 
+def grid_nl(dims) -> int:
+    """Matrix columns of a grid: 6 (3D), 4 (2DV: one cell wide in x or y) or 0
+    (one cell wide in both, or invalid bounds)."""
+    d = np.ascontiguousarray(dims, dtype=np.int32)
+    return int(lib().clowns_grid_nl(d.ctypes.data))
+
+
 def init_matrix_dev(dc: DeviceCase):
     torch = _torch()
     L = lib()
     case = dc.case
+    nl = grid_nl(case.dims)
+    if nl == 0:
+        raise ClownsError("init_matrix: a grid one cell wide in both x and y has no matrix form")
     mp = torch.zeros(1, dtype=torch.float64, device="cuda")
-    alu_c = torch.empty((6, case.inne), dtype=torch.float64, device="cuda")
-    ll_c = torch.empty((6, case.inne), dtype=torch.int32, device="cuda")
+    alu_c = torch.empty((nl, case.inne), dtype=torch.float64, device="cuda")
+    ll_c = torch.empty((nl, case.inne), dtype=torch.int32, device="cuda")
     de_c = torch.empty(case.inne, dtype=torch.float64, device="cuda")
     dims = dc.dims.numpy()
     rc = L.clowns_init_matrix_dev(dims.ctypes.data, case.inne, case.mx2, _ptr(dc.mn), _ptr(dc.in_), _ptr(dc.jn),
@@ -334,8 +345,9 @@ def rows_rhs_assemble_dev(dc: DeviceCase, fln, ifln: int, mp, alu_c, ll_c, de_c,
                                _ptr(mno2mn), _ptr(b), _ptr(xe) + 8, _ptr(de), C.byref(mnoe), C.byref(dmax),
                                _ptr(work), wbytes, _stream())
     _check(rc, "rows_rhs")
-    alu = torch.zeros((6, mm2), dtype=torch.float64, device="cuda")
-    llu = torch.zeros((6, mm2), dtype=torch.int32, device="cuda")
+    nl = alu_c.shape[0]
+    alu = torch.zeros((nl, mm2), dtype=torch.float64, device="cuda")
+    llu = torch.zeros((nl, mm2), dtype=torch.int32, device="cuda")
     err = torch.zeros(1, dtype=torch.int32, device="cuda")
     rc = L.clowns_assemble_dev(dims.ctypes.data, case.inne, case.inne2, case.mx2, _ptr(dc.in_), _ptr(dc.jn),
                                _ptr(dc.kn), _ptr(dc.nf), _ptr(dc.nfb), _ptr(dc.x), _ptr(dc.dx), _ptr(dc.sp),
@@ -528,8 +540,8 @@ def transpose_dev(alu, llu, de, n: int):
     llt = torch.empty_like(llu)
     det = torch.zeros_like(de)
     bad = torch.zeros(1, dtype=torch.int32, device="cuda")
-    rc = L.clowns_transpose_dev(n, na, _ptr(alu), _ptr(llu), _ptr(de), _ptr(alt), _ptr(llt), _ptr(det), _ptr(bad),
-                                _stream())
+    rc = L.clowns_transpose_dev(n, na, nl, _ptr(alu), _ptr(llu), _ptr(de), _ptr(alt), _ptr(llt), _ptr(det),
+                                _ptr(bad), _stream())
     _check(rc, "transpose")
     if int(bad.item()):
         raise ClownsError("transpose: column index out of range")

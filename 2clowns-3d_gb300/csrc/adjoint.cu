@@ -13,24 +13,23 @@
 
 namespace clowns {
 
-__global__ void k_transpose_zero(long n, long na, double* alt, int* llt) {
-    for (long t = (long)blockIdx.x * blockDim.x + threadIdx.x; t < 6 * na; t += (long)gridDim.x * blockDim.x) {
+__global__ void k_transpose_zero(long n, long na, int nl, double* alt, int* llt) {
+    for (long t = (long)blockIdx.x * blockDim.x + threadIdx.x; t < nl * na; t += (long)gridDim.x * blockDim.x) {
         alt[t] = 0.0;
         llt[t] = 0;
     }
 }
 
-__global__ void k_transpose(long n, long na, const double* __restrict__ alu, const int* __restrict__ llu,
+__global__ void k_transpose(long n, long na, int nl, const double* __restrict__ alu, const int* __restrict__ llu,
                             const double* __restrict__ de, double* __restrict__ alt, int* __restrict__ llt,
                             double* __restrict__ det, int* bad) {
     for (long j = (long)blockIdx.x * blockDim.x + threadIdx.x; j < n; j += (long)gridDim.x * blockDim.x) {
         det[j] = de[j];
-#pragma unroll
-        for (int d = 0; d < 6; d++) {
+        for (int d = 0; d < nl; d++) {
             const int i = llu[d * na + j];          // 1-based row, 0 = none
             if (i == 0) continue;
             if (i < 0 || i > n) { atomicOr(bad, 1); continue; }
-            const int od = d ^ 1;                   // x- <-> x+, y- <-> y+, z- <-> z+
+            const int od = d ^ 1;                   // minus <-> plus face of the same axis
             alt[od * na + (i - 1)] = alu[d * na + j];
             llt[od * na + (i - 1)] = (int)j + 1;
         }
@@ -51,12 +50,12 @@ __global__ void k_face_grad(GridIdx g, int ifln, long inne, const int* __restric
         const int r = mno[g.mno_off(in_[c], kn[c], jn[c])];
         if (r == 0) continue;
         const double lr = lam[r - 1], xr = x[r - 1];
-#pragma unroll
-        for (int ll = 0; ll < 6; ll++) {
+        const int nl = g.nl();
+        for (int ll = 0; ll < nl; ll++) {
             const long oc = (long)ll * inne + (c - 1);
             const int lc = ll_c[oc];
             if (lc == 0) continue;
-            const int l = ll >> 1, side = ll & 1;
+            const int l = g.col_axis(ll >> 1), side = ll & 1;
             const int owner = side ? lc : c;
             const double af = a[3L * owner + l];
             if (af == 0.0) continue;
@@ -80,18 +79,18 @@ __global__ void k_face_grad(GridIdx g, int ifln, long inne, const int* __restric
 
 using namespace clowns;
 
-extern "C" int clowns_transpose_dev(int n, int na, const double* alu, const int* llu, const double* de,
+extern "C" int clowns_transpose_dev(int n, int na, int nl, const double* alu, const int* llu, const double* de,
                                     double* alt, int* llt, double* det, int* bad, void* stream) {
-    if (n < 1 || na < n || !alu || !llu || !de || !alt || !llt || !det || !bad) {
+    if (n < 1 || na < n || (nl != 6 && nl != 4) || !alu || !llu || !de || !alt || !llt || !det || !bad) {
         set_last_error_msg("transpose: invalid arguments");
         return CLOWNS_ERR_ARG;
     }
     cudaStream_t s = (cudaStream_t)stream;
-    const int gb = (int)std::min<long>((6L * na + 255) / 256, 152L * 16);
+    const int gb = (int)std::min<long>(((long)nl * na + 255) / 256, 152L * 16);
     CLOWNS_CUDA_TRY(cudaMemsetAsync(bad, 0, sizeof(int), s));
-    k_transpose_zero<<<gb, 256, 0, s>>>(n, na, alt, llt);
-    k_transpose<<<(int)std::min<long>((n + 255) / 256, 152L * 16), 256, 0, s>>>(n, na, alu, llu, de, alt, llt, det,
-                                                                               bad);
+    k_transpose_zero<<<gb, 256, 0, s>>>(n, na, nl, alt, llt);
+    k_transpose<<<(int)std::min<long>((n + 255) / 256, 152L * 16), 256, 0, s>>>(n, na, nl, alu, llu, de, alt, llt,
+                                                                               det, bad);
     CLOWNS_CUDA_TRY(cudaGetLastError());
     return CLOWNS_OK;
 }
@@ -100,8 +99,8 @@ extern "C" int clowns_face_grad_dev(const int* dims, int inne, int inne2, int if
                                     const int* in_, const int* jn, const int* kn, const int* nf, const int* mno,
                                     const double* alu_c, const int* ll_c, const double* a, const double* x,
                                     const double* lambda, double* grad, void* stream) {
-    if (!grid_dims_ok(dims) || inne < 1 || ifln < 0 || !fln || !in_ || !jn || !kn || !nf || !mno || !alu_c || !ll_c || !a ||
-        !x || !lambda || !grad) {
+    if (!grid_dims_ok(dims) || !grid_has_matrix(dims) || inne < 1 || ifln < 0 || !fln || !in_ || !jn || !kn || !nf ||
+        !mno || !alu_c || !ll_c || !a || !x || !lambda || !grad) {
         set_last_error_msg("face_grad: invalid arguments");
         return CLOWNS_ERR_ARG;
     }

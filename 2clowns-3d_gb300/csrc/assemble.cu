@@ -23,11 +23,13 @@ static inline int grid_for(long n) {
 }
 
 // ---------------------------------------------------------------------------
-// mp = minval(dx, dx > 0)**2  (1sub-matrix.F90:17)
-__global__ void k_min_dx(const double* __restrict__ dx, int count, double* mp) {
+// mp = minval(dx, dx > 0)**2 over the axes in `axes` (bit l: axis l): every
+// axis in 3D (1sub-matrix.F90:17), the two of the x-z or y-z plane in 2DV (20-21)
+__global__ void k_min_dx(const double* __restrict__ dx, int count, int axes, double* mp) {
     __shared__ double s[256];
     double m = 1.0e300;
     for (int t = threadIdx.x; t < count; t += blockDim.x) {
+        if (!((axes >> (t % 3)) & 1)) continue;
         double v = dx[t];
         if (v > 0.0 && v < m) m = v;
     }
@@ -49,7 +51,8 @@ __device__ __forceinline__ double cal_alu(double fnn, double dx, double dxm) {
     return (fnn - 0.5) * dx / (fnn * dx + dxm * 0.5) * (-1.0);
 }
 
-// init_matrix (1sub-matrix.F90:25-65), one thread per cell nnn = 1..inne
+// init_matrix (1sub-matrix.F90:25-65), one thread per cell nnn = 1..inne;
+// columns 2q, 2q+1 hold the minus and plus faces of axis col_axis(q)
 __global__ void __launch_bounds__(kAsmBlock) k_init_matrix(GridIdx g, int inne, const int* __restrict__ mn,
                                                           const int* __restrict__ in_, const int* __restrict__ jn,
                                                           const int* __restrict__ kn, const int* __restrict__ nf,
@@ -59,25 +62,25 @@ __global__ void __launch_bounds__(kAsmBlock) k_init_matrix(GridIdx g, int inne, 
                                                           int* __restrict__ ll_c, double* __restrict__ de_c) {
     const double mp = *mp_p;
     const long ld = inne;
+    const int nl = g.nl();
     for (long t = (long)blockIdx.x * blockDim.x + threadIdx.x; t < inne; t += (long)gridDim.x * blockDim.x) {
         const int nnn = (int)t + 1;
         if (nf[nnn] == -1 || fb[nnn] == 0.0) {
-#pragma unroll
-            for (int c = 0; c < 6; c++) { alu_c[c * ld + t] = 0.0; ll_c[c * ld + t] = 0; }
+            for (int c = 0; c < nl; c++) { alu_c[c * ld + t] = 0.0; ll_c[c * ld + t] = 0; }
             de_c[t] = 0.0;
             continue;
         }
         const int i = in_[nnn], j = jn[nnn], k = kn[nnn];
         const int lg[3] = {i, j, k};
         double de = 0.0;
-#pragma unroll
-        for (int l = 0; l < 3; l++) {
+        for (int q = 0; q < nl / 2; q++) {
+            const int l = g.col_axis(q);
 #pragma unroll
             for (int side = 0; side < 2; side++) {
                 const int ii = side ? 1 : -1;
                 const int np = mn[g.nbr(i, j, k, l, ii)];
                 const int npp = side ? np : mn[g.mn_off(i, k, j)];
-                const int col = 2 * l + side;      // 0-based: x-, x+, y-, y+, z-, z+
+                const int col = 2 * q + side;      // 0-based; 3D: x-, x+, y-, y+, z-, z+
                 if ((nf[np] == -1 && nfb[np] != 4) || a[3L * npp + l] == 0.0 || fb[np] == 0.0) {
                     ll_c[col * ld + t] = 0;
                     alu_c[col * ld + t] = 0.0;
@@ -207,8 +210,8 @@ __global__ void __launch_bounds__(kAsmBlock) k_assemble(GridIdx g, int ifln, lon
         }
         const int bl = nfb[nnn];
         const int axis = (bl < 0 ? -bl : bl) - 1;
-#pragma unroll
-        for (int ll = 1; ll <= 6; ll++) {
+        const int nl = g.nl();
+        for (int ll = 1; ll <= nl; ll++) {
             const long oc = (long)(ll - 1) * inne + (nnn - 1);
             const long o = (long)(ll - 1) * na + r;
             const int lc = ll_c[oc];
@@ -229,7 +232,7 @@ __global__ void __launch_bounds__(kAsmBlock) k_assemble(GridIdx g, int ifln, lon
             if (fl == 1) {
                 alu[o] = alu_c[oc];
             } else {
-                const int l = (ll + ll % 2) / 2 - 1;
+                const int l = g.col_axis((ll - 1) / 2);    // 2DV: past the collapsed axis (517-520)
                 if (axis == l) {
                     const int ii = (l == 0) ? i : (l == 1) ? j : k;
                     const int md = ll % 2;
@@ -306,6 +309,11 @@ using namespace clowns;
 // ---------------------------------------------------------------------------
 // C ABI
 
+extern "C" int clowns_grid_nl(const int* dims) {
+    if (!grid_dims_ok(dims) || !grid_has_matrix(dims)) return 0;
+    return GridIdx::make(dims).nl();
+}
+
 extern "C" int clowns_init_matrix_dev(const int* dims, int inne, int mx2, const int* mn, const int* in_,
                                       const int* jn, const int* kn, const int* nf, const int* nfb,
                                       const double* a, const double* fb, const double* dx, double* mp,
@@ -315,9 +323,15 @@ extern "C" int clowns_init_matrix_dev(const int* dims, int inne, int mx2, const 
         set_last_error_msg("init_matrix: invalid arguments");
         return CLOWNS_ERR_ARG;
     }
+    if (!grid_has_matrix(dims)) {
+        set_last_error_msg("init_matrix: a grid one cell wide in both x and y has no matrix form");
+        return CLOWNS_ERR_ARG;
+    }
     cudaStream_t s = (cudaStream_t)stream;
     GridIdx g = GridIdx::make(dims);
-    k_min_dx<<<1, 256, 0, s>>>(dx, 3 * mx2, mp);
+    // 2DV: x and z when one cell wide in y, y and z when one cell wide in x
+    const int axes = g.ie == g.is + 1 ? 6 : g.je == g.js + 1 ? 5 : 7;
+    k_min_dx<<<1, 256, 0, s>>>(dx, 3 * mx2, axes, mp);
     k_init_matrix<<<grid_for(inne), kAsmBlock, 0, s>>>(g, inne, mn, in_, jn, kn, nf, nfb, a, fb, dx, mp, alu_c,
                                                        ll_c, de_c);
     CLOWNS_CUDA_TRY(cudaGetLastError());
@@ -407,6 +421,10 @@ extern "C" int clowns_assemble_dev(const int* dims, int inne, int inne2, int mx2
     if (!grid_dims_ok(dims) || inne < 1 || !in_ || !jn || !kn || !nf || !nfb || !x || !dx || !sp || !fln || !mno || !alu_c ||
         !ll_c || !de_c || mm2 < 1 || !alu || !llu || !de || !err_cell) {
         set_last_error_msg("assemble: invalid arguments");
+        return CLOWNS_ERR_ARG;
+    }
+    if (!grid_has_matrix(dims)) {
+        set_last_error_msg("assemble: a grid one cell wide in both x and y has no matrix form");
         return CLOWNS_ERR_ARG;
     }
     cudaStream_t s = (cudaStream_t)stream;

@@ -34,7 +34,24 @@ struct GridIdx {
     }
     // offset of x(l,i) / dx(l,i), (0:2, 1:mx2)
     __host__ __device__ __forceinline__ long dxo(int l, int i) const { return 3L * (i - 1) + l; }
+    // Matrix columns: 6 in 3D; 4 in the 2DV mode the reference enters for a grid
+    // one cell wide in x or in y (main_2CLOWNS.F90:43-44, 1sub-matrix.F90:15-21).
+    __host__ __device__ __forceinline__ int nl() const { return (ie == is + 1 || je == js + 1) ? 4 : 6; }
+    // Physical axis of matrix columns 2q, 2q+1 (0-based; minus side first): the
+    // axes that are not one cell wide, in the order x, y, z (1sub-matrix.F90:33-36;
+    // the shift of 1sub-momentum.F90:517-520).
+    __host__ __device__ __forceinline__ int col_axis(int q) const {
+        if (ie == is + 1) return q + 1;
+        if (je == js + 1) return q == 0 ? 0 : 2;
+        return q;
+    }
 };
+
+// A grid one cell wide in both x and y has no matrix form in the reference
+// (init_matrix sets two of its four columns, and the surface-row axis shift of
+// cal_matrix_element reaches 3): the entry points that build or read matrix
+// columns refuse it.
+inline bool grid_has_matrix(const int* d) { return d && !(d[3] == d[0] + 1 && d[4] == d[1] + 1); }
 
 // The reference stores x(l, ls-2 .. le+1) in x(0:2, 1:mx2) (data_io.F90:114,
 // 0mod-arrays.F90:205) and numbers cells from ls-1, whose minus neighbours at

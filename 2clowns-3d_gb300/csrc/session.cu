@@ -96,8 +96,8 @@ static int download(void* dst, const void* src, size_t bytes, cudaStream_t s) {
 extern "C" int clowns_session_create(clowns_session** out, const int* dims, int inne, int inne2, int mx2,
                                      const int* mn, const int* in_, const int* jn, const int* kn,
                                      const double* x, const double* dx, const int* objno) {
-    if (!out || !grid_dims_ok(dims) || inne < 1 || inne2 < inne || mx2 < 1 || !mn || !in_ || !jn || !kn || !x || !dx ||
-        !objno) {
+    if (!out || !grid_dims_ok(dims) || !grid_has_matrix(dims) || inne < 1 || inne2 < inne || mx2 < 1 || !mn || !in_ ||
+        !jn || !kn || !x || !dx || !objno) {
         set_last_error_msg("session_create: invalid arguments");
         return CLOWNS_ERR_ARG;
     }
@@ -260,7 +260,7 @@ extern "C" int clowns_session_pressure_loop(clowns_session* S, double dt, double
         }
         MemberIn in;
         in.al = S->alu; in.ll = S->llu; in.d = S->de; in.b = S->b; in.x = S->xe + 1;
-        in.na = S->mm2; in.n = mnoe; in.nl = 6; in.pad = 0;
+        in.na = S->mm2; in.n = mnoe; in.nl = GridIdx::make(S->dims).nl(); in.pad = 0;
         clowns_solve_info info;
         memset(&info, 0, sizeof(info));
         if (mixed)

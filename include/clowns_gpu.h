@@ -17,8 +17,11 @@
  *   f, fb     : f(0:inne2+1), fb(0:inne2+1)
  *   a, un     : a(0:2, 0:inne2+1), component fastest
  *   sp        : sp(0:inne2+1, 0:2), cell index fastest
- *   alu_c     : ALU_C(1:inne, 1:6) column-major (leading dimension inne); ll_c alike
+ *   alu_c     : ALU_C(1:inne, 1:nl) column-major (leading dimension inne); ll_c alike
  *   alu, llu  : alu(1:na, 1:nl) column-major (leading dimension na = mm2)
+ *   nl        : 6 in 3D, 4 in the 2DV mode of a grid one cell wide in x or y
+ *               (clowns_grid_nl); columns 2q-1, 2q are the minus and plus faces
+ *               of the q-th axis that is not one cell wide, in the order x, y, z
  *   b, de, xe : 1-based row arrays passed as a pointer to their element 1
  *               (xe(0) is not touched by the solver)
  *   fln, sfn  : fln(1:ifln) passed as a pointer to element 1
@@ -268,10 +271,20 @@ int clowns_set_nflag_dev(const int* dims, int inne, int inne2, int mx2, const in
                          const int* objno, int* fln, int* ifln, int* sfn, int* isfn,
                          int* passes, void* work, size_t work_bytes, void* stream);
 
-/* init_matrix (src2LOWNS/1sub-matrix.F90:3-66), 3D: ALU_C, LL_C, DE_C for
- * cells 1..inne and mp = minval(dx, dx>0)**2 (written to device *mp).  Rows of
- * cells that are solid or have zero porosity are zero-filled (the reference
- * leaves them unset; they are never read). */
+/* Matrix columns of a grid (dims as above), the value init_matrix gives the
+ * module variable nl (src2LOWNS/1sub-matrix.F90:15-21): 6 in 3D, 4 in the 2DV
+ * mode the reference enters when the grid is one cell wide in x or in y
+ * (main_2CLOWNS.F90:43-44).  0 for invalid bounds or a grid one cell wide in
+ * both, which has no matrix form in the reference (its init_matrix sets two of
+ * four columns); init_matrix, assembly, the face gradient and the session
+ * refuse such grids with CLOWNS_ERR_ARG.  Host function, no device work. */
+int clowns_grid_nl(const int* dims);
+
+/* init_matrix (src2LOWNS/1sub-matrix.F90:3-66): ALU_C, LL_C, DE_C (nl columns,
+ * nl = clowns_grid_nl(dims)) for cells 1..inne and mp = minval(dx, dx>0)**2
+ * over every axis in 3D, over the two axes of the x-z or y-z plane in 2DV
+ * (written to device *mp).  Rows of cells that are solid or have zero porosity
+ * are zero-filled (the reference leaves them unset; they are never read). */
 int clowns_init_matrix_dev(const int* dims, int inne, int mx2, const int* mn, const int* in_,
                            const int* jn, const int* kn, const int* nf, const int* nfb,
                            const double* a, const double* fb, const double* dx, double* mp,
@@ -292,7 +305,8 @@ int clowns_rows_rhs_dev(const int* dims, int inne2, int mx2, const int* mn, cons
                         int* mnoe, double* dmax, void* work, size_t work_bytes, void* stream);
 
 /* cal_matrix_element (src2LOWNS/1sub-momentum.F90:465-551), NORMAL build:
- * alu/llu(1:mm2, 1:6) column-major and de(1:mm2) for every row.  *err_cell
+ * alu/llu(1:mm2, 1:nl) column-major and de(1:mm2) for every row; in 2DV a
+ * surface row's normal axis is found past the collapsed one (lines 517-520).  *err_cell
  * (device int) receives a cell index if a row cell carries a flag other than 1
  * or 2 (the reference stops there, line 491-492), else 0. */
 int clowns_assemble_dev(const int* dims, int inne, int inne2, int mx2, const int* in_,
@@ -317,12 +331,12 @@ int clowns_correct_dev(const int* dims, int inne, int mx2, const int* mn, const 
 
 /* Explicit transpose of an assembled ELL matrix: row i of (alt, llt, det) holds
  * column i of A; the coefficient of row j toward its neighbour i in direction d
- * lands in row i at the opposite direction slot (x- <-> x+, ...).  n rows,
- * leading dimension na, 1-based llu (0 = none).  *bad (device int) is set if an
- * index lies outside 1..n.  The adjoint solve then runs clowns_pcgpme_dev (or
+ * lands in row i at the opposite direction slot (minus <-> plus face of the same
+ * axis).  n rows, leading dimension na, nl columns (6 or 4), 1-based llu (0 =
+ * none).  *bad (device int) is set if an index lies outside 1..n.  The adjoint solve then runs clowns_pcgpme_dev (or
  * the mixed / batched variants) on (alt, llt, det): the reference's PCGPME
  * method applied to A^T, with its own row scaling and sort. */
-int clowns_transpose_dev(int n, int na, const double* alu, const int* llu, const double* de,
+int clowns_transpose_dev(int n, int na, int nl, const double* alu, const int* llu, const double* de,
                          double* alt, int* llt, double* det, int* bad, void* stream);
 
 /* Face-coefficient gradient dJ/da(l, owner) = -lambda^T (dA/da) x for the face

@@ -260,22 +260,40 @@ static inline double cal_alu(double fnn, double dx, double dxm) {
 }
 
 /* init_matrix (1sub-matrix.F90:3-66), dim3d branch (nl = 6). */
+/* Matrix columns (1sub-matrix.F90:15-21): 6 in 3D, 4 in the 2DV mode the
+ * reference enters for a grid one cell wide in x or y (main_2CLOWNS.F90:43-44);
+ * 0 for a grid one cell wide in both, whose column numbering the reference
+ * leaves undefined (only two of four columns are set). */
+int ora_grid_nl(const int* dims) {
+    grid_t g = mkgrid(dims);
+    int cx = g.is == g.ie - 1, cy = g.js == g.je - 1;
+    return (cx && cy) ? 0 : (cx || cy) ? 4 : 6;
+}
+
 void ora_init_matrix(const int* dims, int inne, int mx2, const int* mn, const int* in_,
                      const int* jn, const int* kn, const int* nf, const int* nfb,
                      const double* a, const double* fb, const double* dx,
                      double* mp_out, double* alu_c, int* ll_c, double* de_c) {
     grid_t g = mkgrid(dims);
-    /* mp = minval(dx, dx > 0)**2 (line 17) */
+    int nl = ora_grid_nl(dims);
+    /* mp = minval(dx, dx > 0)**2 over every axis (line 17); 2DV: over x and z
+     * when one cell wide in y, over y and z when one cell wide in x (20-21) */
+    int use[3] = {1, 1, 1};
+    if (nl == 4) {
+        if (g.js == g.je - 1) { use[0] = 1; use[1] = 0; use[2] = 1; }
+        if (g.is == g.ie - 1) { use[0] = 0; use[1] = 1; use[2] = 1; }
+    }
     double m = 0.0;
     int have = 0;
     for (long t = 0; t < 3L * mx2; t++) {
+        if (!use[t % 3]) continue;
         if (dx[t] > ZERO && (!have || dx[t] < m)) { m = dx[t]; have = 1; }
     }
     double mp = m * m;
     *mp_out = mp;
     long ld = inne;
-    memset(alu_c, 0, sizeof(double) * 6 * (size_t)ld);
-    memset(ll_c, 0, sizeof(int) * 6 * (size_t)ld);
+    memset(alu_c, 0, sizeof(double) * (size_t)nl * (size_t)ld);
+    memset(ll_c, 0, sizeof(int) * (size_t)nl * (size_t)ld);
     memset(de_c, 0, sizeof(double) * (size_t)ld);
     for (int nnn = 1; nnn <= inne; nnn++) {
         if (nf[nnn] == IOB || fb[nnn] == ZERO) continue;
@@ -284,6 +302,8 @@ void ora_init_matrix(const int* dims, int inne, int mx2, const int* mn, const in
         int ll = 0;
         double de = ZERO;
         for (int l = 0; l <= 2; l++) {
+            if (g.is == g.ie - 1 && l == 0) continue;     /* nl = 4 (lines 34-35) */
+            if (g.js == g.je - 1 && l == 1) continue;
             ll++;
             for (int ii = -1; ii <= 1; ii += 2) {
                 int np = NBR(i, j, k, l, ii);
@@ -387,6 +407,7 @@ int ora_assemble(const int* dims, int inne, int inne2, int mx2, const int* in_,
                  const double* de_c, int mm2, double* alu, int* llu, double* de) {
     (void)mx2;
     grid_t g = mkgrid(dims);
+    const int nl = ora_grid_nl(dims);
     const double rate = -1.0e-20;
     long ldc = inne, ld = mm2;
     long spld = (long)inne2 + 2;
@@ -403,7 +424,7 @@ int ora_assemble(const int* dims, int inne, int inne2, int mx2, const int* in_,
         } else {
             return nnn;
         }
-        for (int ll = 1; ll <= 6; ll++) {
+        for (int ll = 1; ll <= nl; ll++) {
             long oc = (long)(ll - 1) * ldc + (nnn - 1);
             long o = (long)(ll - 1) * ld + (nn - 1);
             int lc = ll_c[oc];
@@ -422,6 +443,8 @@ int ora_assemble(const int* dims, int inne, int inne2, int mx2, const int* in_,
                         alu[o] = alu_c[oc];
                     } else {
                         int l = (ll + ll % 2) / 2 - 1;
+                        if (g.is == g.ie - 1) l = l + 1;            /* 2DV (lines 519-520) */
+                        if (g.js == g.je - 1 && ll > 2) l = l + 1;
                         if (iabs_(nfb[nnn]) - 1 == l) {
                             int ii = (l == 0) ? i : (l == 1) ? j : k;
                             int md = ll % 2;
@@ -820,13 +843,13 @@ void ora_correct(const int* dims, int inne, int mx2, const int* mn, const int* i
 /* Transposed ELL (adjoint support; no reference counterpart).  alu/llu are the
  * assembled arrays (1-based llu, leading dimension na); column d of row j names
  * the neighbour in direction d, so A(j,i) lands in row i at the opposite slot. */
-void ora_transpose(int n, int na, const double* alu, const int* llu, const double* de,
+void ora_transpose(int n, int na, int nl, const double* alu, const int* llu, const double* de,
                    double* alt, int* llt, double* det) {
-    for (int d = 0; d < 6; d++)
+    for (int d = 0; d < nl; d++)
         for (int r = 0; r < na; r++) { alt[(long)d * na + r] = ZERO; llt[(long)d * na + r] = 0; }
     for (int r = 0; r < n; r++) det[r] = de[r];
     for (int j = 1; j <= n; j++)
-        for (int d = 1; d <= 6; d++) {
+        for (int d = 1; d <= nl; d++) {
             int i = llu[(long)(d - 1) * na + (j - 1)];
             if (i == 0) continue;
             int od = (d % 2) ? d + 1 : d - 1;
@@ -835,11 +858,11 @@ void ora_transpose(int n, int na, const double* alu, const int* llu, const doubl
         }
 }
 
-void ora_spmv(int n, int na, const double* alu, const int* llu, const double* de,
+void ora_spmv(int n, int na, int nl, const double* alu, const int* llu, const double* de,
               const double* x, double* y) {
     for (int i = 1; i <= n; i++) {
         double s = de[i - 1] * x[i - 1];
-        for (int d = 1; d <= 6; d++) {
+        for (int d = 1; d <= nl; d++) {
             int c = llu[(long)(d - 1) * na + (i - 1)];
             if (c) s += alu[(long)(d - 1) * na + (i - 1)] * x[c - 1];
         }

@@ -41,6 +41,10 @@ int ora_set_nflag(const int* dims, int inne, int mx2, const int* mn, const int* 
                   const int* objno, int* fln, int* ifln, int* sfn, int* isfn);
 
 /* init_matrix (1sub-matrix.F90:3-66), 3D (nl = 6).  Writes mp. */
+/* Matrix columns of a grid: 6 (3D), 4 (2DV: one cell wide in x or y,
+ * main_2CLOWNS.F90:43-44, 1sub-matrix.F90:15-21) or 0 (one cell wide in both). */
+int ora_grid_nl(const int* dims);
+
 void ora_init_matrix(const int* dims, int inne, int mx2, const int* mn, const int* in_,
                      const int* jn, const int* kn, const int* nf, const int* nfb,
                      const double* a, const double* fb, const double* dx,
@@ -99,11 +103,11 @@ void ora_correct(const int* dims, int inne, int mx2, const int* mn, const int* i
 
 /* Transposed operator of an assembled (unscaled) ELL matrix: row i of the result
  * holds column i of A in the same direction slots.  No reference counterpart. */
-void ora_transpose(int n, int na, const double* alu, const int* llu, const double* de,
+void ora_transpose(int n, int na, int nl, const double* alu, const int* llu, const double* de,
                    double* alt, int* llt, double* det);
 
 /* y = A x on the assembled (unscaled) ELL matrix, 1-based llu, 0 = absent. */
-void ora_spmv(int n, int na, const double* alu, const int* llu, const double* de,
+void ora_spmv(int n, int na, int nl, const double* alu, const int* llu, const double* de,
               const double* x, double* y);
 
 #ifdef __cplusplus

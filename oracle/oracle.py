@@ -61,9 +61,11 @@ def lib():
             L.ora_correct.restype = None
             L.ora_correct.argtypes = [P, i, i, P, P, P, P, P, P, P, P, d, i, P, P, P, P, P]
             L.ora_transpose.restype = None
-            L.ora_transpose.argtypes = [i, i, P, P, P, P, P, P]
+            L.ora_transpose.argtypes = [i, i, i, P, P, P, P, P, P]
             L.ora_spmv.restype = None
-            L.ora_spmv.argtypes = [i, i, P, P, P, P, P]
+            L.ora_spmv.argtypes = [i, i, i, P, P, P, P, P]
+            L.ora_grid_nl.restype = i
+            L.ora_grid_nl.argtypes = [P]
             L.ora_pcgpme_will.restype = None
             L.ora_pcgpme_will.argtypes = [P, i, i, P, P, i, i, P, d, d, i, i, P, P]
             L.ora_will_postprocess.restype = None
@@ -113,15 +115,23 @@ def set_nflag(case) -> Classified:
 @dataclasses.dataclass
 class StaticMatrix:
     mp: float
-    alu_c: np.ndarray    # (6, inne) == ALU_C(1:inne, 1:6) column-major
-    ll_c: np.ndarray     # (6, inne)
+    alu_c: np.ndarray    # (nl, inne) == ALU_C(1:inne, 1:nl) column-major
+    ll_c: np.ndarray     # (nl, inne)
     de_c: np.ndarray     # (inne,)
+
+
+def grid_nl(dims) -> int:
+    """Matrix columns of a grid: 6 (3D), 4 (2DV: one cell wide in x or y) or 0."""
+    return int(lib().ora_grid_nl(_p(np.ascontiguousarray(dims, dtype=np.int32))))
 
 
 def init_matrix(case, cls: Classified) -> StaticMatrix:
     L = lib()
-    alu_c = np.zeros((6, case.inne), dtype=np.float64)
-    ll_c = np.zeros((6, case.inne), dtype=np.int32)
+    nl = grid_nl(case.dims)
+    if nl == 0:
+        raise ValueError("a grid one cell wide in both x and y has no matrix form in the reference")
+    alu_c = np.zeros((nl, case.inne), dtype=np.float64)
+    ll_c = np.zeros((nl, case.inne), dtype=np.int32)
     de_c = np.zeros(case.inne, dtype=np.float64)
     mp = C.c_double(0.0)
     L.ora_init_matrix(_p(case.dims), case.inne, case.mx2, _p(case.mn), _p(case.in_),
@@ -140,8 +150,8 @@ class System:
     b: np.ndarray        # (mm2+1,), element 0 unused
     de: np.ndarray       # (mm2+1,)
     xe: np.ndarray       # (mm2+1,) == xe(0:mm2)
-    alu: np.ndarray      # (6, mm2) == alu(1:mm2, 1:6)
-    llu: np.ndarray      # (6, mm2)
+    alu: np.ndarray      # (nl, mm2) == alu(1:mm2, 1:nl)
+    llu: np.ndarray      # (nl, mm2)
     dmax: float
 
 
@@ -164,8 +174,9 @@ def rows_rhs_assemble(case, cls: Classified, sm: StaticMatrix, mm2: int | None =
                           C.byref(dmax))
     if mnoe < 0:
         raise RuntimeError("matrix leading dimension too small")
-    alu = np.zeros((6, mm2))
-    llu = np.zeros((6, mm2), dtype=np.int32)
+    nl = sm.alu_c.shape[0]
+    alu = np.zeros((nl, mm2))
+    llu = np.zeros((nl, mm2), dtype=np.int32)
     bad = L.ora_assemble(_p(case.dims), case.inne, case.inne2, case.mx2, _p(case.in_),
                          _p(case.jn), _p(case.kn), _p(cls.nf), _p(cls.nfb), _p(case.x),
                          _p(case.dx), _p(case.sp), cls.ifln, _p(fln), _p(mno), _p(sm.alu_c),
@@ -193,7 +204,7 @@ def pcgpme(alu: np.ndarray, llu: np.ndarray, de: np.ndarray, b: np.ndarray, n: i
            eps: float = 1e-10, parm: float = 5.0, itmax: int = 10000, nthreads: int = 1,
            x0: np.ndarray | None = None) -> SolveResult:
     """Call the restated PCGPME on copies.  ``de``/``b`` are 0-based length >= n;
-    ``alu``/``llu`` are (6, na)."""
+    ``alu``/``llu`` are (nl, na)."""
     L = lib()
     nl, na = alu.shape
     assert na >= n + 64
@@ -292,7 +303,7 @@ def transpose(alu, llu, de, n):
     alt = np.zeros_like(alu)
     llt = np.zeros_like(llu)
     det = np.zeros(n)
-    L.ora_transpose(n, na, _p(np.ascontiguousarray(alu)), _p(np.ascontiguousarray(llu)),
+    L.ora_transpose(n, na, nl, _p(np.ascontiguousarray(alu)), _p(np.ascontiguousarray(llu)),
                     _p(np.ascontiguousarray(de[:n])), _p(alt), _p(llt), _p(det))
     return alt, llt, det
 
@@ -301,7 +312,7 @@ def spmv(alu, llu, de, n, x):
     L = lib()
     nl, na = alu.shape
     y = np.zeros(n)
-    L.ora_spmv(n, na, _p(np.ascontiguousarray(alu)), _p(np.ascontiguousarray(llu)),
+    L.ora_spmv(n, na, nl, _p(np.ascontiguousarray(alu)), _p(np.ascontiguousarray(llu)),
                _p(np.ascontiguousarray(de[:n])), _p(np.ascontiguousarray(x[:n], dtype=np.float64)),
                _p(y))
     return y
@@ -322,7 +333,7 @@ def to_csr(sy: System):
     rows = [np.arange(n)]
     cols = [np.arange(n)]
     vals = [sy.de[1:n + 1]]
-    for d in range(6):
+    for d in range(sy.llu.shape[0]):
         c = sy.llu[d, :n]
         m = c != 0
         rows.append(np.nonzero(m)[0])

@@ -8,9 +8,10 @@ wl = ge.load_package().workload
 
 def small_cases():
     """(label, Case) pairs covering flat tank, beach + obstacles + partial cells,
-    a bore front (x-oriented surface cells, corner cells), a shoreline, and a
+    a bore front (x-oriented surface cells, corner cells), a shoreline, a
     flume read from the reference's file format with boundary cells in the
-    full index range (wave boundaries, obstacle-surface cells, sentinels)."""
+    full index range (wave boundaries, obstacle-surface cells, sentinels), and
+    the 2DV mode in both orientations."""
     return [
         ("tank_24x20x16", wl.make_case(24, 20, 16, dz=0.025, partial=False, seed=0, eps0=1e-12)),
         ("beach_48x40x24", wl.beach_case(48, 40, 24, seed=5, n_obstacles=6)),
@@ -21,6 +22,12 @@ def small_cases():
         ("shore_64x16x24", wl.make_case(64, 16, 24, slope=1.0 / 3.0, n_obstacles=3, seed=11,
                                          amplitude=0.05)),
         ("flume_40x24x20_ingested", ingested_flume(True)[3].case),
+        # 2DV (NL = 4, main_2CLOWNS.F90:43-44): a wave flume one cell wide in y with a
+        # beach and a lowered surface step, and a y-z section one cell wide in x
+        ("flume2dv_96x1x32", wl.make_case(96, 1, 32, dz=0.8 / 32, slope=0.25, n_obstacles=0, seed=31,
+                                           amplitude=0.08, step_layers=2)),
+        ("section2dv_1x80x24", wl.make_case(1, 80, 24, dz=0.8 / 24, slope=None, n_obstacles=0, seed=32,
+                                             amplitude=0.05)),
     ]
 
 

@@ -6,7 +6,8 @@ these vectors pin the C oracle against an implementation that shares none of
 its code: scalar loops transcribed separately from
 
   set_nflag            src2LOWNS/nfd2015.F90:7-306, fxx1 308-332
-  init_matrix          src2LOWNS/1sub-matrix.F90:3-95
+  init_matrix          src2LOWNS/1sub-matrix.F90:3-95 (3D and the 2DV mode of a grid
+                       one cell wide in x or y, main_2CLOWNS.F90:43-44)
   rows + RHS           src2LOWNS/1sub-momentum.F90:265-360, 1sub-main.F90:579-602,
                        lib/src/math_func.F90:51-54
   cal_matrix_element   src2LOWNS/1sub-momentum.F90:465-551
@@ -40,6 +41,11 @@ def golden_cases():
                                      seed=22, amplitude=0.06),
         "bore_12x5x8": wl.make_case(12, 5, 8, dz=0.1, slope=None, n_obstacles=1, obstacle_frac=0.05,
                                     seed=23, amplitude=0.06, step_layers=2, step_at=0.5),
+        # 2DV (NL = 4): one cell wide in y (x-z flume), and one cell wide in x (y-z section)
+        "flume2dv_16x1x8": wl.make_case(16, 1, 8, dz=0.1, slope=0.25, n_obstacles=0, seed=24,
+                                        amplitude=0.06, step_layers=2, step_at=0.5),
+        "section2dv_1x14x8": wl.make_case(1, 14, 8, dz=0.1, slope=None, n_obstacles=0, seed=25,
+                                          amplitude=0.06),
     }
 
 
@@ -61,6 +67,10 @@ class Ref:
         self.jn = [int(v) for v in c.jn]
         self.kn = [int(v) for v in c.kn]
         self.objno = [int(v) for v in c.objno]
+        # 2DV switch of main_2CLOWNS.F90:43-44 and nl of init_matrix (1sub-matrix.F90:15-21)
+        self.cx = self.is_ == self.ie - 1
+        self.cy = self.js == self.je - 1
+        self.nl = 4 if (self.cx or self.cy) else 6
 
     def mn(self, i, k, j):
         return int(self.mn3[j - (self.js - 2), k - (self.ks - 2), i - (self.is_ - 2)])
@@ -197,6 +207,10 @@ def fxx1(R: Ref, ix, ll, i, j, k):
     for l in range(3):
         if l == ll:
             continue
+        if R.cx and l == 0:
+            continue
+        if R.cy and l == 1:
+            continue
         for ii in (-1, 0, 1):
             nnc = R.mn(lg[0] + ix * (ll == 0) + ii * (l == 0), lg[2] + ix * (ll == 2) + ii * (l == 2),
                        lg[1] + ix * (ll == 1) + ii * (l == 1))
@@ -209,12 +223,17 @@ def fxx1(R: Ref, ix, ll, i, j, k):
 
 
 def init_matrix(R: Ref):
-    dxs = [v for v in R.c.dx.ravel().tolist() if v > 0.0]
+    if R.nl == 6:
+        comps = (0, 1, 2)
+    else:                           # the later of the two 2DV assignments wins (lines 20-21)
+        comps = (0, 2) if R.cy else ()
+        comps = (1, 2) if R.cx else comps
+    dxs = [float(R.c.dx[i, l]) for i in range(R.c.dx.shape[0]) for l in comps if R.c.dx[i, l] > 0.0]
     m = min(dxs)
     mp = m * m
     n = R.c.inne
-    alu_c = [[0.0] * n for _ in range(6)]
-    ll_c = [[0] * n for _ in range(6)]
+    alu_c = [[0.0] * n for _ in range(R.nl)]
+    ll_c = [[0] * n for _ in range(R.nl)]
     de_c = [0.0] * n
     for nnn in range(1, n + 1):
         if R.nf[nnn] == -1 or R.fb[nnn] == 0.0:
@@ -222,11 +241,17 @@ def init_matrix(R: Ref):
         i, j, k = R.in_[nnn], R.jn[nnn], R.kn[nnn]
         lg = [i, j, k]
         de = 0.0
+        ll = 0
         for l in range(3):
+            if R.cx and l == 0:
+                continue
+            if R.cy and l == 1:
+                continue
+            ll += 1
             for side, ii in enumerate((-1, 1)):
                 np_ = R.nb(i, j, k, l, ii)
                 npp = R.nb(i, j, k, l, max(0, ii))
-                col = 2 * l + side
+                col = 2 * (ll - 1) + side
                 if (R.nf[np_] == -1 and R.nfb[np_] != 4) or R.a[npp][l] == 0.0 or R.fb[np_] == 0.0:
                     continue
                 dx, dxm = R.DX(l, lg[l]), R.DX(l, lg[l] + ii)
@@ -272,8 +297,8 @@ def rows_rhs_assemble(R: Ref, fln, mp, alu_c, ll_c, de_c, mm2):
             if not (abs(q) <= 1e-15 and abs(q) != 0.0):
                 b[r] = mp * dr1 / c.dt
             dmax = max(dmax, abs(dr1))
-    alu = [[0.0] * mm2 for _ in range(6)]
-    llu = [[0] * mm2 for _ in range(6)]
+    alu = [[0.0] * mm2 for _ in range(R.nl)]
+    llu = [[0] * mm2 for _ in range(R.nl)]
     de = [0.0] * (mm2 + 1)
     for nnn in fln[1:]:
         i, j, k = R.in_[nnn], R.jn[nnn], R.kn[nnn]
@@ -281,7 +306,7 @@ def rows_rhs_assemble(R: Ref, fln, mp, alu_c, ll_c, de_c, mm2):
         if nn == 0:
             continue
         de[nn] = de_c[nnn - 1] if R.nf[nnn] == 1 else 1.0
-        for ll in range(1, 7):
+        for ll in range(1, R.nl + 1):
             lc = ll_c[ll - 1][nnn - 1]
             if lc == 0:
                 continue
@@ -295,6 +320,10 @@ def rows_rhs_assemble(R: Ref, fln, mp, alu_c, ll_c, de_c, mm2):
                 alu[ll - 1][nn - 1] = alu_c[ll - 1][nnn - 1]
             else:
                 l = (ll + ll % 2) // 2 - 1
+                if R.cx:                        # 1sub-momentum.F90:519-520
+                    l = l + 1
+                if R.cy and ll > 2:
+                    l = l + 1
                 if abs(R.nfb[nnn]) - 1 == l:
                     ii = (i, j, k)[l]
                     md = ll % 2
@@ -311,31 +340,35 @@ def pcgpme(alu, llu, de, b, n, eps, parm=5.0, itmax=10000):
     P1 = parm if parm >= 1.0 else 4.0
     P2 = P1 + 1.0
     N2 = 64
-    AL = [[alu[k][i] for i in range(n)] for k in range(6)]
-    LL = [[llu[k][i] for i in range(n)] for k in range(6)]
+    NL = len(alu)
+    AL = [[alu[k][i] for i in range(n)] for k in range(NL)]
+    LL = [[llu[k][i] for i in range(n)] for k in range(NL)]
     D = [de[i + 1] for i in range(n)]
     B = [b[i + 1] for i in range(n)]
     for I in range(1, n + 1):
         w = 0.0
-        for K in range(6):
+        for K in range(NL):
             if LL[K][I - 1] == 0:
                 LL[K][I - 1] = n + 1 + I % 64
             w = w + abs(AL[K][I - 1])
         t = D[I - 1]
         w = P2 / (max(w, t) + t * P1)
-        for K in range(6):
+        for K in range(NL):
             AL[K][I - 1] = AL[K][I - 1] * w
         D[I - 1] = D[I - 1] * w
         B[I - 1] = B[I - 1] * w
     for I in range(n):
-        for K in range(5):
-            for KK in range(K + 1, 6):
+        for K in range(NL - 1):
+            for KK in range(K + 1, NL):
                 if abs(AL[K][I]) < abs(AL[KK][I]):
                     AL[K][I], AL[KK][I] = AL[KK][I], AL[K][I]
                     LL[K][I], LL[KK][I] = LL[KK][I], LL[K][I]
     L = n + N2
 
     def axsub(x):
+        if NL == 4:                     # vertical 2D (pcgpme_para.F90:340-345)
+            return [x[i] * D[i] + AL[0][i] * x[LL[0][i] - 1] + AL[1][i] * x[LL[1][i] - 1]
+                    + AL[2][i] * x[LL[2][i] - 1] + AL[3][i] * x[LL[3][i] - 1] for i in range(n)] + [0.0] * N2
         return [x[i] * D[i] + AL[0][i] * x[LL[0][i] - 1] + AL[1][i] * x[LL[1][i] - 1]
                 + AL[2][i] * x[LL[2][i] - 1] + AL[3][i] * x[LL[3][i] - 1]
                 + AL[4][i] * x[LL[4][i] - 1] + AL[5][i] * x[LL[5][i] - 1] for i in range(n)] + [0.0] * N2
@@ -345,6 +378,8 @@ def pcgpme(alu, llu, de, b, n, eps, parm=5.0, itmax=10000):
         q = [w[i] - AL[1][i] * w[LL[1][i] - 1] for i in range(n)] + p[n:]
         w = [q[i] - AL[2][i] * q[LL[2][i] - 1] for i in range(n)] + [0.0] * N2
         q = [w[i] - AL[3][i] * w[LL[3][i] - 1] for i in range(n)] + p[n:]
+        if NL <= 4:                     # sweeps 5 and 6 only when NL > 4 (pcgpme_para.F90:306)
+            return q
         w = [q[i] - AL[4][i] * q[LL[4][i] - 1] - AL[5][i] * q[LL[5][i] - 1] for i in range(n)]
         return w + p[n:]
 

@@ -20,7 +20,8 @@ def _golden():
     return m
 
 
-@pytest.mark.parametrize("name", ["tank_6x5x6", "beach_10x6x8", "bore_12x5x8"])
+@pytest.mark.parametrize("name", ["tank_6x5x6", "beach_10x6x8", "bore_12x5x8", "flume2dv_16x1x8",
+                                  "section2dv_1x14x8"])
 def test_oracle_matches_golden(ora, name):
     g = np.load(GOLD / f"{name}.npz")
     case = _golden().golden_cases()[name]
@@ -53,6 +54,25 @@ def test_golden_cases_cover_the_edge_cases():
     assert -3 in orient and (orient & {-1, 1}), orient
     assert int(g["passes"]) >= 2
     assert (g["alu"] == -1e-20).any()
+
+
+def test_golden_2dv_cases_use_four_columns(ora):
+    """A grid one cell wide in y (or x) takes the reference's 2DV form: NL = 4
+    columns over the x-z (y-z) plane, mp from those two axes only, the axis of
+    surface rows shifted past the collapsed one (main_2CLOWNS.F90:43-44,
+    1sub-matrix.F90:15-36, 1sub-momentum.F90:517-520); a grid one cell wide in
+    both has no defined form and is refused."""
+    for name, axes in (("flume2dv_16x1x8", (0, 2)), ("section2dv_1x14x8", (1, 2))):
+        g = np.load(GOLD / f"{name}.npz")
+        case = _golden().golden_cases()[name]
+        assert ora.grid_nl(case.dims) == 4
+        assert g["alu_c"].shape[0] == 4 and g["alu"].shape[0] == 4
+        dx = case.dx[:, list(axes)]
+        assert float(g["mp"]) == float(dx[dx > 0].min()) ** 2
+        # surface rows carry extrapolation coefficients on their normal axis
+        assert (g["alu"] != 0).any() and (g["alu"] == -1e-20).any()
+    col = wl.make_case(1, 1, 8, dz=0.1, slope=None, n_obstacles=0, seed=3, amplitude=0.0)
+    assert ora.grid_nl(col.dims) == 0
 
 
 def test_known_answer_interior_fluid_row(ora):
