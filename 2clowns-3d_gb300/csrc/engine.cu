@@ -324,6 +324,19 @@ static EngLayout eng_layout(int M, const int* n, int mixed, int wave = -1) {
     return L;
 }
 
+// Rows per block and stream of the balanced kernels' L2 prologue (0: none);
+// CLOWNS_L2_PREFETCH overrides the default.  Measured at 2.8 M rows (FP64 /
+// mixed ms per solve): 0 -> 117.2 / 72.4, 512 -> 116.1 / 71.5, 1024 -> 117.3 /
+// 71.9, 2048 and more -> 120.2 / 72.7-75.4 (prefetched lines evicted before use).
+constexpr int kL2PrefetchRows = 512;
+static int l2_prefetch_rows() {
+    static const int rows = [] {
+        const char* v = getenv("CLOWNS_L2_PREFETCH");
+        return v ? std::max(0, atoi(v)) : kL2PrefetchRows;
+    }();
+    return rows;
+}
+
 template <typename T>
 static Eng<T> eng_bind(void* work, const EngLayout& L) {
     char* b = (char*)work;
@@ -366,6 +379,7 @@ static Eng<T> eng_bind(void* work, const EngLayout& L) {
     for (int k = 0; k < kWaveBufs; k++) E.w[k] = L.wave ? (T*)(b + L.o_wbuf[k]) : nullptr;
     E.baltab = nullptr;       // set once the launch sizes are uploaded (upload_bal_tables)
     E.nl = 6;                 // set by the solve from its members' NL
+    E.pf = l2_prefetch_rows();
     E.balg = L.o_balg ? (const int*)(b + L.o_balg) : nullptr;
     return E;
 }
@@ -720,7 +734,7 @@ template <typename T>
 static std::string eng_key(const Eng<T>& E) {
     std::string k;
     auto put = [&](const auto& v) { k.append((const char*)&v, sizeof(v)); };
-    put(E.NV); put(E.M); put(E.nblk); put(E.n1); put(E.nl);
+    put(E.NV); put(E.M); put(E.nblk); put(E.n1); put(E.nl); put(E.pf);
     put(E.al); put(E.ll); put(E.d); put(E.r); put(E.p); put(E.r0); put(E.q); put(E.e); put(E.v); put(E.t);
     put(E.xi); put(E.W); put(E.x64); put(E.r64); put(E.s64); put(E.t64);
     put(E.blk_member); put(E.blk_rows); put(E.mem_off); put(E.mem_n); put(E.mem_nblk); put(E.mem_blk0);

@@ -134,6 +134,8 @@ struct Eng {
     const BalBlock* baltab;   // ensembles: 16 block tables of the balanced kernels (nullptr: none)
     const int* balg;          // ensembles: the blocks of each table's launch (16)
     int nl;                   // columns the members' matrices fill: 6 (3D) or 4 (2DH); the rest are empty
+    int pf;                   // balanced kernels: rows per block and stream asked of L2 before the
+                              // wait on the previous kernel (0: none)
 };
 
 // ---------------------------------------------------------------------------
@@ -891,11 +893,19 @@ __device__ __forceinline__ void ph_initres(const Eng<T>& E) {
 // with pdl_enter(): under programmatic dependent launch (graph mode) it lets the
 // next kernel's blocks be scheduled as this grid's blocks retire, then waits
 // for the previous grid to complete; without PDL both calls are no-ops.
-__device__ __forceinline__ void pdl_enter() {
+__device__ __forceinline__ void pdl_trigger() {
 #if defined(__CUDA_ARCH__) && (__CUDA_ARCH__ >= 900)
     cudaTriggerProgrammaticLaunchCompletion();
+#endif
+}
+__device__ __forceinline__ void pdl_wait() {
+#if defined(__CUDA_ARCH__) && (__CUDA_ARCH__ >= 900)
     cudaGridDependencySynchronize();
 #endif
+}
+__device__ __forceinline__ void pdl_enter() {
+    pdl_trigger();
+    pdl_wait();
 }
 
 template <typename T>
@@ -1008,6 +1018,35 @@ __device__ __forceinline__ bool bal_rows(const Eng<T>& E, const BalBlock* __rest
     return go;
 }
 
+// L2 prologue of the balanced kernels.  Under programmatic dependent launch a
+// kernel's blocks take the SM slots the previous kernel's blocks leave, while
+// that kernel's last block still runs its reduction tail (6-8 us in which HBM
+// has nothing to do).  Before waiting on the previous kernel, a block asks L2
+// for the first E.pf rows of its range of each stream it reads (the matrix and
+// the vectors the previous kernel does not write), so that those bytes arrive
+// during the tail.  A prefetch returns nothing to the thread: the values the
+// kernel computes with are loaded after the wait, whatever the prefetch found.
+// Single systems only: an ensemble block's rows come from a table that the loop
+// rewrites on the device.
+__device__ __forceinline__ void l2_prefetch_lines(const void* p0, const void* p1) {
+    const unsigned long long b = (unsigned long long)p1;
+    for (unsigned long long q = ((unsigned long long)p0 & ~127ull) + 128ull * threadIdx.x; q < b;
+         q += 128ull * blockDim.x)
+        asm volatile("prefetch.global.L2 [%0];" ::"l"(q));
+}
+template <typename T>
+__device__ __forceinline__ bool pf_range(const Eng<T>& E, const BalBlock* tab, long& lo, long& hi) {
+    if (E.pf <= 0 || tab) return false;
+    BalBlock bb;
+    bal_rows(E, tab, bb, lo, hi);
+    hi = min(hi, lo + (long)E.pf);
+    return lo < hi;
+}
+template <typename U>
+__device__ __forceinline__ void pf_rows(const U* s, long lo, long hi) {
+    l2_prefetch_lines(s + lo, s + hi);
+}
+
 template <typename T, int R>
 constexpr int kBalMinBlocks = R == 4 ? (sizeof(T) == 8 ? 3 : 4) : 1;
 
@@ -1027,8 +1066,18 @@ __device__ __forceinline__ void step_fence() { asm volatile("" ::: "memory"); }
 // columns hold zero coefficients at the zero row and are not read).
 template <typename T, int R, int NL>
 __global__ void __launch_bounds__(kEngBlock, kBalMinBlocks<T, R>) k_bal_axsub(Eng<T> E, const BalBlock* __restrict__ tab, const T* __restrict__ in, T* __restrict__ out) {
-    pdl_enter();
+    pdl_trigger();
     const long NV = E.NV;
+    long plo, phi;
+    if (pf_range(E, tab, plo, phi)) {
+        pf_rows(E.d, plo, phi);
+#pragma unroll
+        for (int k = 0; k < NL; k++) {
+            pf_rows(E.al + k * NV, plo, phi);
+            pf_rows(E.ll + k * NV, plo, phi);
+        }
+    }
+    pdl_wait();
     long lo, hi;
     BalBlock bb;
     if (!bal_rows(E, tab, bb, lo, hi)) return;
@@ -1064,11 +1113,16 @@ __global__ void __launch_bounds__(kEngBlock, kBalMinBlocks<T, R>) k_bal_axsub(En
 template <typename T, int R>
 __global__ void __launch_bounds__(kEngBlock, kBalMinBlocks<T, R>) k_bal_sweep(Eng<T> E, const BalBlock* __restrict__ tab, int k, const T* __restrict__ in,
                                                         T* __restrict__ out) {
-    pdl_enter();
+    pdl_trigger();
     const long NV = E.NV;
     const T* __restrict__ a = E.al + k * NV;
     const int* __restrict__ c = E.ll + k * NV;
     long lo, hi;
+    if (pf_range(E, tab, lo, hi)) {
+        pf_rows(a, lo, hi);
+        pf_rows(c, lo, hi);
+    }
+    pdl_wait();
     BalBlock bb;
     if (!bal_rows(E, tab, bb, lo, hi)) return;
     for (long base = lo + threadIdx.x; base < hi; base += (long)blockDim.x * R) {
@@ -1096,13 +1150,20 @@ __global__ void __launch_bounds__(kEngBlock, kBalMinBlocks<T, R>) k_bal_sweep(En
 template <typename T, int R>
 __global__ void __launch_bounds__(kEngBlock, kBalMinBlocks<T, R>) k_bal_sweep2(Eng<T> E, const BalBlock* __restrict__ tab, int k, const T* __restrict__ in,
                                                          T* __restrict__ out) {
-    pdl_enter();
+    pdl_trigger();
     const long NV = E.NV;
     const T* __restrict__ a0 = E.al + k * NV;
     const int* __restrict__ c0 = E.ll + k * NV;
     const T* __restrict__ a1 = a0 + NV;
     const int* __restrict__ c1 = c0 + NV;
     long lo, hi;
+    if (pf_range(E, tab, lo, hi)) {
+        pf_rows(a0, lo, hi);
+        pf_rows(c0, lo, hi);
+        pf_rows(a1, lo, hi);
+        pf_rows(c1, lo, hi);
+    }
+    pdl_wait();
     BalBlock bb;
     if (!bal_rows(E, tab, bb, lo, hi)) return;
     for (long base = lo + threadIdx.x; base < hi; base += (long)blockDim.x * R) {
@@ -1156,12 +1217,26 @@ __device__ __forceinline__ void bal_flush(const Eng<T>& E, T (&v)[B * NVAL], lon
 // NL = 4: a copy with the reduction
 template <typename T, int MODE, int R, int NL>
 __global__ void __launch_bounds__(kEngBlock, kBalMinBlocks<T, R>) k_bal_sweep56(Eng<T> E, const BalBlock* __restrict__ tab, const T* __restrict__ in, T* __restrict__ out) {
-    pdl_enter();
+    pdl_trigger();
     const long NV = E.NV;
     const T* __restrict__ a5 = E.al + 4 * NV;
     const T* __restrict__ a6 = E.al + 5 * NV;
     const int* __restrict__ c5 = E.ll + 4 * NV;
     const int* __restrict__ c6 = E.ll + 5 * NV;
+    {
+        long plo, phi;
+        if (pf_range(E, tab, plo, phi)) {
+            if (NL == 6) {
+                pf_rows(a5, plo, phi);
+                pf_rows(c5, plo, phi);
+                pf_rows(a6, plo, phi);
+                pf_rows(c6, plo, phi);
+            }
+            if (MODE == 1) pf_rows(E.r0, plo, phi);
+            if (MODE == 2) pf_rows(E.e, plo, phi);
+        }
+    }
+    pdl_wait();
     BalBlock bb;
     long off;
     int n, c0, c1;
@@ -1232,8 +1307,10 @@ __global__ void __launch_bounds__(kEngBlock, kBalMinBlocks<T, R>) k_bal_sweep56(
 
 template <typename T, int R>
 __global__ void __launch_bounds__(kEngBlock, kBalMinBlocks<T, R>) k_bal_eupdate(Eng<T> E, const BalBlock* __restrict__ tab) {
-    pdl_enter();
+    pdl_trigger();
     long lo, hi;
+    if (pf_range(E, tab, lo, hi)) pf_rows(E.r, lo, hi);
+    pdl_wait();
     BalBlock bb;
     if (!bal_rows(E, tab, bb, lo, hi)) return;
     const T ALP = T(sld(&E.S[bb.m].ALP));
@@ -1256,7 +1333,18 @@ __global__ void __launch_bounds__(kEngBlock, kBalMinBlocks<T, R>) k_bal_eupdate(
 
 template <typename T, int R>
 __global__ void __launch_bounds__(kEngBlock, kBalMinBlocks<T, R>) k_bal_xrupdate(Eng<T> E, const BalBlock* __restrict__ tab) {
-    pdl_enter();
+    pdl_trigger();
+    {
+        long plo, phi;
+        if (pf_range(E, tab, plo, phi)) {
+            pf_rows(E.e, plo, phi);
+            pf_rows(E.xi, plo, phi);
+            pf_rows(E.p, plo, phi);
+            pf_rows(E.v, plo, phi);
+            pf_rows(E.r0, plo, phi);
+        }
+    }
+    pdl_wait();
     BalBlock bb;
     long off;
     int n, c0, c1;
@@ -1314,8 +1402,14 @@ __global__ void __launch_bounds__(kEngBlock, kBalMinBlocks<T, R>) k_bal_xrupdate
 
 template <typename T, int R>
 __global__ void __launch_bounds__(kEngBlock, kBalMinBlocks<T, R>) k_bal_pupdate(Eng<T> E, const BalBlock* __restrict__ tab) {
-    pdl_enter();
+    pdl_trigger();
     long lo, hi;
+    if (pf_range(E, tab, lo, hi)) {
+        pf_rows(E.r, lo, hi);
+        pf_rows(E.p, lo, hi);
+        pf_rows(E.q, lo, hi);
+    }
+    pdl_wait();
     BalBlock bb;
     if (!bal_rows(E, tab, bb, lo, hi)) return;
     const T BETA = T(sld(&E.S[bb.m].BETA)), AMU = T(sld(&E.S[bb.m].AMU));
