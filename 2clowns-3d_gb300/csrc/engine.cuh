@@ -1062,6 +1062,30 @@ constexpr int kBalBatch = (sizeof(T) == 8 && R == 4 && NVAL == 2) ? 1 : 4;
 // register budgets assume.
 __device__ __forceinline__ void step_fence() { asm volatile("" ::: "memory"); }
 
+// Chunk mapping of the element-wise balanced kernels (as the dot-product ones):
+// warp w of a block takes the block's chunks c0 + CPS w', c0 + CPS (w' + 8), ...
+// (CPS = R / 4 chunks per step, w' = w rotated by the block index, so that the
+// block's last, incomplete round of chunks does not always fall on the same SM
+// sub-partitions) and lane l row 32 u + l of each chunk.  A warp whose chunk
+// lies past the block's range leaves the loop: only the member's last chunk
+// has lanes without a row (ok = false), which compute on row `off` and store
+// nothing.
+__device__ __forceinline__ int bal_warp() {
+    const int nw = blockDim.x >> 5;
+    return (int)(((threadIdx.x >> 5) + blockIdx.x) % nw);
+}
+template <int R>
+__device__ __forceinline__ void chunk_step(long off, int n, int cb, int c1, long (&i)[R], bool (&ok)[R]) {
+    const int lane = threadIdx.x & 31;
+#pragma unroll
+    for (int u = 0; u < R; u++) {
+        const int cc = cb + u / kChunkRows;
+        const long r = (long)cc * kChunk + 32 * (u % kChunkRows) + lane;
+        ok[u] = cc < c1 && r < n;
+        i[u] = off + (ok[u] ? r : 0);
+    }
+}
+
 // NL: the columns the matrix fills (6, or 4 for a 2DH system, whose two empty
 // columns hold zero coefficients at the zero row and are not read).
 template <typename T, int R, int NL>
@@ -1078,35 +1102,34 @@ __global__ void __launch_bounds__(kEngBlock, kBalMinBlocks<T, R>) k_bal_axsub(En
         }
     }
     pdl_wait();
-    long lo, hi;
     BalBlock bb;
-    if (!bal_rows(E, tab, bb, lo, hi)) return;
-    for (long base = lo + threadIdx.x; base < hi; base += (long)blockDim.x * R) {
-        T s[R];
+    long off;
+    int n, c0, c1;
+    if (!bal_block(E, tab, bb, off, n, c0, c1)) return;
+    constexpr int CPS = R / kChunkRows;
+    const int nw = blockDim.x >> 5;
+    for (int cb = c0 + bal_warp() * CPS; cb < c1; cb += nw * CPS) {
+        long i[R];
         bool ok[R];
+        chunk_step<R>(off, n, cb, c1, i, ok);
+        T s[R];
 #pragma unroll
-        for (int u = 0; u < R; u++) {
-            const long r = base + (long)u * blockDim.x;
-            ok[u] = r < hi;
-            const long i = ok[u] ? r : lo;
-            s[u] = ldg2(in + i) * ld_stream(E.d + i);
-        }
+        for (int u = 0; u < R; u++) s[u] = ldg2(in + i[u]) * ld_stream(E.d + i[u]);
 #pragma unroll
         for (int k = 0; k < NL; k++) {
             T a[R];
             int c[R];
 #pragma unroll
             for (int u = 0; u < R; u++) {
-                const long i = ok[u] ? base + (long)u * blockDim.x : lo;
-                a[u] = ld_stream(E.al + k * NV + i);
-                c[u] = ld_stream(E.ll + k * NV + i);
+                a[u] = ld_stream(E.al + k * NV + i[u]);
+                c[u] = ld_stream(E.ll + k * NV + i[u]);
             }
 #pragma unroll
             for (int u = 0; u < R; u++) s[u] = fma_rn(a[u], ldg2(in + c[u]), s[u]);
         }
 #pragma unroll
         for (int u = 0; u < R; u++)
-            if (ok[u]) out[base + (long)u * blockDim.x] = s[u];
+            if (ok[u]) out[i[u]] = s[u];
     }
 }
 
@@ -1124,25 +1147,28 @@ __global__ void __launch_bounds__(kEngBlock, kBalMinBlocks<T, R>) k_bal_sweep(En
     }
     pdl_wait();
     BalBlock bb;
-    if (!bal_rows(E, tab, bb, lo, hi)) return;
-    for (long base = lo + threadIdx.x; base < hi; base += (long)blockDim.x * R) {
+    long off;
+    int n, c0, c1;
+    if (!bal_block(E, tab, bb, off, n, c0, c1)) return;
+    constexpr int CPS = R / kChunkRows;
+    const int nw = blockDim.x >> 5;
+    for (int cb = c0 + bal_warp() * CPS; cb < c1; cb += nw * CPS) {
+        long i[R];
+        bool ok[R];
+        chunk_step<R>(off, n, cb, c1, i, ok);
         T av[R], xv[R], gv[R];
         int cv[R];
-        bool ok[R];
 #pragma unroll
         for (int u = 0; u < R; u++) {
-            const long r = base + (long)u * blockDim.x;
-            ok[u] = r < hi;
-            const long i = ok[u] ? r : lo;
-            av[u] = ld_stream(a + i);
-            cv[u] = ld_stream(c + i);
-            xv[u] = ldg2(in + i);
+            av[u] = ld_stream(a + i[u]);
+            cv[u] = ld_stream(c + i[u]);
+            xv[u] = ldg2(in + i[u]);
         }
 #pragma unroll
         for (int u = 0; u < R; u++) gv[u] = ldg2(in + cv[u]);
 #pragma unroll
         for (int u = 0; u < R; u++)
-            if (ok[u]) out[base + (long)u * blockDim.x] = fnma(av[u], gv[u], xv[u]);
+            if (ok[u]) out[i[u]] = fnma(av[u], gv[u], xv[u]);
     }
 }
 
@@ -1165,21 +1191,24 @@ __global__ void __launch_bounds__(kEngBlock, kBalMinBlocks<T, R>) k_bal_sweep2(E
     }
     pdl_wait();
     BalBlock bb;
-    if (!bal_rows(E, tab, bb, lo, hi)) return;
-    for (long base = lo + threadIdx.x; base < hi; base += (long)blockDim.x * R) {
+    long off;
+    int n, k0, k1;
+    if (!bal_block(E, tab, bb, off, n, k0, k1)) return;
+    constexpr int CPS = R / kChunkRows;
+    const int nw = blockDim.x >> 5;
+    for (int kb = k0 + bal_warp() * CPS; kb < k1; kb += nw * CPS) {
+        long i[R];
+        bool ok[R];
+        chunk_step<R>(off, n, kb, k1, i, ok);
         T x[R], aa[R], ab[R], xj[R], aj[R];
         int ca[R], cb[R], cj[R];
-        bool ok[R];
 #pragma unroll
         for (int u = 0; u < R; u++) {
-            const long r = base + (long)u * blockDim.x;
-            ok[u] = r < hi;
-            const long i = ok[u] ? r : lo;
-            x[u] = ldg2(in + i);
-            aa[u] = ld_stream(a0 + i);
-            ca[u] = ld_stream(c0 + i);
-            ab[u] = ld_stream(a1 + i);
-            cb[u] = ld_stream(c1 + i);
+            x[u] = ldg2(in + i[u]);
+            aa[u] = ld_stream(a0 + i[u]);
+            ca[u] = ld_stream(c0 + i[u]);
+            ab[u] = ld_stream(a1 + i[u]);
+            cb[u] = ld_stream(c1 + i[u]);
         }
 #pragma unroll
         for (int u = 0; u < R; u++) {
@@ -1195,7 +1224,7 @@ __global__ void __launch_bounds__(kEngBlock, kBalMinBlocks<T, R>) k_bal_sweep2(E
         }
 #pragma unroll
         for (int u = 0; u < R; u++)
-            if (ok[u]) out[base + (long)u * blockDim.x] = fnma(ab[u], oj[u], oi[u]);
+            if (ok[u]) out[i[u]] = fnma(ab[u], oj[u], oi[u]);
     }
 }
 
@@ -1312,22 +1341,25 @@ __global__ void __launch_bounds__(kEngBlock, kBalMinBlocks<T, R>) k_bal_eupdate(
     if (pf_range(E, tab, lo, hi)) pf_rows(E.r, lo, hi);
     pdl_wait();
     BalBlock bb;
-    if (!bal_rows(E, tab, bb, lo, hi)) return;
+    long off;
+    int n, c0, c1;
+    if (!bal_block(E, tab, bb, off, n, c0, c1)) return;
     const T ALP = T(sld(&E.S[bb.m].ALP));
-    for (long base = lo + threadIdx.x; base < hi; base += (long)blockDim.x * R) {
+    constexpr int CPS = R / kChunkRows;
+    const int nw = blockDim.x >> 5;
+    for (int cb = c0 + bal_warp() * CPS; cb < c1; cb += nw * CPS) {
+        long i[R];
+        bool ok[R];
+        chunk_step<R>(off, n, cb, c1, i, ok);
         T rv[R], qv[R];
 #pragma unroll
         for (int u = 0; u < R; u++) {
-            const long r = base + (long)u * blockDim.x;
-            const long i = r < hi ? r : lo;
-            rv[u] = ldg2(E.r + i);
-            qv[u] = ldg2(E.q + i);
+            rv[u] = ldg2(E.r + i[u]);
+            qv[u] = ldg2(E.q + i[u]);
         }
 #pragma unroll
-        for (int u = 0; u < R; u++) {
-            const long r = base + (long)u * blockDim.x;
-            if (r < hi) E.e[r] = fnma(ALP, qv[u], rv[u]);
-        }
+        for (int u = 0; u < R; u++)
+            if (ok[u]) E.e[i[u]] = fnma(ALP, qv[u], rv[u]);
     }
 }
 
@@ -1411,23 +1443,26 @@ __global__ void __launch_bounds__(kEngBlock, kBalMinBlocks<T, R>) k_bal_pupdate(
     }
     pdl_wait();
     BalBlock bb;
-    if (!bal_rows(E, tab, bb, lo, hi)) return;
+    long off;
+    int n, c0, c1;
+    if (!bal_block(E, tab, bb, off, n, c0, c1)) return;
     const T BETA = T(sld(&E.S[bb.m].BETA)), AMU = T(sld(&E.S[bb.m].AMU));
-    for (long base = lo + threadIdx.x; base < hi; base += (long)blockDim.x * R) {
+    constexpr int CPS = R / kChunkRows;
+    const int nw = blockDim.x >> 5;
+    for (int cb = c0 + bal_warp() * CPS; cb < c1; cb += nw * CPS) {
+        long i[R];
+        bool ok[R];
+        chunk_step<R>(off, n, cb, c1, i, ok);
         T rv[R], pv[R], qv[R];
 #pragma unroll
         for (int u = 0; u < R; u++) {
-            const long r = base + (long)u * blockDim.x;
-            const long i = r < hi ? r : lo;
-            rv[u] = ldg2(E.r + i);
-            pv[u] = ldg2(E.p + i);
-            qv[u] = ldg2(E.q + i);
+            rv[u] = ldg2(E.r + i[u]);
+            pv[u] = ldg2(E.p + i[u]);
+            qv[u] = ldg2(E.q + i[u]);
         }
 #pragma unroll
-        for (int u = 0; u < R; u++) {
-            const long r = base + (long)u * blockDim.x;
-            if (r < hi) E.p[r] = fma_rn(BETA, fnma(AMU, qv[u], pv[u]), rv[u]);
-        }
+        for (int u = 0; u < R; u++)
+            if (ok[u]) E.p[i[u]] = fma_rn(BETA, fnma(AMU, qv[u], pv[u]), rv[u]);
     }
 }
 
