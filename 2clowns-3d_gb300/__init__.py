@@ -106,6 +106,7 @@ _SIGS = {
     "clowns_tuned_shape": (C.c_int, [C.c_int, C.c_void_p, C.c_int, C.c_void_p, C.c_void_p, C.c_void_p,
                                      C.c_void_p, C.c_void_p]),
     "clowns_last_kernel_launches": (C.c_long, []),
+    "clowns_fp64_fma_rate": (C.c_int, [C.c_void_p, C.c_void_p]),
     "clowns_test_arm_wait_timeout": (C.c_int, [C.c_long, C.c_int]),
     "clowns_session_create": (C.c_int, [C.c_void_p, C.c_void_p, C.c_int, C.c_int, C.c_int] + [C.c_void_p] * 7),
     "clowns_session_set_fields": (C.c_int, [C.c_void_p] * 9),
@@ -402,6 +403,16 @@ def last_kernel_launches():
     """Kernels the calling thread's last solve launched (host launches plus the
     kernel nodes executed inside loop graphs)."""
     return int(lib().clowns_last_kernel_launches())
+
+
+def fp64_fma_rate(stream=None):
+    """Measured FP64 fused multiply-add rate of the current device (lane
+    operations per second): the ceiling of the FP64 solve's arithmetic."""
+    import torch
+    s = stream if stream is not None else torch.cuda.current_stream()
+    out = C.c_double(0.0)
+    _check(lib().clowns_fp64_fma_rate(C.byref(out), C.c_void_p(s.cuda_stream)), "fp64_fma_rate")
+    return out.value
 
 
 class Member(C.Structure):

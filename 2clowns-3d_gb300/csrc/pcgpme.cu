@@ -114,6 +114,53 @@ extern "C" int clowns_tuned_shape(int m, const int* n, int precision, int* mode,
 
 extern "C" long clowns_last_kernel_launches(void) { return engine_last_launches(); }
 
+// FP64 pipe probe: eight independent fused multiply-add chains per thread, no
+// memory traffic in the loop, 8 blocks of 256 threads per SM.  The measured
+// rate bounds the FP64 solve's arithmetic the way the copy bandwidth bounds its
+// streams.
+static __device__ double g_fma_sink;
+static __global__ void __launch_bounds__(256) k_fma_rate(int iters, double a, double b) {
+    double v[8];
+#pragma unroll
+    for (int j = 0; j < 8; j++) v[j] = threadIdx.x * 1e-9 + j;
+    for (int i = 0; i < iters; i++) {
+#pragma unroll
+        for (int j = 0; j < 8; j++) v[j] = __fma_rn(v[j], a, b);
+    }
+    double s = 0.0;
+#pragma unroll
+    for (int j = 0; j < 8; j++) s += v[j];
+    if (s == 1.5e300) g_fma_sink = s;   // never true; keeps the chains
+}
+
+extern "C" int clowns_fp64_fma_rate(double* fma_per_s, void* stream) {
+    if (!fma_per_s) {
+        set_last_error_msg("fp64_fma_rate: fma_per_s is null");
+        return CLOWNS_ERR_ARG;
+    }
+    cudaStream_t s = (cudaStream_t)stream;
+    int dev = 0, sms = 0;
+    CLOWNS_CUDA_TRY(cudaGetDevice(&dev));
+    CLOWNS_CUDA_TRY(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
+    const int blocks = 8 * sms, threads = 256, iters = 1024, reps = 3;
+    cudaEvent_t e0, e1;
+    CLOWNS_CUDA_TRY(cudaEventCreate(&e0));
+    CLOWNS_CUDA_TRY(cudaEventCreate(&e1));
+    k_fma_rate<<<blocks, threads, 0, s>>>(iters, 0.999999, 1e-7);     // warm-up
+    cudaEventRecord(e0, s);
+    for (int r = 0; r < reps; r++) k_fma_rate<<<blocks, threads, 0, s>>>(iters, 0.999999, 1e-7);
+    cudaEventRecord(e1, s);
+    const cudaError_t err = cudaEventSynchronize(e1);
+    float ms = 0.f;
+    if (err == cudaSuccess) cudaEventElapsedTime(&ms, e0, e1);
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    CLOWNS_CUDA_TRY(err);
+    CLOWNS_CUDA_TRY(cudaGetLastError());
+    *fma_per_s = (double)blocks * threads * iters * 8.0 * reps / (ms * 1e-3);
+    return CLOWNS_OK;
+}
+
 extern "C" int clowns_test_arm_wait_timeout(long polls, int absent_block) {
     if (polls < 1 || absent_block < 0) {
         set_last_error_msg("test_arm_wait_timeout: polls >= 1 and absent_block >= 0 required");

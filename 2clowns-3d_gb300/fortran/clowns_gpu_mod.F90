@@ -152,6 +152,13 @@ module clowns_gpu
             import :: c_long
         end function clowns_last_kernel_launches
 
+        ! measured FP64 fused multiply-add rate of the device (lane operations per second)
+        integer(c_int) function clowns_fp64_fma_rate(fma_per_s, stream) bind(C, name="clowns_fp64_fma_rate")
+            import :: c_int, c_double, c_ptr
+            real(c_double), intent(out) :: fma_per_s
+            type(c_ptr), value :: stream
+        end function clowns_fp64_fma_rate
+
         ! ---- PCGPME_WILL (2DH dispersion solve) --------------------------------------
         ! host arrays; B in: RHS, out: what the reference leaves in B
         integer(c_int) function pcgpme_will_gpu(al, nl, na, ll, d, n, n2, b, eps, parm, iter) &

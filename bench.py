@@ -56,8 +56,16 @@ def measured_peaks():
 # accumulation; 96 B for the FP64 -> FP32 conversion).
 # Measured DRAM bytes per row and iteration of the loop graph (ncu, the graph as
 # one unit, beach_256x256x96): profiles/pcgpme_loop_dram_beach_256x256x96.md.
-TRAFFIC_ROW_ITER_FP64 = 448.7
-TRAFFIC_ROW_ITER_MIXED = 252.1
+TRAFFIC_ROW_ITER_FP64 = 435.6
+TRAFFIC_ROW_ITER_MIXED = 250.9
+
+# FP64 arithmetic of one iteration per row, in fused multiply-adds (a multiply or
+# an add counts as one): AXSUB D x + 6 AL = 7 and LDUSUB 6 sweeps = 6 per
+# application (26 for two), RQ 1, e 1, AMU and SS 2, x 2, r 1, RN and C1 2, p 2
+# -> 37 (pcgpme_para.F90:147-352).  The kernels issue about 41 (ncu counters:
+# warp sums of the dot products and rows of partial chunks):
+# profiles/pcgpme_reduction_kernels_full_beach_192x192x64.md.
+FMA_ROW_ITER_FP64 = 37
 
 
 def bytes_solve_fp64(n: int, iters: int) -> float:
@@ -602,6 +610,8 @@ def run_gpu(args, world, rank, local):
     peak, peak_kind = measured_peaks()
     alg = bytes_solve_fp64(n, it)
     achieved = alg / per_solve_s / 1e9
+    args.fma_peak = pkg.fp64_fma_rate(stream)          # measured here, outside the timed region
+    args.fma_achieved = FMA_ROW_ITER_FP64 * float(n) * it / per_solve_s
     x_plain = x[:n].cpu().numpy().copy()
     args.res_plain = true_residual(ds, x)
 
@@ -733,6 +743,11 @@ def _report(pkg, args, world, rank, case, n, ms, infos, info, it, value, alg, ac
                                            "profiles/pcgpme_loop_dram_beach_256x256x96.md",
                          "frac_with_index_streams": bytes_solve_fp64_with_indices(n, it) / alg * achieved / peak,
                          "algorithmic_bytes_per_solve": alg},
+            "roofline_fp64": {"bound": "fp64", "kernel": "pcgpme FP64 solve (one graph launch)",
+                              "achieved": args.fma_achieved / 1e9, "peak": args.fma_peak / 1e9,
+                              "peak_kind": "measured (clowns_fp64_fma_rate, this run)", "unit": "G FMA/s",
+                              "frac": args.fma_achieved / args.fma_peak,
+                              "fma_per_row_iter": FMA_ROW_ITER_FP64},
             "e2e": {"value": e2e_value, "unit": "solves/s", "h2d_bytes_per_step": h2d,
                     "d2h_bytes_per_step": d2h},
             "gpu_launches": args.timed_launches,

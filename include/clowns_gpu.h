@@ -204,6 +204,12 @@ int clowns_test_arm_wait_timeout(long polls, int absent_block);
  * Engine bookkeeping with no counterpart in the reference. */
 long clowns_last_kernel_launches(void);
 
+/* Measured FP64 fused multiply-add rate of the current device (lane operations
+ * per second, independent chains with no memory traffic): the ceiling of the
+ * FP64 solve's arithmetic, reported beside the copy bandwidth.  About 40 ms on
+ * `stream`.  Diagnostic with no counterpart in the reference. */
+int clowns_fp64_fma_rate(double* fma_per_s, void* stream);
+
 /* PCGPME_WILL, the 2DH dispersion solve (replaces src2LOWNS/pcgpme_2DH.f90:1-374,
  * called at 1sub-2DH-momentum.f90:325 as PCGPME_WILL(L%AL,4,L%indisp,L%LL,
  * L%DIAG,L%indisp,64,PSI,eps0,PARM,ITER)).  The same preconditioned BiCGSTAB
