@@ -142,22 +142,32 @@ extern "C" int clowns_fp64_fma_rate(double* fma_per_s, void* stream) {
     int dev = 0, sms = 0;
     CLOWNS_CUDA_TRY(cudaGetDevice(&dev));
     CLOWNS_CUDA_TRY(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
-    const int blocks = 8 * sms, threads = 256, iters = 1024, reps = 3;
-    cudaEvent_t e0, e1;
-    CLOWNS_CUDA_TRY(cudaEventCreate(&e0));
-    CLOWNS_CUDA_TRY(cudaEventCreate(&e1));
-    k_fma_rate<<<blocks, threads, 0, s>>>(iters, 0.999999, 1e-7);     // warm-up
-    cudaEventRecord(e0, s);
-    for (int r = 0; r < reps; r++) k_fma_rate<<<blocks, threads, 0, s>>>(iters, 0.999999, 1e-7);
-    cudaEventRecord(e1, s);
-    const cudaError_t err = cudaEventSynchronize(e1);
-    float ms = 0.f;
-    if (err == cudaSuccess) cudaEventElapsedTime(&ms, e0, e1);
-    cudaEventDestroy(e0);
-    cudaEventDestroy(e1);
+    // 5.1 G FMAs per launch (about 9 ms); two warm-up launches, then the best
+    // of five timed ones
+    const int blocks = 8 * sms, threads = 256, iters = 2048, warm = 2, reps = 5;
+    cudaEvent_t ev[2 * reps];
+    int made = 0;
+    cudaError_t err = cudaSuccess;
+    while (made < 2 * reps && (err = cudaEventCreate(&ev[made])) == cudaSuccess) made++;
+    if (err == cudaSuccess) {
+        for (int r = 0; r < warm; r++) k_fma_rate<<<blocks, threads, 0, s>>>(iters, 0.999999, 1e-7);
+        for (int r = 0; r < reps; r++) {
+            cudaEventRecord(ev[2 * r], s);
+            k_fma_rate<<<blocks, threads, 0, s>>>(iters, 0.999999, 1e-7);
+            cudaEventRecord(ev[2 * r + 1], s);
+        }
+        err = cudaEventSynchronize(ev[2 * reps - 1]);
+    }
+    float best = 0.f;
+    for (int r = 0; r < reps && err == cudaSuccess; r++) {
+        float ms = 0.f;
+        err = cudaEventElapsedTime(&ms, ev[2 * r], ev[2 * r + 1]);
+        if (r == 0 || ms < best) best = ms;
+    }
+    for (int k = 0; k < made; k++) cudaEventDestroy(ev[k]);
     CLOWNS_CUDA_TRY(err);
     CLOWNS_CUDA_TRY(cudaGetLastError());
-    *fma_per_s = (double)blocks * threads * iters * 8.0 * reps / (ms * 1e-3);
+    *fma_per_s = (double)blocks * threads * iters * 8.0 / (best * 1e-3);
     return CLOWNS_OK;
 }
 

@@ -56,15 +56,15 @@ def measured_peaks():
 # accumulation; 96 B for the FP64 -> FP32 conversion).
 # Measured DRAM bytes per row and iteration of the loop graph (ncu, the graph as
 # one unit, beach_256x256x96): profiles/pcgpme_loop_dram_beach_256x256x96.md.
-TRAFFIC_ROW_ITER_FP64 = 435.6
-TRAFFIC_ROW_ITER_MIXED = 250.9
+TRAFFIC_ROW_ITER_FP64 = 434.7
+TRAFFIC_ROW_ITER_MIXED = 250.6
 
 # FP64 arithmetic of one iteration per row, in fused multiply-adds (a multiply or
 # an add counts as one): AXSUB D x + 6 AL = 7 and LDUSUB 6 sweeps = 6 per
 # application (26 for two), RQ 1, e 1, AMU and SS 2, x 2, r 1, RN and C1 2, p 2
 # -> 37 (pcgpme_para.F90:147-352).  The kernels issue about 41 (ncu counters:
 # warp sums of the dot products and rows of partial chunks):
-# profiles/pcgpme_reduction_kernels_full_beach_192x192x64.md.
+# profiles/pcgpme_kernels_full_beach_192x192x64.md.
 FMA_ROW_ITER_FP64 = 37
 
 

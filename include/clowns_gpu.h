@@ -206,8 +206,8 @@ long clowns_last_kernel_launches(void);
 
 /* Measured FP64 fused multiply-add rate of the current device (lane operations
  * per second, independent chains with no memory traffic): the ceiling of the
- * FP64 solve's arithmetic, reported beside the copy bandwidth.  About 40 ms on
- * `stream`.  Diagnostic with no counterpart in the reference. */
+ * FP64 solve's arithmetic, reported beside the copy bandwidth: the best of five
+ * timed launches of 5.1 G FMAs after two warm-ups, about 70 ms on `stream`.  Diagnostic with no counterpart in the reference. */
 int clowns_fp64_fma_rate(double* fma_per_s, void* stream);
 
 /* PCGPME_WILL, the 2DH dispersion solve (replaces src2LOWNS/pcgpme_2DH.f90:1-374,

@@ -90,12 +90,22 @@ def test_operator_apply(gpu, ora, prepared, label):
 
 @pytest.mark.parametrize("label", IDS)
 def test_solve_matches_oracle(gpu, ora, prepared, label):
-    """Converged pressure within 1e-10 relative L2 of the oracle's PCGPME when both
-    solve to 1e-13 (at the nominal tolerance both carry ~1e-10 solver error)."""
+    """Converged pressure against the oracle's PCGPME (serial) on the same system.
+
+    Solved to ERR <= 1e-13 both pressures agree within 1e-11 relative L2
+    (measured: at most 4.1e-13 over these cases).  At the case's own tolerance
+    eps each carries its own solver error: they agree within 10 eps (measured:
+    at most 4.1 eps), and the GPU pressure's true residual ||b - A x|| / ||b||,
+    checked against the assembled matrix without the oracle's solve, is within
+    2 eps (measured: at most 1.02 eps).  Iteration counts follow rounding near
+    the stop tests (pcgpme_para.F90:228-232) and must agree within a sixth
+    (measured: at most 13.6 %)."""
     import torch
     case, cls, sm, sy, dc, ds = prepared[label]
     n = sy.mnoe
     solver = gpu.Solver(n)
+    A = ora.to_csr(sy)
+    b = sy.b[1:n + 1]
     for eps in (1e-13, case.eps0):
         x = torch.zeros(ds.mm2, dtype=torch.float64, device="cuda")
         info = solver.solve(ds.alu, ds.llu, ds.de, ds.b, x, eps=eps)
@@ -104,13 +114,13 @@ def test_solve_matches_oracle(gpu, ora, prepared, label):
         rel = np.linalg.norm(xg - ref.x) / np.linalg.norm(ref.x)
         assert info.ier == 0 and ref.ier == 0
         if eps == 1e-13:
-            assert rel <= 1e-10, (label, rel, info.as_dict(), ref.iters)
+            assert rel <= 1e-11, (label, rel, info.as_dict(), ref.iters)
         else:
             assert info.eps <= eps and info.reason in (0, 1)
-            assert rel <= 50 * eps, (label, rel)
-        # iteration counts follow rounding near the stop tests (stagnation test of
-        # pcgpme_para.F90:228): reported, required to agree to within 25 %
-        assert abs(info.iter - ref.iters) <= max(5, ref.iters // 4), (info.iter, ref.iters)
+            assert rel <= 10 * eps, (label, rel)
+            true_res = np.linalg.norm(b - A @ xg) / np.linalg.norm(b)
+            assert true_res <= 2 * eps, (label, true_res)
+        assert abs(info.iter - ref.iters) <= max(3, ref.iters // 6), (info.iter, ref.iters)
 
 
 def test_solve_vs_direct(gpu, ora, prepared):
