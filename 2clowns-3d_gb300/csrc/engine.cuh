@@ -1242,6 +1242,42 @@ __device__ __forceinline__ void bal_flush(const Eng<T>& E, T (&v)[B * NVAL], lon
     if ((threadIdx.x & (32 / V - 1)) == 0 && cc < c1) put_chunk(E, gc_member + cc, k, (double)s);
 }
 
+// FP64 chunk totals through shared memory.  A butterfly over one or two
+// values costs every lane five FP64 additions per value; the FP64 dot-product
+// kernels at 4 rows per thread (one chunk per warp and step) instead store each
+// chunk's 32 lane values and, every kTreeSteps steps, let one thread per
+// (chunk, value) add them up along the butterfly's own tree -- lanes differing
+// in bit 4 first, in bit 0 last -- so the total has the same bits at about one
+// addition per lane value.
+template <typename T, int R>
+constexpr bool kTreeSmem = sizeof(T) == 8 && R == 4;
+constexpr int kTreeSteps = 4;
+constexpr int kTreeRow = 33;    // padded row of 32 lane values (no bank conflicts)
+
+template <typename A, int BIT, int PAT>
+__device__ __forceinline__ A lane_tree(const A* r) {
+    if constexpr (BIT == 4) {
+        return r[PAT] + r[PAT | 16];
+    } else {
+        return lane_tree<A, BIT + 1, PAT>(r) + lane_tree<A, BIT + 1, PAT | (1 << BIT)>(r);
+    }
+}
+
+// Chunk totals of one round: slot (st, w, q) holds the lane values of value q
+// of the chunk warp w took at step s0 + st.  Reducing threads rotate with the
+// block index over the SM sub-partitions.
+template <typename T, int NVAL>
+__device__ __forceinline__ void tree_flush(const Eng<T>& E, const T* tbuf, long gcm, int c0, int c1, int s0,
+                                           int nsteps, int nwarps) {
+    const int t = (int)((threadIdx.x + 32u * (blockIdx.x % (unsigned)nwarps)) % blockDim.x);
+    if (t >= kTreeSteps * nwarps * NVAL) return;
+    const int slot = t / NVAL, q = t % NVAL;
+    const int st = slot / nwarps, ww = slot % nwarps;
+    const int cb = c0 + nwarps * (s0 + st) + ww;
+    if (s0 + st >= nsteps || cb >= c1) return;
+    put_chunk(E, gcm + cb, q, (double)lane_tree<T, 0, 0>(tbuf + t * kTreeRow));
+}
+
 // sweeps 5, 6 with the RQ (MODE 1) or AMU (MODE 2) reduction (as tl_sweep56);
 // NL = 4: a copy with the reduction
 template <typename T, int MODE, int R, int NL>
@@ -1278,6 +1314,60 @@ __global__ void __launch_bounds__(kEngBlock, kBalMinBlocks<T, R>) k_bal_sweep56(
     constexpr bool six = NL == 6;                    // NL = 4: sweeps 5 and 6 are empty, out = in
     const int lane = threadIdx.x & 31, w = threadIdx.x >> 5, nwarps = blockDim.x >> 5;
     const long gcm = off / kChunk;
+    if constexpr (kTreeSmem<T, R> && MODE != 0) {
+        __shared__ T tbuf[kTreeSteps * (kEngBlock / 32) * NVAL * kTreeRow];
+        if (done) return;
+        const int nsteps = (c1 - c0 + nwarps - 1) / nwarps;
+        for (int s0 = 0; s0 < nsteps; s0 += kTreeSteps) {
+#pragma unroll 1
+            for (int st = 0; st < kTreeSteps; st++) {
+                const int cb = c0 + nwarps * (s0 + st) + w;
+                if (s0 + st >= nsteps || cb >= c1) break;          // the same for the whole warp
+                T a5v[R], a6v[R], xv[R], wv[R], g5[R], g6[R];
+                int c5v[R], c6v[R];
+                bool ok[R];
+                long i[R];
+#pragma unroll
+                for (int u = 0; u < R; u++) {
+                    const long r = (long)cb * kChunk + 32 * u + lane;
+                    ok[u] = r < n;
+                    i[u] = off + (ok[u] ? r : 0);
+                    if (six) {
+                        a5v[u] = ld_stream(a5 + i[u]);
+                        a6v[u] = ld_stream(a6 + i[u]);
+                        c5v[u] = ld_stream(c5 + i[u]);
+                        c6v[u] = ld_stream(c6 + i[u]);
+                    }
+                    xv[u] = ldg2(in + i[u]);
+                    wv[u] = ldg2((MODE == 1 ? E.r0 : E.e) + i[u]);
+                }
+                if (six) {
+#pragma unroll
+                    for (int u = 0; u < R; u++) {
+                        g5[u] = ldg2(in + c5v[u]);
+                        g6[u] = ldg2(in + c6v[u]);
+                    }
+                }
+                T v[NVAL];
+#pragma unroll
+                for (int q = 0; q < NVAL; q++) v[q] = T(0);
+#pragma unroll
+                for (int u = 0; u < R; u++) {
+                    if (!ok[u]) continue;
+                    const T y = six ? fnma(a6v[u], g6[u], fnma(a5v[u], g5[u], xv[u])) : xv[u];
+                    out[i[u]] = y;
+                    v[0] = fma_rn(wv[u], y, v[0]);
+                    if (MODE == 2) v[NVAL - 1] = fma_rn(y, y, v[NVAL - 1]);
+                }
+#pragma unroll
+                for (int q = 0; q < NVAL; q++) tbuf[((st * nwarps + w) * NVAL + q) * kTreeRow + lane] = v[q];
+                step_fence();
+            }
+            __syncthreads();
+            tree_flush<T, NVAL>(E, tbuf, gcm, c0, c1, s0, nsteps, nwarps);
+            __syncthreads();
+        }
+    } else
     for (int s0 = 0; c0 + (nwarps * s0 + w) * CPS < c1; s0 += SPB) {
         T v[B * NVAL];
 #pragma unroll
@@ -1388,6 +1478,48 @@ __global__ void __launch_bounds__(kEngBlock, kBalMinBlocks<T, R>) k_bal_xrupdate
     constexpr int SPB = B / CPS;
     const int lane = threadIdx.x & 31, w = threadIdx.x >> 5, nwarps = blockDim.x >> 5;
     const long gcm = off / kChunk;
+    if constexpr (kTreeSmem<T, R>) {
+        __shared__ T tbuf[kTreeSteps * (kEngBlock / 32) * 2 * kTreeRow];
+        if (done) return;
+        const int nsteps = (c1 - c0 + nwarps - 1) / nwarps;
+        for (int s0 = 0; s0 < nsteps; s0 += kTreeSteps) {
+#pragma unroll 1
+            for (int st = 0; st < kTreeSteps; st++) {
+                const int cb = c0 + nwarps * (s0 + st) + w;
+                if (s0 + st >= nsteps || cb >= c1) break;          // the same for the whole warp
+                T ev[R], xv[R], pv[R], vv[R], r0v[R];
+                bool ok[R];
+                long i[R];
+#pragma unroll
+                for (int u = 0; u < R; u++) {
+                    const long r = (long)cb * kChunk + 32 * u + lane;
+                    ok[u] = r < n;
+                    i[u] = off + (ok[u] ? r : 0);
+                    ev[u] = ldg2(E.e + i[u]);
+                    xv[u] = ldg2(E.xi + i[u]);
+                    pv[u] = ldg2(E.p + i[u]);
+                    vv[u] = ldg2(E.v + i[u]);
+                    r0v[u] = ldg2(E.r0 + i[u]);
+                }
+                T v0 = T(0), v1 = T(0);
+#pragma unroll
+                for (int u = 0; u < R; u++) {
+                    if (!ok[u]) continue;
+                    E.xi[i[u]] = fma_rn(AMU, ev[u], fma_rn(ALP, pv[u], xv[u]));
+                    const T rn = fnma(AMU, vv[u], ev[u]);
+                    E.r[i[u]] = rn;
+                    v0 = fma_rn(rn, rn, v0);
+                    v1 = fma_rn(rn, r0v[u], v1);
+                }
+                tbuf[((st * nwarps + w) * 2 + 0) * kTreeRow + lane] = v0;
+                tbuf[((st * nwarps + w) * 2 + 1) * kTreeRow + lane] = v1;
+                step_fence();
+            }
+            __syncthreads();
+            tree_flush<T, 2>(E, tbuf, gcm, c0, c1, s0, nsteps, nwarps);
+            __syncthreads();
+        }
+    } else
     for (int s0 = 0; c0 + (nwarps * s0 + w) * CPS < c1; s0 += SPB) {
         T v[B * 2];
 #pragma unroll
