@@ -1242,15 +1242,16 @@ __device__ __forceinline__ void bal_flush(const Eng<T>& E, T (&v)[B * NVAL], lon
     if ((threadIdx.x & (32 / V - 1)) == 0 && cc < c1) put_chunk(E, gc_member + cc, k, (double)s);
 }
 
-// FP64 chunk totals through shared memory.  A butterfly over one or two
-// values costs every lane five FP64 additions per value; the FP64 dot-product
-// kernels at 4 rows per thread (one chunk per warp and step) instead store each
-// chunk's 32 lane values and, every kTreeSteps steps, let one thread per
-// (chunk, value) add them up along the butterfly's own tree -- lanes differing
-// in bit 4 first, in bit 0 last -- so the total has the same bits at about one
-// addition per lane value.
+// Chunk totals through shared memory.  A butterfly over one or two values
+// costs every lane five additions per value (on GB300's slow FP64 pipe, the
+// bound of the FP64 dot-product kernels) and holds the batch of values in
+// registers.  The dot-product kernels at 4 rows per thread (one chunk per warp
+// and step) instead store each chunk's 32 lane values and, every kTreeSteps
+// steps, let one thread per (chunk, value) add them up in T along the
+// butterfly's own tree -- lanes differing in bit 4 first, in bit 0 last -- so
+// the total has the same bits at about one addition per lane value.
 template <typename T, int R>
-constexpr bool kTreeSmem = sizeof(T) == 8 && R == 4;
+constexpr bool kTreeSmem = R == 4;
 constexpr int kTreeSteps = 4;
 constexpr int kTreeRow = 33;    // padded row of 32 lane values (no bank conflicts)
 
@@ -1375,7 +1376,7 @@ __global__ void __launch_bounds__(kEngBlock, kBalMinBlocks<T, R>) k_bal_sweep56(
 #pragma unroll
         for (int st = 0; st < SPB; st++) {
             const int cb = c0 + (nwarps * (s0 + st) + w) * CPS;
-            T a5v[R], a6v[R], xv[R], g5[R], g6[R];
+            T a5v[R], a6v[R], xv[R], wv[R], g5[R], g6[R];
             int c5v[R], c6v[R];
             bool ok[R];
 #pragma unroll
@@ -1391,6 +1392,7 @@ __global__ void __launch_bounds__(kEngBlock, kBalMinBlocks<T, R>) k_bal_sweep56(
                     c6v[u] = ld_stream(c6 + i);
                 }
                 xv[u] = ldg2(in + i);
+                if (MODE != 0) wv[u] = ldg2((MODE == 1 ? E.r0 : E.e) + i);   // with the streams, not after the stores
             }
             if (six) {
 #pragma unroll
@@ -1406,11 +1408,8 @@ __global__ void __launch_bounds__(kEngBlock, kBalMinBlocks<T, R>) k_bal_sweep56(
                 const T y = six ? fnma(a6v[u], g6[u], fnma(a5v[u], g5[u], xv[u])) : xv[u];
                 out[i] = y;
                 const int q = (st * CPS + u / kChunkRows) * NVAL;
-                if (MODE == 1) v[q] = fma_rn(ldg2(E.r0 + i), y, v[q]);
-                if (MODE == 2) {
-                    v[q] = fma_rn(ldg2(E.e + i), y, v[q]);
-                    v[q + NVAL - 1] = fma_rn(y, y, v[q + NVAL - 1]);
-                }
+                if (MODE != 0) v[q] = fma_rn(wv[u], y, v[q]);
+                if (MODE == 2) v[q + NVAL - 1] = fma_rn(y, y, v[q + NVAL - 1]);
             }
             step_fence();
         }

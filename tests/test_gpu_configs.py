@@ -10,12 +10,14 @@ For the two FP64 configurations the cell classification (flags, fluid and
 surface lists), the row numbering, the right-hand side, the assembled matrix and
 the row-scaled, sorted matrix PCGPME iterates with must equal the oracle's bit
 for bit; the pressure solved to ERR <= 1e-13 must lie within 1e-10 relative L2
-of the oracle's, and at the configuration's own tolerance the GPU pressure must
-be no farther from that tightly converged pressure than twice the oracle's own
-distance (both stop anywhere inside the same ERR ball; the factor two is the
-bound on where in it a solve stops, not a precision allowance).  Iteration
-counts are reported in the assertion messages, not bounded: they follow the
-rounding of the dot products near the stop tests."""
+of the oracle's.  At the configuration's own tolerance eps the GPU pressure is
+checked without the oracle's solve, whose OpenMP reductions stop it at a
+different place inside the same ERR ball from run to run: its true residual
+||b - A x|| / ||b|| against the assembled matrix must be within 2 eps, and its
+distance to the tightly converged pressure within 10 eps (the bounds of the
+small parity cases; the oracle's own distance is reported beside it).
+Iteration counts are reported in the assertion messages, not bounded: they
+follow the rounding of the dot products near the stop tests."""
 import os
 
 import numpy as np
@@ -78,9 +80,13 @@ def _fp64_config(gpu, ora, case):
     assert rel13 <= 1e-10, (case.label, rel13, "iters gpu/oracle", i13.iter, r13.iters)
     xg, info, ref = out[case.eps0]
     d_gpu, d_ora = _rel(xg, r13.x), _rel(ref.x, r13.x)
-    assert info.eps <= case.eps0 and info.reason in (0, 1)
-    assert d_gpu <= 2.0 * d_ora + 1e-14, (case.label, "distance to the 1e-13 pressure gpu/oracle", d_gpu, d_ora,
-                                          "iters gpu/oracle", info.iter, ref.iters)
+    b = sy.b[1:n + 1]
+    true_res = float(np.linalg.norm(b - ora.to_csr(sy) @ xg) / np.linalg.norm(b))
+    msg = (case.label, "true residual", true_res, "distance to the 1e-13 pressure gpu/oracle", d_gpu, d_ora,
+           "iters gpu/oracle", info.iter, ref.iters)
+    assert info.eps <= case.eps0 and info.reason in (0, 1), msg
+    assert true_res <= 2 * case.eps0, msg
+    assert d_gpu <= 10 * case.eps0, msg
 
 
 def test_config_tank_64x64x32(gpu, ora):
