@@ -304,9 +304,12 @@ def run_ensemble(args):
             fn()
         ms, res = time_device(fn, args.steps, stream)
         infos = res[-1]
+        row_iters = float(sum(n * i.iter for n, i in zip(sizes, infos)))
         out[name] = {"ms_per_ensemble": ms / args.steps, "solves_per_s": len(sizes) * args.steps / (ms / 1000.0),
                      "iters_total": int(sum(i.iter for i in infos)), "max_eps": max(i.eps for i in infos),
-                     "ier": sorted(set(int(i.ier) for i in infos))}
+                     "ier": sorted(set(int(i.ier) for i in infos)),
+                     # sum over members of rows x iterations (inner ones for mixed), and the time per unit
+                     "row_iterations": row_iters, "ps_per_row_iteration": ms / args.steps * 1e9 / row_iters}
     line = {"metric": "ensemble pressure solves/s", "unit": "solves/s", "members": len(sizes),
             "rows_total": int(sum(sizes)), "rows_min": int(min(sizes)), "rows_max": int(max(sizes)),
             "tol": eps, "generation_s": t_gen, "legs": out,
