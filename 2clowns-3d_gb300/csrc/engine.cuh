@@ -1252,7 +1252,7 @@ __device__ __forceinline__ void bal_flush(const Eng<T>& E, T (&v)[B * NVAL], lon
 // the total has the same bits at about one addition per lane value.
 template <typename T, int R>
 constexpr bool kTreeSmem = R == 4;
-constexpr int kTreeSteps = 4;
+constexpr int kTreeSteps = 8;
 constexpr int kTreeRow = 33;    // padded row of 32 lane values (no bank conflicts)
 
 template <typename A, int BIT, int PAT>
