@@ -1050,12 +1050,12 @@ __device__ __forceinline__ void pf_rows(const U* s, long lo, long hi) {
 template <typename T, int R>
 constexpr int kBalMinBlocks = R == 4 ? (sizeof(T) == 8 ? 3 : 4) : 1;
 
-// Chunks per transposed butterfly in the balanced dot-product kernels: four
-// (2.25 additions per chunk and value pair instead of five), one for the FP64
-// x/r update at 4 rows per thread, whose loads already fill its 80 registers
-// (a batch of two spills).
+// Chunks per transposed butterfly in the register path of the balanced
+// dot-product kernels (8 rows per thread; at 4 rows per thread they form the
+// chunk totals in shared memory, kTreeSmem): four, 2.25 additions per chunk and
+// value pair instead of five.
 template <typename T, int R, int NVAL>
-constexpr int kBalBatch = (sizeof(T) == 8 && R == 4 && NVAL == 2) ? 1 : 4;
+constexpr int kBalBatch = 4;
 
 // Keeps the compiler from hoisting the next step's loads above this step's
 // stores: each step keeps its own window of R rows in flight, as the kernels'
