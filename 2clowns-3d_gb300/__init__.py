@@ -394,7 +394,8 @@ def tuned_shape(sizes, precision=0):
     if mo.value == 1:
         bal = (8 if f.value & 8 else 4) if f.value & 4 else 0
         return {"mode": "graph", "block": 256 if bal else b.value, "fused_sweeps": bool(f.value & 1),
-                "reduce_block": 64 if f.value & 2 else (256 if bal else b.value), "balanced_rows": bal}
+                "reduce_block": 64 if f.value & 2 else (256 if bal else b.value), "balanced_rows": bal,
+                "staged_axsub": bool(f.value & 16)}
     return {"mode": {0: "persistent", 3: "wave"}.get(mo.value, str(mo.value)), "block": b.value,
             "grid": g.value, "registers": r.value}
 

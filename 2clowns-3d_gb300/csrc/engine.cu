@@ -12,6 +12,7 @@
 #include <mutex>
 #include <string>
 #include <tuple>
+#include <type_traits>
 #include <vector>
 
 #include "engine.cuh"
@@ -379,6 +380,7 @@ static Eng<T> eng_bind(void* work, const EngLayout& L) {
     for (int k = 0; k < kWaveBufs; k++) E.w[k] = L.wave ? (T*)(b + L.o_wbuf[k]) : nullptr;
     E.baltab = nullptr;       // set once the launch sizes are uploaded (upload_bal_tables)
     E.nl = 6;                 // set by the solve from its members' NL
+    E.abort = &((GridBar*)(b + L.o_bar))->abort;
     E.pf = l2_prefetch_rows();
     E.balg = L.o_balg ? (const int*)(b + L.o_balg) : nullptr;
     return E;
@@ -442,6 +444,7 @@ struct Shape {
     int fuse = 1;   // LDUSUB sweeps 1-2 and 3-4 as fused pairs (else four single sweeps)
     int rblock = kStepBlock;   // threads per tile of the dot-product kernels (64: 8 rows per thread)
     int bal = 0;    // single systems: balanced one-wave kernels with bal rows per thread per step (4 or 8)
+    int stg = 0;    // FP32 single systems, balanced at 4 rows: AXSUB with its streams staged by bulk copies
 };
 
 
@@ -511,6 +514,7 @@ struct LoopShape {
     int fuse = 1;     // graph / host launches: fused sweep pairs
     int rblock = kStepBlock;   // graph / host launches: block of the dot-product kernels
     int bal = 0;      // graph / host launches, single systems: balanced kernels, rows per thread (4, 8)
+    int stg = 0;      // with bal = 4, FP32 single systems: the staged AXSUB (k_bal_axsub_stg)
 };
 
 // CLOWNS_LOOP_MODE=graph|persistent|launch|wave forces one execution of the loop
@@ -558,11 +562,12 @@ static int loop_max_grid(int block, int minb, int* out, bool wave = false) {
 // Kernel launch with optional programmatic serialization (captured as a
 // programmatic edge inside a graph).
 template <typename... KArgs, typename... Args>
-static void klaunch(bool pdl, void (*kern)(KArgs...), int grid, int block, cudaStream_t s, Args... args) {
+static void klaunch_smem(bool pdl, void (*kern)(KArgs...), int grid, int block, size_t smem, cudaStream_t s,
+                         Args... args) {
     cudaLaunchConfig_t cfg = {};
     cfg.gridDim = dim3(grid);
     cfg.blockDim = dim3(block);
-    cfg.dynamicSmemBytes = 0;
+    cfg.dynamicSmemBytes = smem;
     cfg.stream = s;
     cudaLaunchAttribute at[1];
     if (pdl) {
@@ -572,6 +577,10 @@ static void klaunch(bool pdl, void (*kern)(KArgs...), int grid, int block, cudaS
         cfg.numAttrs = 1;
     }
     cudaLaunchKernelEx(&cfg, kern, args...);
+}
+template <typename... KArgs, typename... Args>
+static void klaunch(bool pdl, void (*kern)(KArgs...), int grid, int block, cudaStream_t s, Args... args) {
+    klaunch_smem(pdl, kern, grid, block, 0, s, args...);
 }
 
 template <typename T>
@@ -612,6 +621,29 @@ struct BalGrids {
     int ax, sw, s2, r1, r2, eu, xr, pu;
 };
 
+// One wave of the staged AXSUB (its dynamic shared memory raised once, before
+// any capture; 0 if the device refuses it, and the tuner then leaves it out).
+template <int NL>
+static int stg_grid() {
+    static const int g = [] {
+        if (cudaFuncSetAttribute(k_bal_axsub_stg<NL>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                 (int)kStgSmem<NL>) != cudaSuccess) {
+            cudaGetLastError();
+            return 0;
+        }
+        int per_sm = 0, dev = 0, sms = 0;
+        if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_bal_axsub_stg<NL>, kEngBlock, kStgSmem<NL>) !=
+                cudaSuccess ||
+            cudaGetDevice(&dev) != cudaSuccess ||
+            cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess || per_sm < 1) {
+            cudaGetLastError();
+            return 0;
+        }
+        return per_sm * sms;
+    }();
+    return g;
+}
+
 // The balanced kernels' one-wave grids (queried once; before any capture)
 template <typename T, int R>
 static const BalGrids& bal_grids() {
@@ -623,9 +655,13 @@ static const BalGrids& bal_grids() {
 }
 
 template <typename T>
-static void prepare_bal(int bal) {
+static void prepare_bal(int bal, int stg) {
     if (bal == 8) bal_grids<T, 8>();
     else if (bal) bal_grids<T, 4>();
+    if (stg) {
+        stg_grid<6>();
+        stg_grid<4>();
+    }
 }
 
 // Kernel kinds of the balanced iteration, in the order of BalGrids and of the
@@ -672,7 +708,14 @@ static void g_iteration_bal(bool pdl, const Eng<T>& E, const Shape& sh, cudaStre
         return E.M == 1 ? nullptr : E.baltab + (size_t)((R == 8 ? 8 : 0) + k) * kBalTabMax;
     };
     auto apply = [&](const T* in, T* out, int mode) {
-        klaunch(pdl, k_bal_axsub<T, R, NL>, grid(kBalAx), B, s, E, tab(kBalAx), in, E.t);
+        if constexpr (std::is_same<T, float>::value && R == 4) {
+            if (sh.stg && E.M == 1 && stg_grid<NL>() > 0)
+                klaunch_smem(pdl, k_bal_axsub_stg<NL>, std::min(stg_grid<NL>(), n), B, kStgSmem<NL>, s, E, in, E.t);
+            else
+                klaunch(pdl, k_bal_axsub<T, R, NL>, grid(kBalAx), B, s, E, tab(kBalAx), in, E.t);
+        } else {
+            klaunch(pdl, k_bal_axsub<T, R, NL>, grid(kBalAx), B, s, E, tab(kBalAx), in, E.t);
+        }
         if (sh.fuse) {
             klaunch(pdl, k_bal_sweep2<T, R>, grid(kBalS2), B, s, E, tab(kBalS2), 0, (const T*)E.t, out);
             klaunch(pdl, k_bal_sweep2<T, R>, grid(kBalS2), B, s, E, tab(kBalS2), 2, (const T*)out, E.t);
@@ -695,6 +738,16 @@ static void g_iteration_bal(bool pdl, const Eng<T>& E, const Shape& sh, cudaStre
 // Balanced kernels serve single systems, and ensembles whose tables are uploaded.
 template <typename T>
 static bool bal_usable(const Eng<T>& E) { return E.M == 1 || E.baltab != nullptr; }
+
+// The staged AXSUB serves FP32 single systems on the balanced kernels at 4 rows
+// per thread (its grid is its own, so ensembles' block tables do not fit it).
+template <typename T>
+static bool stg_usable(const Eng<T>& E, int bal) {
+    if constexpr (std::is_same<T, float>::value)
+        return E.M == 1 && bal == 4 && (E.nl == 4 ? stg_grid<4>() : stg_grid<6>()) > 0;
+    else
+        return false;
+}
 
 template <typename T>
 static void g_iteration(bool pdl, const Eng<T>& E, const Shape& sh, cudaStream_t s) {
@@ -723,9 +776,9 @@ static void g_iteration(bool pdl, const Eng<T>& E, const Shape& sh, cudaStream_t
 // different members) must not share a graph.
 struct GraphKey {
     std::string eng;
-    int prec, fuse, rblock, bal;
+    int prec, fuse, rblock, bal, stg;
     bool operator<(const GraphKey& o) const {
-        return std::tie(eng, prec, fuse, rblock, bal) < std::tie(o.eng, o.prec, o.fuse, o.rblock, o.bal);
+        return std::tie(eng, prec, fuse, rblock, bal, stg) < std::tie(o.eng, o.prec, o.fuse, o.rblock, o.bal, o.stg);
     }
 };
 
@@ -734,7 +787,7 @@ template <typename T>
 static std::string eng_key(const Eng<T>& E) {
     std::string k;
     auto put = [&](const auto& v) { k.append((const char*)&v, sizeof(v)); };
-    put(E.NV); put(E.M); put(E.nblk); put(E.n1); put(E.nl); put(E.pf);
+    put(E.NV); put(E.M); put(E.nblk); put(E.n1); put(E.nl); put(E.pf); put(E.abort);
     put(E.al); put(E.ll); put(E.d); put(E.r); put(E.p); put(E.r0); put(E.q); put(E.e); put(E.v); put(E.t);
     put(E.xi); put(E.W); put(E.x64); put(E.r64); put(E.s64); put(E.t64);
     put(E.blk_member); put(E.blk_rows); put(E.mem_off); put(E.mem_n); put(E.mem_nblk); put(E.mem_blk0);
@@ -755,7 +808,7 @@ void release_all_graphs() {
 
 // WHILE { iteration ; guard } captured into a fresh graph
 template <typename T>
-static int build_loop_graph(const Eng<T>& E, bool pdl, int fuse, int rblock, int bal, cudaGraphExec_t* out) {
+static int build_loop_graph(const Eng<T>& E, bool pdl, int fuse, int rblock, int bal, int stg, cudaGraphExec_t* out) {
     if (!g_cap) CLOWNS_CUDA_TRY(cudaStreamCreateWithFlags(&g_cap, cudaStreamNonBlocking));
     cudaGraph_t graph;
     CLOWNS_CUDA_TRY(cudaGraphCreate(&graph, 0));
@@ -768,12 +821,13 @@ static int build_loop_graph(const Eng<T>& E, bool pdl, int fuse, int rblock, int
     cudaGraphNode_t cnode;
     CLOWNS_CUDA_TRY(cudaGraphAddNode(&cnode, graph, nullptr, nullptr, 0, &cp));
     cudaGraph_t body = cp.conditional.phGraph_out[0];
-    prepare_bal<T>(bal);
+    prepare_bal<T>(bal, stg);
     CLOWNS_CUDA_TRY(cudaStreamBeginCaptureToGraph(g_cap, body, nullptr, nullptr, 0, cudaStreamCaptureModeThreadLocal));
     Shape sh;
     sh.fuse = fuse;
     sh.rblock = rblock;
     sh.bal = bal;
+    sh.stg = stg;
     g_iteration(pdl, E, sh, g_cap);
     BalBlock* tabs = bal && E.M > 1 && E.baltab ? (BalBlock*)E.baltab : nullptr;
     klaunch(pdl, k_eng_guard, 1, 256, g_cap, E.S, E.M, E.ctrl, h, (const int*)E.mem_n, tabs, E.balg);
@@ -798,16 +852,16 @@ static int build_loop_graph(const Eng<T>& E, bool pdl, int fuse, int rblock, int
 }
 
 template <typename T>
-static int loop_graph(const Eng<T>& E, const void* work, int prec, int fuse, int rblock, int bal,
+static int loop_graph(const Eng<T>& E, const void* work, int prec, int fuse, int rblock, int bal, int stg,
                       cudaGraphExec_t* out) {
     std::lock_guard<std::mutex> lk(g_graph_mu);
     (void)work;
-    GraphKey key{eng_key(E), prec, fuse, rblock, bal};
+    GraphKey key{eng_key(E), prec, fuse, rblock, bal, stg};
     auto it = g_graphs.find(key);
     if (it != g_graphs.end()) { *out = it->second; return CLOWNS_OK; }
     cudaGraphExec_t ex;
-    int rc = build_loop_graph(E, true, fuse, rblock, bal, &ex);              // programmatic edges
-    if (rc) rc = build_loop_graph(E, false, fuse, rblock, bal, &ex);         // plain edges if refused
+    int rc = build_loop_graph(E, true, fuse, rblock, bal, stg, &ex);         // programmatic edges
+    if (rc) rc = build_loop_graph(E, false, fuse, rblock, bal, stg, &ex);    // plain edges if refused
     if (rc) return rc;
     if (g_graphs.size() >= 64) {
         cudaGraphExecDestroy(g_graphs.begin()->second);
@@ -879,6 +933,8 @@ static int run_loop(Eng<T> E, const void* work, GridBar* gb, int prec, const Loo
         ksh.fuse = sh.fuse;
         ksh.rblock = sh.rblock;
         ksh.bal = sh.bal;
+        ksh.stg = sh.stg;
+        prepare_bal<T>(sh.bal, sh.stg);
         int cap = 0;
         CLOWNS_CUDA_TRY(cudaMemcpyAsync(&cap, E.ctrl + 1, sizeof(int), cudaMemcpyDeviceToHost, s));
         CLOWNS_CUDA_TRY(cudaStreamSynchronize(s));
@@ -918,7 +974,7 @@ static int run_loop(Eng<T> E, const void* work, GridBar* gb, int prec, const Loo
     }
     if (sh.graph) {
         cudaGraphExec_t ex;
-        int rc = loop_graph(E, work, prec, sh.fuse, sh.rblock, sh.bal, &ex);
+        int rc = loop_graph(E, work, prec, sh.fuse, sh.rblock, sh.bal, sh.stg, &ex);
         if (rc) return rc;
         CLOWNS_CUDA_TRY(cudaMemsetAsync(gb, 0, sizeof(GridBar), s));
         CLOWNS_CUDA_TRY(cudaGraphLaunch(ex, s));
@@ -969,6 +1025,8 @@ static int tune_loop(Eng<T> E, const void* work, GridBar* gb, long key_nv, int k
         sh.rblock = (rz && !strcmp(rz, "64")) ? 64 : kStepBlock;
         const char* bz = getenv("CLOWNS_BALANCED_ROWS");  // forced executions: tile kernels unless 4 or 8
         sh.bal = !bal_usable(E) || !bz ? 0 : !strcmp(bz, "8") ? 8 : !strcmp(bz, "4") ? 4 : 0;
+        const char* sz = getenv("CLOWNS_AXSUB_STAGED");   // forced: the staged FP32 AXSUB if "1"
+        sh.stg = stg_usable(E, sh.bal) && sz && !strcmp(sz, "1");
         *out = sh;
         return CLOWNS_OK;
     }
@@ -1058,6 +1116,16 @@ static int tune_loop(Eng<T> E, const void* work, GridBar* gb, long key_nv, int k
                     gsh.bal = rows;
                     cands.push_back(gsh);
                 }
+        // FP32 single systems: the same with the staged AXSUB
+        if (stg_usable(E, 4))
+            for (int fuse : {1, 0}) {
+                LoopShape gsh;
+                gsh.graph = 1;
+                gsh.fuse = fuse;
+                gsh.bal = 4;
+                gsh.stg = 1;
+                cands.push_back(gsh);
+            }
     }
     if (cands.empty()) {
         set_last_error_msg("pcgpme: the forced loop execution does not serve this system");
@@ -1106,7 +1174,8 @@ static int tune_loop(Eng<T> E, const void* work, GridBar* gb, long key_nv, int k
 
 // mode: 0 persistent, 1 CUDA graph, 3 wavefront; fuse (graph): bit 0 fused sweep
 // pairs, bit 1 dot-product kernels at 64 threads per tile, bit 2 balanced
-// one-wave kernels (bit 3: 8 rows per thread per step, else 4)
+// one-wave kernels (bit 3: 8 rows per thread per step, else 4), bit 4 the
+// staged FP32 AXSUB
 int engine_tuned_shape(long nv, int prec, int single, int* mode, int* block, int* grid, int* minb, int* fuse) {
     std::lock_guard<std::mutex> lk(g_loop_mu);
     auto it = g_loop_shapes.find(std::make_tuple(nv, prec, single, forced_loop_mode()));
@@ -1116,7 +1185,9 @@ int engine_tuned_shape(long nv, int prec, int single, int* mode, int* block, int
     *block = sh.block;
     *grid = sh.graph == 1 ? 0 : sh.grid;
     *minb = sh.graph == 1 ? 0 : sh.minb;
-    *fuse = sh.graph == 1 ? (sh.fuse | (sh.rblock != kStepBlock ? 2 : 0) | (sh.bal ? 4 : 0) | (sh.bal == 8 ? 8 : 0)) : 0;
+    *fuse = sh.graph == 1 ? (sh.fuse | (sh.rblock != kStepBlock ? 2 : 0) | (sh.bal ? 4 : 0) | (sh.bal == 8 ? 8 : 0) |
+                             (sh.stg ? 16 : 0))
+                          : 0;
     return CLOWNS_OK;
 }
 

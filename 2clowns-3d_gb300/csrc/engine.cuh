@@ -136,6 +136,7 @@ struct Eng {
     int nl;                   // columns the members' matrices fill: 6 (3D) or 4 (2DH); the rest are empty
     int pf;                   // balanced kernels: rows per block and stream asked of L2 before the
                               // wait on the previous kernel (0: none)
+    int* abort;               // set by a kernel whose bounded wait ran out (the grid barrier's flag)
 };
 
 // ---------------------------------------------------------------------------
@@ -1169,6 +1170,142 @@ __global__ void __launch_bounds__(kEngBlock, kBalMinBlocks<T, R>) k_bal_sweep(En
 #pragma unroll
         for (int u = 0; u < R; u++)
             if (ok[u]) out[i[u]] = fnma(av[u], gv[u], xv[u]);
+    }
+}
+
+// ---------------------------------------------------------------------------
+// AXSUB with its streams staged in shared memory by the bulk-copy engine (FP32
+// inner solve of the mixed path, single systems).  Warp w of a block takes the
+// block's chunks c0 + w, c0 + w + 8, ...; for each it needs D, AL(:, 1..NL) and
+// LL(:, 1..NL) of 128 rows (13 rows of 512 B for NL = 6), which one lane asks
+// of `cp.async.bulk` into the warp's two-stage ring while the warp gathers and
+// computes the previous chunk, completion counted on one mbarrier per stage.
+// The matrix does not change during the loop, so the first stages are asked
+// for before the wait on the previous kernel.  The arithmetic is
+// k_bal_axsub's, in the same order.  Every wait is bounded: a warp whose copy
+// has not landed (in every lane) after kStgSpinLimit polls raises E.abort (the
+// host reports the solve as failed) and, before its block exits, waits (bounded
+// again) for the copies it has in flight.
+constexpr int kStgStages = 2;
+constexpr long kStgSpinLimit = 1L << 22;
+
+__device__ __forceinline__ unsigned smem_addr(const void* p) { return (unsigned)__cvta_generic_to_shared(p); }
+__device__ __forceinline__ void mbar_init(unsigned long long* bar, unsigned count) {
+    asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smem_addr(bar)), "r"(count) : "memory");
+}
+__device__ __forceinline__ void mbar_expect_tx(unsigned long long* bar, unsigned bytes) {
+    asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(smem_addr(bar)), "r"(bytes)
+                 : "memory");
+}
+__device__ __forceinline__ bool mbar_try_wait(unsigned long long* bar, unsigned phase) {
+    unsigned ok;
+    asm volatile(
+        "{\n .reg .pred p;\n mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n selp.u32 %0, 1, 0, p;\n}"
+        : "=r"(ok)
+        : "r"(smem_addr(bar)), "r"(phase)
+        : "memory");
+    return ok != 0;
+}
+// global -> shared bulk copy of `bytes` (a multiple of 16, both addresses 16-byte aligned)
+__device__ __forceinline__ void bulk_g2s(void* dst, const void* src, unsigned bytes, unsigned long long* bar) {
+    asm volatile("cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(
+                     smem_addr(dst)),
+                 "l"(src), "r"(bytes), "r"(smem_addr(bar))
+                 : "memory");
+}
+
+template <int NL>
+constexpr int kStgStageBytes = kChunk * ((1 + NL) * 4 + NL * 4);   // FP32 D, AL, int LL
+template <int NL>
+constexpr size_t kStgSmem = (size_t)(kEngBlock / 32) * kStgStages * kStgStageBytes<NL>;
+
+template <int NL>
+__global__ void __launch_bounds__(kEngBlock, 1) k_bal_axsub_stg(Eng<float> E, const float* __restrict__ in,
+                                                               float* __restrict__ out) {
+    extern __shared__ __align__(128) unsigned char stg_smem[];
+    __shared__ __align__(8) unsigned long long full[kEngBlock / 32][kStgStages];
+    constexpr int NW = kEngBlock / 32, SB = kStgStageBytes<NL>;
+    pdl_trigger();
+    const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+    if (threadIdx.x == 0) {
+        for (int q = 0; q < NW; q++)
+            for (int b = 0; b < kStgStages; b++) mbar_init(&full[q][b], 1);
+        asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+    }
+    __syncthreads();
+    BalBlock bb;
+    long off;
+    int n, c0, c1;
+    bal_block(E, (const BalBlock*)nullptr, bb, off, n, c0, c1);
+    const long NV = E.NV;
+    unsigned char* ring = stg_smem + (size_t)w * kStgStages * SB;
+    auto issue = [&](int k) {           // one lane: chunk k of this warp into stage k % kStgStages
+        const int b = k % kStgStages;
+        const long r0 = off + (long)(c0 + w + NW * k) * kChunk;
+        unsigned char* st = ring + (size_t)b * SB;
+        mbar_expect_tx(&full[w][b], SB);
+        bulk_g2s(st, E.d + r0, kChunk * 4, &full[w][b]);
+#pragma unroll
+        for (int c = 0; c < NL; c++) {
+            bulk_g2s(st + kChunk * 4 * (1 + c), E.al + c * NV + r0, kChunk * 4, &full[w][b]);
+            bulk_g2s(st + kChunk * 4 * (1 + NL + c), E.ll + c * NV + r0, kChunk * 4, &full[w][b]);
+        }
+    };
+    const int nk = c1 - c0 > w ? (c1 - c0 - w + NW - 1) / NW : 0;     // chunks of this warp
+    if (lane == 0)
+        for (int k = 0; k < kStgStages && k < nk; k++) issue(k);
+    __syncwarp();
+    pdl_wait();                           // `in` is the previous kernel's output
+    int issued = min(nk, kStgStages), waited = 0;
+    for (int k = 0; k < nk; k++) {
+        const int b = k % kStgStages;
+        bool landed = false;
+        for (long spins = 0; spins < kStgSpinLimit && !landed; spins++)
+            landed = mbar_try_wait(&full[w][b], (k / kStgStages) & 1);
+        if (!__all_sync(0xffffffffu, landed)) {
+            if (lane == 0) atomicExch(E.abort, 1);
+            break;
+        }
+        waited = k + 1;
+        const int cb = c0 + w + NW * k;
+        const unsigned char* st = ring + (size_t)b * SB;
+        const float* sd = (const float*)st;
+        const float* sa = sd + kChunk;
+        const int* sc = (const int*)(st + kChunk * 4 * (1 + NL));
+        float s[kChunkRows];
+        float g[NL][kChunkRows];
+#pragma unroll
+        for (int u = 0; u < kChunkRows; u++) {
+            const long r = (long)cb * kChunk + 32 * u + lane;
+            s[u] = in[off + (r < n ? r : 0)];
+#pragma unroll
+            for (int c = 0; c < NL; c++) g[c][u] = in[sc[c * kChunk + 32 * u + lane]];
+        }
+#pragma unroll
+        for (int u = 0; u < kChunkRows; u++) {
+            const int rr = 32 * u + lane;
+            s[u] = s[u] * sd[rr];
+#pragma unroll
+            for (int c = 0; c < NL; c++) s[u] = fma_rn(sa[c * kChunk + rr], g[c][u], s[u]);
+        }
+        __syncwarp();                     // every lane has read stage b
+        if (lane == 0 && k + kStgStages < nk) {
+            issue(k + kStgStages);
+            issued = k + kStgStages + 1;
+        }
+#pragma unroll
+        for (int u = 0; u < kChunkRows; u++) {
+            const long r = (long)cb * kChunk + 32 * u + lane;
+            if (r < n) out[off + r] = s[u];
+        }
+    }
+    // after a wait ran out: the copies still in flight land before the block's
+    // shared memory is released
+    issued = __shfl_sync(0xffffffffu, issued, 0);
+    for (int k = waited; k < issued; k++) {
+        long spins = 0;
+        while (!mbar_try_wait(&full[w][k % kStgStages], (k / kStgStages) & 1) && ++spins < kStgSpinLimit) {
+        }
     }
 }
 

@@ -179,8 +179,9 @@ int clowns_pcgpme_batched_dev(int m, const clowns_member* members, int precision
  * dot-product kernels run 64 threads per 512-row tile (8 rows per thread), bit 2
  * set when a single system runs the balanced kernels (each kernel one wave of
  * 256-thread blocks over even row ranges, one reduction per block), bit 3 set
- * when those take 8 rows per thread per step (else 4).  CLOWNS_ERR_ARG until
- * a solve of that size has run. */
+ * when those take 8 rows per thread per step (else 4), bit 4 set when an FP32
+ * single system's AXSUB has its streams staged in shared memory by bulk copies.
+ * CLOWNS_ERR_ARG until a solve of that size has run. */
 #define CLOWNS_LOOP_PERSISTENT 0
 #define CLOWNS_LOOP_GRAPH 1
 #define CLOWNS_LOOP_WAVE 3

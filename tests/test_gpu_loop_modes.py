@@ -1,8 +1,9 @@
 """Every execution of the iteration loop the autotuner can pick, forced one at a
 time: the CUDA graph of tile kernels (fused or single LDUSUB sweeps, 128 or 64
 threads per dot-product tile), the graph of balanced one-wave kernels (4 or 8
-rows per thread), the same kernels launched from the host, the persistent
-cooperative kernel and the wavefront kernel.
+rows per thread; for the FP32 inner solve also with the AXSUB whose streams are
+staged in shared memory by bulk copies), the same kernels launched from the
+host, the persistent cooperative kernel and the wavefront kernel.
 
 All of them form dot products with one summation tree (128-row chunks, a fixed
 butterfly per chunk, fixed group and member trees), so every execution must
@@ -19,21 +20,23 @@ from cases import small_cases
 pytestmark = pytest.mark.gpu
 
 CASES = small_cases()
-# (CLOWNS_LOOP_MODE, CLOWNS_SWEEP_FUSE, CLOWNS_REDUCE_BLOCK, CLOWNS_BALANCED_ROWS)
+# (CLOWNS_LOOP_MODE, CLOWNS_SWEEP_FUSE, CLOWNS_REDUCE_BLOCK, CLOWNS_BALANCED_ROWS, CLOWNS_AXSUB_STAGED)
 MODES = [
-    ("graph", "1", "128", "0"),
-    ("graph", "0", "128", "0"),
-    ("graph", "1", "64", "0"),
-    ("graph", "1", "128", "4"),
-    ("graph", "0", "128", "4"),
-    ("graph", "1", "128", "8"),
-    ("launch", "0", "128", "0"),
-    ("launch", "1", "128", "4"),
-    ("persistent", "1", "128", "0"),
-    ("wave", "1", "128", "0"),
+    ("graph", "1", "128", "0", "0"),
+    ("graph", "0", "128", "0", "0"),
+    ("graph", "1", "64", "0", "0"),
+    ("graph", "1", "128", "4", "0"),
+    ("graph", "0", "128", "4", "0"),
+    ("graph", "1", "128", "8", "0"),
+    ("graph", "1", "128", "4", "1"),
+    ("launch", "0", "128", "0", "0"),
+    ("launch", "1", "128", "4", "0"),
+    ("launch", "1", "128", "4", "1"),
+    ("persistent", "1", "128", "0", "0"),
+    ("wave", "1", "128", "0", "0"),
 ]
 IDS = ["-".join(m) for m in MODES]
-ENSEMBLE_MODES = [MODES[0], MODES[3], MODES[5], MODES[8]]
+ENSEMBLE_MODES = [MODES[0], MODES[3], MODES[5], MODES[10]]
 
 
 def _x(ds):
@@ -42,11 +45,12 @@ def _x(ds):
 
 
 def _force(monkeypatch, mode):
-    loop, fuse, rblock, bal = mode
+    loop, fuse, rblock, bal, staged = mode
     monkeypatch.setenv("CLOWNS_LOOP_MODE", loop)
     monkeypatch.setenv("CLOWNS_SWEEP_FUSE", fuse)
     monkeypatch.setenv("CLOWNS_REDUCE_BLOCK", rblock)
     monkeypatch.setenv("CLOWNS_BALANCED_ROWS", bal)
+    monkeypatch.setenv("CLOWNS_AXSUB_STAGED", staged)
 
 
 @pytest.fixture(scope="module")
