@@ -325,6 +325,19 @@ static EngLayout eng_layout(int M, const int* n, int mixed, int wave = -1) {
     return L;
 }
 
+// Matrix columns the balanced kernels keep in L2 (the first ones of the sorted
+// order): as many as fit a budget of CLOWNS_L2_KEEP_MB (default kL2KeepMB) at
+// (word + index) bytes per row.
+constexpr int kL2KeepMB = 40;
+static int l2_keep_cols(long NV, int tsize) {
+    static const long mb = [] {
+        const char* v = getenv("CLOWNS_L2_KEEP_MB");
+        return v ? std::max(0L, atol(v)) : (long)kL2KeepMB;
+    }();
+    const long col = NV * (tsize + 4L);
+    return (int)std::min(6L, mb * 1000000L / std::max(1L, col));
+}
+
 // Rows per block and stream of the balanced kernels' L2 prologue (0: none);
 // CLOWNS_L2_PREFETCH overrides the default.  Measured at 2.8 M rows (FP64 /
 // mixed ms per solve): 0 -> 117.2 / 72.4, 512 -> 116.1 / 71.5, 1024 -> 117.3 /
@@ -381,6 +394,7 @@ static Eng<T> eng_bind(void* work, const EngLayout& L) {
     E.baltab = nullptr;       // set once the launch sizes are uploaded (upload_bal_tables)
     E.nl = 6;                 // set by the solve from its members' NL
     E.abort = &((GridBar*)(b + L.o_bar))->abort;
+    E.keep = l2_keep_cols(L.NV, L.tsize);
     E.pf = l2_prefetch_rows();
     E.balg = L.o_balg ? (const int*)(b + L.o_balg) : nullptr;
     return E;
@@ -787,7 +801,7 @@ template <typename T>
 static std::string eng_key(const Eng<T>& E) {
     std::string k;
     auto put = [&](const auto& v) { k.append((const char*)&v, sizeof(v)); };
-    put(E.NV); put(E.M); put(E.nblk); put(E.n1); put(E.nl); put(E.pf); put(E.abort);
+    put(E.NV); put(E.M); put(E.nblk); put(E.n1); put(E.nl); put(E.pf); put(E.abort); put(E.keep);
     put(E.al); put(E.ll); put(E.d); put(E.r); put(E.p); put(E.r0); put(E.q); put(E.e); put(E.v); put(E.t);
     put(E.xi); put(E.W); put(E.x64); put(E.r64); put(E.s64); put(E.t64);
     put(E.blk_member); put(E.blk_rows); put(E.mem_off); put(E.mem_n); put(E.mem_nblk); put(E.mem_blk0);

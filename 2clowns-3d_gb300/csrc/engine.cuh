@@ -137,6 +137,8 @@ struct Eng {
     int pf;                   // balanced kernels: rows per block and stream asked of L2 before the
                               // wait on the previous kernel (0: none)
     int* abort;               // set by a kernel whose bounded wait ran out (the grid barrier's flag)
+    int keep;                 // balanced kernels: the first `keep` matrix columns are loaded with an L2
+                              // evict_last policy (0: all streamed)
 };
 
 // ---------------------------------------------------------------------------
@@ -1058,6 +1060,37 @@ constexpr int kBalMinBlocks = R == 4 ? (sizeof(T) == 8 ? 3 : 4) : 1;
 template <typename T, int R, int NVAL>
 constexpr int kBalBatch = 4;
 
+// Loads of the matrix columns.  Each application of PM A reads every column
+// twice (AXSUB and its LDUSUB sweep) and an iteration does two applications;
+// the first E.keep columns are loaded with an L2 evict_last policy, which keeps
+// them resident across iterations, the others with evict_first (both evict-first
+// in L1): one load instruction either way (ld.global.L2::cache_hint with a
+// policy from createpolicy), the column picking the policy register.  E.keep
+// comes from a byte budget that leaves most of L2 to the Krylov vectors.
+struct ColPolicy {
+    unsigned long long keep, stream;
+    __device__ __forceinline__ ColPolicy() {
+        asm("createpolicy.fractional.L2::evict_last.b64 %0, 1.0;" : "=l"(keep));
+        asm("createpolicy.fractional.L2::evict_first.b64 %0, 1.0;" : "=l"(stream));
+    }
+    __device__ __forceinline__ unsigned long long col(int k, int kept) const { return k < kept ? keep : stream; }
+};
+__device__ __forceinline__ double ld_col(const double* a, unsigned long long pol) {
+    double v;
+    asm("ld.global.L1::evict_first.L2::cache_hint.f64 %0, [%1], %2;" : "=d"(v) : "l"(a), "l"(pol));
+    return v;
+}
+__device__ __forceinline__ float ld_col(const float* a, unsigned long long pol) {
+    float v;
+    asm("ld.global.L1::evict_first.L2::cache_hint.f32 %0, [%1], %2;" : "=f"(v) : "l"(a), "l"(pol));
+    return v;
+}
+__device__ __forceinline__ int ld_col(const int* a, unsigned long long pol) {
+    int v;
+    asm("ld.global.L1::evict_first.L2::cache_hint.s32 %0, [%1], %2;" : "=r"(v) : "l"(a), "l"(pol));
+    return v;
+}
+
 // Keeps the compiler from hoisting the next step's loads above this step's
 // stores: each step keeps its own window of R rows in flight, as the kernels'
 // register budgets assume.
@@ -1107,6 +1140,7 @@ __global__ void __launch_bounds__(kEngBlock, kBalMinBlocks<T, R>) k_bal_axsub(En
     long off;
     int n, c0, c1;
     if (!bal_block(E, tab, bb, off, n, c0, c1)) return;
+    const ColPolicy cp;
     constexpr int CPS = R / kChunkRows;
     const int nw = blockDim.x >> 5;
     for (int cb = c0 + bal_warp() * CPS; cb < c1; cb += nw * CPS) {
@@ -1120,10 +1154,11 @@ __global__ void __launch_bounds__(kEngBlock, kBalMinBlocks<T, R>) k_bal_axsub(En
         for (int k = 0; k < NL; k++) {
             T a[R];
             int c[R];
+            const unsigned long long pol = cp.col(k, E.keep);
 #pragma unroll
             for (int u = 0; u < R; u++) {
-                a[u] = ld_stream(E.al + k * NV + i[u]);
-                c[u] = ld_stream(E.ll + k * NV + i[u]);
+                a[u] = ld_col(E.al + k * NV + i[u], pol);
+                c[u] = ld_col(E.ll + k * NV + i[u], pol);
             }
 #pragma unroll
             for (int u = 0; u < R; u++) s[u] = fma_rn(a[u], ldg2(in + c[u]), s[u]);
@@ -1151,6 +1186,7 @@ __global__ void __launch_bounds__(kEngBlock, kBalMinBlocks<T, R>) k_bal_sweep(En
     long off;
     int n, c0, c1;
     if (!bal_block(E, tab, bb, off, n, c0, c1)) return;
+    const unsigned long long pol = ColPolicy().col(k, E.keep);
     constexpr int CPS = R / kChunkRows;
     const int nw = blockDim.x >> 5;
     for (int cb = c0 + bal_warp() * CPS; cb < c1; cb += nw * CPS) {
@@ -1161,8 +1197,8 @@ __global__ void __launch_bounds__(kEngBlock, kBalMinBlocks<T, R>) k_bal_sweep(En
         int cv[R];
 #pragma unroll
         for (int u = 0; u < R; u++) {
-            av[u] = ld_stream(a + i[u]);
-            cv[u] = ld_stream(c + i[u]);
+            av[u] = ld_col(a + i[u], pol);
+            cv[u] = ld_col(c + i[u], pol);
             xv[u] = ldg2(in + i[u]);
         }
 #pragma unroll
@@ -1331,6 +1367,8 @@ __global__ void __launch_bounds__(kEngBlock, kBalMinBlocks<T, R>) k_bal_sweep2(E
     long off;
     int n, k0, k1;
     if (!bal_block(E, tab, bb, off, n, k0, k1)) return;
+    const ColPolicy cp;
+    const unsigned long long pol0 = cp.col(k, E.keep), pol1 = cp.col(k + 1, E.keep);
     constexpr int CPS = R / kChunkRows;
     const int nw = blockDim.x >> 5;
     for (int kb = k0 + bal_warp() * CPS; kb < k1; kb += nw * CPS) {
@@ -1342,10 +1380,10 @@ __global__ void __launch_bounds__(kEngBlock, kBalMinBlocks<T, R>) k_bal_sweep2(E
 #pragma unroll
         for (int u = 0; u < R; u++) {
             x[u] = ldg2(in + i[u]);
-            aa[u] = ld_stream(a0 + i[u]);
-            ca[u] = ld_stream(c0 + i[u]);
-            ab[u] = ld_stream(a1 + i[u]);
-            cb[u] = ld_stream(c1 + i[u]);
+            aa[u] = ld_col(a0 + i[u], pol0);
+            ca[u] = ld_col(c0 + i[u], pol0);
+            ab[u] = ld_col(a1 + i[u], pol1);
+            cb[u] = ld_col(c1 + i[u], pol1);
         }
 #pragma unroll
         for (int u = 0; u < R; u++) {
