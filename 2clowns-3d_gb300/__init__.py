@@ -381,8 +381,9 @@ PREC_MIXED = 1
 def tuned_shape(sizes, precision=0):
     """Execution the autotuner chose for the iteration loop of this row space:
     {"mode": "graph", "block": .., "fused_sweeps": .., "reduce_block": ..,
-    "balanced_rows": 0 | 4 | 8} (balanced_rows > 0: one-wave kernels over even
-    row ranges, that many rows per thread per step) or
+    "balanced_rows": 0 | 4 | 8, "staged_axsub": ..} (balanced_rows > 0: one-wave
+    kernels over even row ranges, that many rows per thread per step;
+    staged_axsub: the FP32 AXSUB with its streams staged by bulk copies) or
     {"mode": "persistent" | "wave", "block": .., "grid": .., "registers": ..},
     or None before a solve of that size has run."""
     L = lib()
