@@ -972,9 +972,13 @@ __global__ void __launch_bounds__(kEngBlock) k_eng_initres(Eng<T> E) {
 // together, and the per-block costs -- launch, the stop-flag and scalar loads,
 // the reduction tail -- are paid G times per kernel instead of once per
 // 512-row tile (5517 times at 2.8 M rows).  The per-row arithmetic is the tile
-// kernels'.  The dot-product kernels give warp w the block's chunks w, w + 8, ...
-// (R / 4 adjacent chunks per step), fold them as the canonical reduction
-// prescribes, and sum four chunks at a time with one transposed butterfly.
+// kernels'.  Every kernel gives warp w of the block the block's chunks w, w + 8,
+// ... (R / 4 adjacent chunks per step; the element-wise kernels rotate w by the
+// block index), so a warp past the block's range leaves the loop instead of
+// computing on dummy rows.  The dot-product kernels fold each chunk as the
+// canonical reduction prescribes and form the chunk totals in shared memory (4
+// rows per thread, kTreeSmem) or four chunks at a time with one transposed
+// butterfly (8 rows per thread).
 //
 // For a single system only the kernels whose results outlive a stop test read
 // the stop flag: sweep56 (its reduction and finalisation) and xrupdate (x, r
