@@ -173,7 +173,7 @@ def run_reference(args, world, rank):
     pkg = ge.load_package()
     ora = ge.load_oracle()
     ora.build()
-    case = pkg.workload.beach_256x256x96()
+    case = workload_case(pkg, args.workload)
     cls, sm, sy = ora.prepare(case)
     threads = os.cpu_count() or 1
     for _ in range(args.warmup):
@@ -190,10 +190,10 @@ def run_reference(args, world, rank):
         "n_gpus": args.gpus, "steps": args.steps, "warmup": args.warmup,
         "ms_per_step": 1000.0 * tot / args.steps, "higher_is_better": True, "scaling": "weak",
         "vs_baseline": None, "dtype": "f64", "data": "synthetic (seeded generator)",
-        "config": {"workload": WORKLOAD, "rows": sy.mnoe, "tol": case.eps0, "iters": last.iters},
+        "config": {"workload": args.workload, "rows": sy.mnoe, "tol": case.eps0, "iters": last.iters},
         "cpu_baseline": {"value": value, "unit": "solves/s", "cores": threads, "kind": "port",
                          "cpu_model": cpu_model(),
-                         "sample": f"full solves of {WORKLOAD} (N={sy.mnoe}, {last.iters} iterations), "
+                         "sample": f"full solves of {args.workload} (N={sy.mnoe}, {last.iters} iterations), "
                                    f"OpenMP restatement of pcgpme_para.F90, {threads} threads"},
         "e2e": {"value": value, "unit": "solves/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
     }
