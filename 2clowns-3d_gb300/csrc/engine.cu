@@ -1011,7 +1011,7 @@ static int check_abort(GridBar* gb, cudaStream_t s) {
     CLOWNS_CUDA_TRY(cudaMemcpyAsync(&abort, &gb->abort, sizeof(int), cudaMemcpyDeviceToHost, s));
     CLOWNS_CUDA_TRY(cudaStreamSynchronize(s));
     if (abort) {
-        set_last_error_msg("pcgpme: a grid barrier timed out; the solve was abandoned");
+        set_last_error_msg("pcgpme: a bounded device wait (grid barrier or staged copy) timed out; the solve was abandoned");
         return CLOWNS_ERR_NOCONV;
     }
     return CLOWNS_OK;
