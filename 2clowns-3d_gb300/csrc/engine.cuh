@@ -324,42 +324,62 @@ __device__ __forceinline__ void stop_member(MemberScalars* S, int reason, int ie
     if (ier) S->ier = ier;
 }
 
+// The member's scalars copied into the block's shared memory at a kernel's
+// start (44 words, one per thread), for the finalisation at its end.
+__device__ __forceinline__ void copy_scalars(MemberScalars& dst, const MemberScalars* S) {
+    constexpr int W = (int)(sizeof(MemberScalars) / 4);
+    if (threadIdx.x < W) ((int*)&dst)[threadIdx.x] = __ldcg((const int*)S + threadIdx.x);
+}
+
+// Old scalar values for a finalisation: read through L2 from the member's
+// scalars (PRE = false) or from a copy the block took when the kernel started
+// (PRE = true; nothing writes them while the kernel runs).
+template <bool PRE>
+__device__ __forceinline__ double rd(const double* p) { return PRE ? *p : sld(p); }
+template <bool PRE>
+__device__ __forceinline__ int rd(const int* p) { return PRE ? *p : sld(p); }
+
 // Finalisation of the reductions, by one thread once a member's totals are
 // known.  MODE 1: RQ -> ALP = C1 / RQ (pcgpme_para.F90:167); MODE 2: AMU =
 // (e,v) / (v,v) (197).
-template <int MODE>
-__device__ __forceinline__ void finish_sweep56(MemberScalars* S, const double (&tot)[2]) {
+template <int MODE, bool PRE = false>
+__device__ __forceinline__ void finish_sweep56(MemberScalars* S, const double (&tot)[2],
+                                               const MemberScalars* src = nullptr) {
+    if (!PRE) src = S;
     if (MODE == 1) {
-        const double C1 = sld(&S->C1);
+        const double C1 = rd<PRE>(&src->C1);
         S->RQ = tot[0];
         const double ALP = C1 / tot[0];                         // 167
         S->ALP = ALP;
         if (!isfinite(tot[0]) || !isfinite(ALP)) {
-            S->K = sld(&S->K) + 1;
-            stop_member(S, CLOWNS_STOP_NONFINITE, sld(&S->mode) != 1 ? CLOWNS_IER_NONFINITE : 0);
+            S->K = rd<PRE>(&src->K) + 1;
+            stop_member(S, CLOWNS_STOP_NONFINITE, rd<PRE>(&src->mode) != 1 ? CLOWNS_IER_NONFINITE : 0);
         }
     } else {
         S->SS = tot[1];
         const double AMU = tot[0] / tot[1];                     // 197
         S->AMU = AMU;
         if (!isfinite(tot[1]) || !isfinite(AMU)) {
-            S->K = sld(&S->K) + 1;
-            stop_member(S, CLOWNS_STOP_NONFINITE, sld(&S->mode) != 1 ? CLOWNS_IER_NONFINITE : 0);
+            S->K = rd<PRE>(&src->K) + 1;
+            stop_member(S, CLOWNS_STOP_NONFINITE, rd<PRE>(&src->mode) != 1 ? CLOWNS_IER_NONFINITE : 0);
         }
     }
 }
 
 // RN, C1 -> ERR, the stop tests and BETA (pcgpme_para.F90:215-254).
-__device__ __forceinline__ void finish_xrupdate(MemberScalars* S, const double (&tot)[2]) {
+template <bool PRE = false>
+__device__ __forceinline__ void finish_xrupdate(MemberScalars* S, const double (&tot)[2],
+                                                const MemberScalars* src = nullptr) {
+    if (!PRE) src = S;
     const double RN = tot[0], C1 = tot[1];
-    const double AMUs = sld(&S->AMU), RQ = sld(&S->RQ), BN = sld(&S->BN);
-    const double ERRP = sld(&S->ERRP), EPS = sld(&S->EPS);
-    const int mode = sld(&S->mode), ITER = sld(&S->ITER);
+    const double AMUs = rd<PRE>(&src->AMU), RQ = rd<PRE>(&src->RQ), BN = rd<PRE>(&src->BN);
+    const double ERRP = rd<PRE>(&src->ERRP), EPS = rd<PRE>(&src->EPS);
+    const int mode = rd<PRE>(&src->mode), ITER = rd<PRE>(&src->ITER);
     S->RN = RN;
     S->C1 = C1;
-    const int K = sld(&S->K) + 1;
+    const int K = rd<PRE>(&src->K) + 1;
     S->K = K;
-    S->total_iter = sld(&S->total_iter) + 1;
+    S->total_iter = rd<PRE>(&src->total_iter) + 1;
     const double ERR = sqrt(RN / BN);                            // 215
     S->ERR = ERR;
     if (!isfinite(RN) || !isfinite(C1)) {
@@ -1487,6 +1507,8 @@ __global__ void __launch_bounds__(kEngBlock, kBalMinBlocks<T, R>) k_bal_sweep56(
     int n, c0, c1;
     if (!bal_block(E, tab, bb, off, n, c0, c1)) return;
     const int done = sld(&E.S[bb.m].done);
+    __shared__ MemberScalars s_pre;
+    if (MODE != 0) copy_scalars(s_pre, E.S + bb.m);
     constexpr int CPS = R / kChunkRows;              // chunks per warp and step
     constexpr int NVAL = MODE == 2 ? 2 : 1;
     constexpr int B = kBalBatch<T, R, NVAL>;
@@ -1598,8 +1620,7 @@ __global__ void __launch_bounds__(kEngBlock, kBalMinBlocks<T, R>) k_bal_sweep56(
     double tot[2];
     if (!account_chunks(E, bb.m, c0, c1, tot) || lane != 0) return;
     E.ticket[bb.m] = 0;
-    finish_sweep56<MODE>(E.S + bb.m, tot);
-    __threadfence();
+    finish_sweep56<MODE, true>(E.S + bb.m, tot, &s_pre);   // kernel completion publishes it
 }
 
 template <typename T, int R>
@@ -1651,6 +1672,8 @@ __global__ void __launch_bounds__(kEngBlock, kBalMinBlocks<T, R>) k_bal_xrupdate
     if (!bal_block(E, tab, bb, off, n, c0, c1)) return;
     const int done = sld(&E.S[bb.m].done);
     const T ALP = T(sld(&E.S[bb.m].ALP)), AMU = T(sld(&E.S[bb.m].AMU));
+    __shared__ MemberScalars s_pre;
+    copy_scalars(s_pre, E.S + bb.m);
     constexpr int CPS = R / kChunkRows;
     constexpr int B = kBalBatch<T, R, 2>;
     constexpr int SPB = B / CPS;
@@ -1738,8 +1761,7 @@ __global__ void __launch_bounds__(kEngBlock, kBalMinBlocks<T, R>) k_bal_xrupdate
     double tot[2];
     if (!account_chunks(E, bb.m, c0, c1, tot) || lane != 0) return;
     E.ticket[bb.m] = 0;
-    finish_xrupdate(E.S + bb.m, tot);
-    __threadfence();
+    finish_xrupdate<true>(E.S + bb.m, tot, &s_pre);          // kernel completion publishes it
 }
 
 template <typename T, int R>
