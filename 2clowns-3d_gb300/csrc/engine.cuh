@@ -210,6 +210,17 @@ __device__ __forceinline__ void chunk_total(const Eng<T>& E, long gc, A (&v)[NV]
     if ((threadIdx.x & (32 / NV - 1)) == 0) put_chunk(E, gc, idx, (double)s);
 }
 
+// Ticket increment with acquire-release semantics at GPU scope: it releases
+// the writes that precede it in the issuing thread's order -- the writes of the
+// other threads of the block included, when a block or warp barrier separates
+// them from it -- and acquires the writes released by earlier increments, for
+// the issuing thread and for whatever a barrier orders after it.
+__device__ __forceinline__ unsigned ticket_add(unsigned* p, unsigned v) {
+    unsigned old;
+    asm volatile("atom.acq_rel.gpu.global.add.u32 %0, [%1], %2;" : "=r"(old) : "l"(p), "r"(v) : "memory");
+    return old;
+}
+
 // Called by EVERY thread of the block once the block's writers recorded the
 // totals of member m's chunks [c0, c1) (member-relative; empty allowed).  Accounts the chunks to their groups; the block that completes a
 // group sums it in one warp, and the warp that completes the member's last group
@@ -228,22 +239,20 @@ __device__ __noinline__ bool account_chunks(const Eng<T>& E, int m, int c0, int 
     bool fin = false;
     const int g_lo = c1 > c0 ? c0 / kGroupChunks : 0;
     const int g_hi = c1 > c0 ? (c1 - 1) / kGroupChunks : -1;
-    __threadfence();                              // this thread's chunk totals are visible device-wide
-    __syncthreads();                              // ... before any ticket of the block
+    __syncthreads();                              // the block's chunk totals precede its tickets
     for (int gb = g_lo; gb <= g_hi || gb == g_lo; gb += kList) {
         if (threadIdx.x == 0) s_n = 0;
         __syncthreads();
         for (int g = gb + threadIdx.x; g <= g_hi && g < gb + kList; g += blockDim.x) {
             const int cnt = min(c1, (g + 1) * kGroupChunks) - max(c0, g * kGroupChunks);
             const int need = min(kGroupChunks, nc - g * kGroupChunks);
-            const unsigned old = atomicAdd(&E.gticket[G0 + g], (unsigned)cnt);
+            const unsigned old = ticket_add(&E.gticket[G0 + g], (unsigned)cnt);
             if (old + (unsigned)cnt == (unsigned)need) s_list[atomicAdd(&s_n, 1)] = g;
         }
         __syncthreads();
         const int nd = s_n;
         for (int q = wid; q < nd; q += nw) {
-            const int g = s_list[q];
-            __threadfence();
+            const int g = s_list[q];                // acquired by the ticket that completed it
             const long p0 = 2 * (gc0 + (long)g * kGroupChunks);
             const int cg = min(kGroupChunks, nc - g * kGroupChunks);
             double a = 0.0, b = 0.0;
@@ -258,15 +267,14 @@ __device__ __noinline__ bool account_chunks(const Eng<T>& E, int m, int c0, int 
             double s = warp_pair_sum(a, b);
             if (lane == 0) E.gpartials[2L * (G0 + g) + 0] = s;
             if (lane == 16) E.gpartials[2L * (G0 + g) + 1] = s;
-            if (lane == 0 || lane == 16) __threadfence();
-            __syncwarp();
+            __syncwarp();                           // both totals precede lane 0's ticket
             unsigned last = 0;
             if (lane == 0) {
                 E.gticket[G0 + g] = 0;
-                last = atomicAdd(&E.ticket[m], 1u) == (unsigned)ng - 1u;
+                last = ticket_add(&E.ticket[m], 1u) == (unsigned)ng - 1u;
             }
+            __syncwarp();                           // lane 0's acquire precedes the warp's loads
             if (__shfl_sync(0xffffffffu, last, 0)) {
-                __threadfence();
                 a = b = 0.0;
                 for (int j = lane; j < ng; j += 32) {
                     a += __ldcg(E.gpartials + 2L * (G0 + j) + 0);
