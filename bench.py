@@ -56,7 +56,7 @@ def measured_peaks():
 # accumulation; 96 B for the FP64 -> FP32 conversion).
 # Measured DRAM bytes per row and iteration of the loop graph (ncu, the graph as
 # one unit, beach_256x256x96): profiles/pcgpme_loop_dram_beach_256x256x96.md.
-TRAFFIC_ROW_ITER_FP64 = 434.0
+TRAFFIC_ROW_ITER_FP64 = 434.2
 TRAFFIC_ROW_ITER_MIXED = 224.6
 
 # FP64 arithmetic of one iteration per row, in fused multiply-adds (a multiply or
