@@ -374,8 +374,7 @@ int clowns_face_grad_dev(const int* dims, int inne, int inne2, int ifln, const i
  * The call allocates nothing (no cudaMalloc/cudaFree, no allocating library
  * routine) and returns CLOWNS_ERR_LIMIT for n > CLOWNS_STATIC_MAX_ROWS.  The
  * first call on a device looks up the array's device address (once per device,
- * with that device current); make that first call before any stream capture.
- * Every call shares the array and re-initialises what it reads, so calls that
+ * with that device current).  Every call shares the array and re-initialises what it reads, so calls that
  * overlap on the GPU (other streams or host threads) race on it. */
 int clowns_pcgpme_static_dev(const double* al, int nl, int na, const int* ll, const double* d,
                              int n, const double* b, double* x, double eps, double parm, int iter,
