@@ -194,8 +194,8 @@ __device__ __forceinline__ A warp_tsum(A (&v)[V], int& idx) {
 }
 
 // Record a chunk total (global chunk index gc, value k of NV) -- by one lane.
-// Plain store: account_chunks fences every thread's stores once, before the
-// block's tickets.
+// Plain store: account_chunks orders every thread's stores before the block's
+// tickets (a block barrier, then acquire-release ticket increments).
 template <typename T>
 __device__ __forceinline__ void put_chunk(const Eng<T>& E, long gc, int k, double v) {
     E.partials[2 * gc + k] = v;
@@ -222,9 +222,10 @@ __device__ __forceinline__ unsigned ticket_add(unsigned* p, unsigned v) {
 }
 
 // Called by EVERY thread of the block once the block's writers recorded the
-// totals of member m's chunks [c0, c1) (member-relative; empty allowed).  Accounts the chunks to their groups; the block that completes a
-// group sums it in one warp, and the warp that completes the member's last group
-// sums the member.  Returns true in all lanes of that warp, with the member
+// totals of member m's chunks [c0, c1) (member-relative; empty allowed).
+// Accounts the chunks to their groups; the block that completes a group sums it
+// in one warp, and the warp that completes the member's last group sums the
+// member.  Returns true in all lanes of that warp, with the member
 // totals in tot[] (every lane); false elsewhere.
 template <typename T>
 __device__ __noinline__ bool account_chunks(const Eng<T>& E, int m, int c0, int c1, double (&tot)[2]) {
