@@ -201,7 +201,8 @@ int clowns_test_arm_wait_timeout(long polls, int absent_block);
 
 /* Kernels the calling thread's last solve (plain or mixed, single or batched)
  * launched: host launches plus the kernel nodes its loop graphs executed
- * (16 per iteration), not counting the autotuner's one-time trial runs.
+ * (per iteration 16 with single LDUSUB sweeps, 12 with fused sweep pairs, the
+ * loop guard included), not counting the autotuner's one-time trial runs.
  * Engine bookkeeping with no counterpart in the reference. */
 long clowns_last_kernel_launches(void);
 
