@@ -4,8 +4,9 @@
  * TEST INFRASTRUCTURE ONLY: the checker for the CUDA path.  Only the tests, the
  * smoke check and the CPU-baseline leg of the benchmark load this library.
  *
- * Parity status: UNPINNED (no Fortran compiler, no reference fixtures); see the
- * header file.  Each function cites the reference lines it restates.  The
+ * Parity status: pinned to the reference's own source, run through a Fortran
+ * translator (no Fortran compiler exists here); see the header file.  Each
+ * function cites the reference lines it restates.  The
  * arithmetic keeps the reference's evaluation order; the build uses
  * -ffp-contract=off so no multiply-add is fused on any host, which keeps the
  * matrix coefficients (and hence the per-row sort) bit-reproducible.

@@ -5,11 +5,18 @@
  * tests, the smoke check and the CPU-baseline leg of the benchmark call it; the
  * product library never links or calls it.
  *
- * Parity status: UNPINNED.  The reference is Fortran 90 built only with ifort
- * (src2LOWNS/Makefile:1,5); no Fortran compiler exists where this was written,
- * and the reference ships no tests, golden vectors or input cases.  The
- * restatement is therefore pinned only by hand-derived known-answer tests,
- * algebraic properties and an independent scipy direct solve.
+ * Parity status: pinned to the reference's own source, executed.  The
+ * reference is Fortran 90 built only with ifort (src2LOWNS/Makefile:1,5), no
+ * Fortran compiler exists where this was written, and the reference ships no
+ * tests, golden vectors or input cases.  Its routines are run instead through
+ * a translator of the Fortran subset they use (tests/golden/fortran_exec.py,
+ * whose semantics tests/test_fortran_exec.py fixes), and this restatement
+ * reproduces their outputs bit for bit (tests/test_oracle_reference_runs.py):
+ * set_nflag, init_matrix, numbering and right-hand side, cal_matrix_element,
+ * PCGPME, the ik loop with the correction, and PCGPME_WILL.  The pin is to the
+ * source's written evaluation order; the ifort build (-O3 -xHost) may fuse or
+ * reorder floating-point operations, which nothing here can reproduce.
+ * Hand-derived known answers and a scipy direct solve check it as well.
  *
  * Array conventions (identical to the reference's module arrays):
  *   dims[6]      = is, js, ks, ie, je, ke

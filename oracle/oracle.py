@@ -1,7 +1,8 @@
 """ctypes front end of the CPU oracle (test infrastructure only).
 
 Loaded by the tests, the smoke check and the CPU-baseline leg of the benchmark.
-It never backs the product path.  Parity status: unpinned (see clowns_oracle.h).
+It never backs the product path.  Parity status: pinned to the reference's own
+source, run through a Fortran translator (see clowns_oracle.h).
 """
 from __future__ import annotations
 

@@ -1,0 +1,207 @@
+"""Run the reference's own Fortran routines on seeded cases and record their
+outputs in tests/golden/reference_runs.json.
+
+The reference builds only with ifort (src2LOWNS/Makefile:1,5) and no Fortran
+compiler exists here, so its source files are executed through
+tests/golden/fortran_exec.py, which translates the Fortran they use to Python
+in memory (never stored) with the build's macros (Makefile:5: -DRAN -DNORMAL
+-DOBJECT -DSLIDE0, -r8) and one OpenMP thread.  The routines run are the
+reference's own, chained as the model chains them:
+
+  set_nflag              src2LOWNS/nfd2015.F90:7-306 (fxx1 308-332), from the raw flags
+  init_matrix            src2LOWNS/1sub-matrix.F90:3-95
+  cal_err_of_continuity  src2LOWNS/1sub-momentum.F90:235-417 (renzoku_n 1sub-main.F90:579-602,
+                         renzoku_fv lib/src/math_func.F90:51-54, alloc_matrix 0mod-arrays.F90:356-370)
+  cal_matrix_element     src2LOWNS/1sub-momentum.F90:465-551
+  cal_poisson_equation   src2LOWNS/1sub-momentum.F90:553-588 -> PCGPME, pcgpme_para.F90:1-353
+  the ik loop            src2LOWNS/1sub-momentum.F90:41-60 (check_dmax 419-463, p -= xe,
+                         estimate_velocity2 590-651, momentum_d math_func.F90:251-255)
+  PCGPME_WILL            src2LOWNS/pcgpme_2DH.f90:1-373
+
+The module constants come from the reference's module files (0mod-variables.F90);
+the case data fill the module arrays in the bounds the reference allocates them
+with (0mod-arrays.F90:205-237, 290, 356-370); lf is the identity
+(main_2CLOWNS.F90:33) and dim3d follows main_2CLOWNS.F90:43-44.
+
+Only digests (sha256 of each output's bytes) and scalars are written: the cases
+are rebuilt from the seeded generator by tests/golden/reference_cases.py, and
+tests/test_oracle_reference_runs.py checks the oracle against these outputs bit
+for bit.  The reference is read from REFERENCE_ROOT (default /root/reference).
+
+Usage:  python tests/golden/make_ref_golden.py [REFERENCE_ROOT]
+"""
+from __future__ import annotations
+
+import json
+import pathlib
+import sys
+import time
+
+import numpy as np
+
+HERE = pathlib.Path(__file__).resolve().parent
+sys.path.insert(0, str(HERE))
+
+import fortran_exec as fx  # noqa: E402
+import reference_cases as rc  # noqa: E402
+
+DEFINES = {"RAN", "NORMAL", "OBJECT", "SLIDE0"}
+GRID_SOURCES = ["src2LOWNS/0mod-type_interface.F90", "src2LOWNS/0mod-variables.F90",
+                "src2LOWNS/0mod-arrays.F90", "src2LOWNS/nfd2015.F90", "src2LOWNS/1sub-matrix.F90",
+                "src2LOWNS/1sub-momentum.F90", "src2LOWNS/1sub-main.F90", "lib/src/math_func.F90",
+                "src2LOWNS/pcgpme_para.F90"]
+WILL_SOURCES = ["src2LOWNS/0mod-type_interface.F90", "src2LOWNS/0mod-variables.F90",
+                "src2LOWNS/pcgpme_2DH.f90"]
+# cal_err_of_continuity reads its local k, set only by the numbering branch of
+# the first ik pass, on later passes too (1sub-momentum.F90:352), where it only
+# chooses DMAX1, which nothing reads; 0 stands in for the undefined value.
+UNDEFINED = {("cal_err_of_continuity", "k"): 0}
+
+
+def allocate_matrix(prog, V, A):
+    """The allocation cal_err_of_continuity makes on the first ik pass
+    (1sub-momentum.F90:253-255: m_alloc = ifln + 5000, alloc_matrix), done
+    before it so that xe(0) can be given a value: estimate_velocity2 reads
+    xe(0) for a cell or neighbour without a matrix row (mno = 0,
+    1sub-momentum.F90:606, 617, 632, 640), an element nothing writes; the
+    memory ALLOCATE hands out fresh is zero, and 0 stands in for it."""
+    V.f_m_alloc = V.f_ifln + 5000
+    prog.call("alloc_matrix", V.f_m_alloc, V.f_ie, V.f_je, V.f_ke)
+    A.f_xe[0] = 0.0
+
+
+class CellFlag:
+    """type(cellflag) (0mod-type_interface.F90:7-9)."""
+
+    __slots__ = ("f_f", "f_b", "f_fp", "f_bp")
+
+    def __init__(self, f, b):
+        self.f_f, self.f_b, self.f_fp, self.f_bp = f, b, None, None
+
+
+def farray(kind, values, bounds):
+    lb = [lo for lo, _ in bounds]
+    ext = [hi - lo + 1 for lo, hi in bounds]
+    conv = {"real": float, "int": int}.get(kind, lambda v: v)
+    vals = [conv(v) for v in values]
+    n = int(np.prod(ext))
+    if len(vals) != n:
+        raise ValueError(f"{len(vals)} values for {n} elements")
+    return fx.FArray(vals, 0, lb, ext, kind)
+
+
+def program(root: pathlib.Path, sources):
+    texts = [(root / f).read_text(encoding="latin-1") for f in sources]
+    return fx.Program(texts, DEFINES, undefined=UNDEFINED)
+
+
+def load_grid(prog, case):
+    """Module state of one domain before set_nflag, from the case's raw flags."""
+    V, A = prog.module("variables"), prog.module("arrays")
+    is_, js, ks, ie, je, ke = (int(v) for v in case.dims)
+    V.f_is, V.f_js, V.f_ks, V.f_ie, V.f_je, V.f_ke = is_, js, ks, ie, je, ke
+    V.f_inns, V.f_inne, V.f_inne2 = 1, int(case.inne), int(case.inne2)
+    V.f_dt, V.f_eps0 = float(case.dt), float(case.eps0)
+    V.f_ik, V.f_m_alloc, V.f_n, V.f_t, V.f_icon, V.f_ricon = 0, 0, 1, 0.0, 0, 0
+    V.f_isfn, V.f_isfn2, V.f_ifln = 0, 0, 0
+    m2 = int(case.inne2) + 1
+    A.f_lf = farray("int", [1 if r == c else 0 for c in range(3) for r in range(3)], [(0, 2), (0, 2)])
+    A.f_dim3d = not (is_ == ie - 1 or js == je - 1)
+    for nm, arr in (("in", case.in_), ("jn", case.jn), ("kn", case.kn)):
+        setattr(A, "f_" + nm, farray("int", arr[1:m2 + 1], [(1, m2)]))
+    A.f_nff = farray("obj", [CellFlag(int(f), int(b)) for f, b in zip(case.nf, case.nfb)], [(0, m2)])
+    A.f_fb = farray("real", case.fb, [(0, m2)])
+    A.f_f = farray("real", case.f, [(0, m2)])
+    A.f_a = farray("real", case.a.ravel(), [(0, 2), (0, m2)])
+    A.f_un = farray("real", case.un.ravel(), [(0, 2), (0, m2)])
+    A.f_dx = farray("real", case.dx.ravel(), [(0, 2), (1, case.mx2)])
+    A.f_x = farray("real", case.x.ravel(), [(0, 2), (1, case.mx2)])
+    A.f_mn = farray("int", case.mn.ravel(), [(is_ - 2, ie + 2), (ks - 2, ke + 2), (js - 2, je + 2)])
+    A.f_sp = farray("real", case.sp.ravel(), [(0, m2), (0, 2)])
+    A.f_objno = farray("int", case.objno, [(0, m2)])
+    A.f_fln = farray("int", [0] * (m2 + 1), [(1, m2 + 1)])
+    A.f_sfn = farray("int", [0] * (m2 + 1), [(1, m2 + 1)])
+    A.f_p = farray("real", [0.0] * (m2 + 1), [(0, m2)])
+    return V, A
+
+
+def vals(a):
+    return np.array(a.values())
+
+
+def run_grid(root, case, solve: bool, loop: bool) -> dict:
+    d = rc.digest
+    out = {"input": rc.case_digest(case)}
+    prog = program(root, GRID_SOURCES)
+    V, A = load_grid(prog, case)
+    prog.call("set_nflag")
+    nff = A.f_nff.values()
+    ifln, isfn = V.f_ifln, V.f_isfn
+    out["nflag"] = {"nf": d(np.array([o.f_f for o in nff])), "nfb": d(np.array([o.f_b for o in nff])),
+                    "f": d(vals(A.f_f)), "ifln": ifln, "fln": d(vals(A.f_fln)[:ifln]), "isfn": isfn,
+                    "sfn": d(vals(A.f_sfn)[:isfn])}
+    prog.call("init_matrix")
+    allocate_matrix(prog, V, A)
+    nl, inne = V.f_nl, V.f_inne
+    de_c = vals(A.f_de_c)
+    alu_c = vals(A.f_alu_c).reshape(nl, inne)
+    ll_c = np.array([-1 if v is None else v for v in A.f_ll_c.values()]).reshape(nl, inne)
+    # rows init_matrix skips (objects, fb = 0: 1sub-matrix.F90:26) stay undefined in the reference
+    undefined = np.isnan(de_c)
+    if not np.array_equal(np.isnan(alu_c).any(axis=0), undefined):
+        raise RuntimeError("init_matrix left part of a row undefined")
+    rows = ~undefined
+    out["init"] = {"nl": nl, "mp": V.f_mp, "undefined_rows": rc.runs(np.flatnonzero(undefined) + 1),
+                   "alu_c": d(alu_c[:, rows]), "ll_c": d(ll_c[:, rows]), "de_c": d(de_c[rows])}
+    prog.call("cal_err_of_continuity")
+    mnoe, mm2 = V.f_mnoe, V.f_mm2
+    out["rows"] = {"mnoe": mnoe, "mm2": mm2, "dmax": V.f_dmax, "mno": d(vals(A.f_mno)),
+                   "mno2mn": d(vals(A.f_mno2mn)[:mnoe]), "b": d(vals(A.f_b)[:mnoe])}
+    prog.call("cal_matrix_element")
+    out["asm"] = {"alu": d(vals(A.f_alu).reshape(nl, mm2)[:, :mnoe]),
+                  "llu": d(vals(A.f_llu).reshape(nl, mm2)[:, :mnoe]), "de": d(vals(A.f_de)[:mnoe])}
+    if solve:
+        prog.call("cal_poisson_equation")
+        out["solve"] = {"iter": V.f_iter, "eps": V.f_eps, "ier": prog.env["s_cal_poisson_equation"].f_ier,
+                        "x": d(vals(A.f_xe)[1:mnoe + 1])}
+    if loop:
+        prog = program(root, GRID_SOURCES)
+        prog.fragment("cal_momentum", 41, 60, "ik_loop")
+        V, A = load_grid(prog, case)
+        V.f_d0, V.f_eps0 = rc.LOOP_D0, rc.LOOP_EPS0
+        prog.call("set_nflag")
+        prog.call("init_matrix")
+        allocate_matrix(prog, V, A)
+        prog.call("ik_loop")
+        out["loop"] = {"ik": V.f_ik, "dmax": V.f_dmax, "p": d(vals(A.f_p)),
+                       "un": d(vals(A.f_un).reshape(-1, 3))}
+    return out
+
+
+def run_will(root, ds, eps) -> dict:
+    prog = program(root, WILL_SOURCES)
+    nl, na = ds.al.shape
+    n = ds.n
+    al = farray("real", [ds.al[k, i] for k in range(nl) for i in range(na)], [(1, na), (1, nl)])
+    ll = farray("int", [ds.ll[k, i] for k in range(nl) for i in range(na)], [(1, na), (1, nl)])
+    dd = farray("real", ds.d[:n], [(1, n)])
+    bb = farray("real", ds.b[:n], [(1, n)])
+    prog.call("pcgpme_will", al, nl, na, ll, dd, n, 64, bb, float(eps), 5.0, 10000)
+    return {"input": rc.will_digest(ds), "b": rc.digest(vals(bb))}
+
+
+def main(argv):
+    root = pathlib.Path(argv[1] if len(argv) > 1 else "/root/reference")
+    res = {"grids": {}, "will": {}}
+    for label, (case, solve, loop) in rc.grid_cases().items():
+        t = time.time()
+        res["grids"][label] = run_grid(root, case, solve, loop)
+        print(f"{label}: {time.time() - t:.1f} s", flush=True)
+    for label, (ds, eps) in rc.will_cases().items():
+        res["will"][label] = run_will(root, ds, eps)
+        print(f"{label}: done", flush=True)
+    (HERE / "reference_runs.json").write_text(json.dumps(res, indent=1, sort_keys=True) + "\n")
+
+
+if __name__ == "__main__":
+    main(sys.argv)

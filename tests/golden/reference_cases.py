@@ -1,0 +1,131 @@
+"""Inputs on which the reference's own routines were run (tests/golden/make_ref_golden.py)
+and the oracle is checked against their outputs (tests/test_oracle_reference_runs.py).
+
+Every case is rebuilt from the seeded generator, so the committed fixture holds
+only the reference's outputs (hashes of their bytes and scalars).  A digest of
+the inputs is stored beside them: a changed generator shows as an input
+mismatch, not as a false parity failure.
+"""
+from __future__ import annotations
+
+import hashlib
+import pathlib
+import sys
+
+import numpy as np
+
+HERE = pathlib.Path(__file__).resolve().parent
+for _p in (HERE.parent.parent, HERE.parent, HERE):
+    if str(_p) not in sys.path:
+        sys.path.insert(0, str(_p))
+
+import __graft_entry__ as ge  # noqa: E402
+
+wl = ge.load_package().workload
+
+
+def speckled(case, seed: int, droplets: int, bubbles: int):
+    """The case with seeded droplets above its free surface (air cells given a
+    volume fraction) and bubbles below it (fluid cells emptied), so that the
+    surface classification prunes isolated surface cells and loops."""
+    c = case.copy()
+    rng = np.random.default_rng(seed)
+    inne = c.inne
+    f = c.f
+    air = np.flatnonzero((c.nf[1:inne + 1] == 0) & (c.fb[1:inne + 1] > 0.0)) + 1
+    wet = np.flatnonzero((c.nf[1:inne + 1] == 1) & (f[1:inne + 1] >= 1.0)) + 1
+    if len(air):
+        pick = rng.choice(air, size=min(droplets, len(air)), replace=False)
+        f[pick] = rng.uniform(0.05, 1.0, size=len(pick))
+        c.nf[pick] = 1
+    if len(wet):
+        pick = rng.choice(wet, size=min(bubbles, len(wet)), replace=False)
+        f[pick] = 0.0
+        c.nf[pick] = 0
+    c.label = (c.label or "") + "+speckled"
+    return c
+
+
+def grid_cases():
+    """label -> (case, run the solve, run the ik loop).  Solves and ik loops run
+    only on the systems small enough for the translated reference (a few
+    thousand rows); classification, coefficients, numbering, right-hand side
+    and assembly run on all."""
+    from make_golden import golden_cases
+    from cases import small_cases
+
+    out = {}
+    for label, c in golden_cases().items():
+        out[label] = (c, True, True)
+    small = dict(small_cases())
+    for label in ("tank_24x20x16", "flume2dv_96x1x32", "section2dv_1x80x24"):
+        out[label] = (small[label], True, False)
+    for label in ("beach_48x40x24", "bore_40x24x32", "shore_64x16x24", "flume_40x24x20_ingested"):
+        out[label] = (small[label], False, False)
+    base = wl.make_case(20, 12, 16, dz=0.05, slope=0.25, n_obstacles=2, seed=41, amplitude=0.08,
+                        step_layers=2)
+    out["speckled_20x12x16"] = (speckled(base, seed=42, droplets=40, bubbles=25), True, True)
+    base2 = wl.make_case(24, 1, 16, dz=0.05, slope=0.25, n_obstacles=0, seed=43, amplitude=0.08)
+    out["speckled2dv_24x1x16"] = (speckled(base2, seed=44, droplets=12, bubbles=8), True, True)
+    return out
+
+
+def will_cases():
+    """label -> (2DH system, tolerance): PCGPME_WILL inputs."""
+    return {
+        "dispersion_14x10": (wl.dispersion_system(14, 10, seed=5), 1e-12),
+        "dispersion_24x18": (wl.dispersion_system(24, 18, seed=7), 1e-10),
+        "dispersion_30x8": (wl.dispersion_system(30, 8, seed=3), 1e-12),
+        "dispersion_40x32": (wl.dispersion_system(40, 32, seed=11), 1e-12),
+    }
+
+
+LOOP_D0, LOOP_EPS0 = 1e-9, 1e-7          # two or more ik passes on the small grids
+
+
+def digest(a) -> str:
+    """sha256 of an array's dtype, shape and bytes (little-endian)."""
+    a = np.asarray(a)
+    if a.dtype.kind == "O":                      # values of a translated array slice
+        a = np.array(a.tolist())
+        if a.dtype.kind == "O":
+            raise ValueError("undefined values in a recorded output")
+    if a.dtype.kind == "f":
+        a = a.astype("<f8")
+    elif a.dtype.kind in "iu":
+        a = a.astype("<i8")
+    elif a.dtype.kind == "b":
+        a = a.astype("u1")
+    h = hashlib.sha256()
+    h.update(str(a.dtype).encode() + str(a.shape).encode())
+    h.update(np.ascontiguousarray(a).tobytes())
+    return h.hexdigest()
+
+
+def runs(idx) -> list:
+    """Sorted indices as inclusive [first, last] runs."""
+    out = []
+    for i in (int(v) for v in idx):
+        if out and out[-1][1] == i - 1:
+            out[-1][1] = i
+        else:
+            out.append([i, i])
+    return out
+
+
+def runs_mask(r, n: int) -> np.ndarray:
+    """Boolean mask over 1..n (index 0 = row 1) of the rows the runs list."""
+    m = np.zeros(n, dtype=bool)
+    for a, b in r:
+        m[a - 1:b] = True
+    return m
+
+
+def case_digest(c) -> str:
+    parts = [c.dims, c.mn, c.in_, c.jn, c.kn, c.nf, c.nfb, c.f, c.fb, c.a, c.un, c.sp, c.x, c.dx, c.objno,
+             np.array([c.dt, c.eps0])]
+    return digest(np.concatenate([np.asarray(p, dtype=np.float64).ravel() for p in parts]))
+
+
+def will_digest(ds) -> str:
+    return digest(np.concatenate([np.asarray(p, dtype=np.float64).ravel() for p in (ds.al, ds.ll, ds.d, ds.b)]))

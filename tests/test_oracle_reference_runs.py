@@ -1,0 +1,101 @@
+"""The oracle against the reference's own routines, run on the same seeded inputs.
+
+tests/golden/reference_runs.json holds the outputs of the reference's Fortran
+source (set_nflag, init_matrix, cal_err_of_continuity, cal_matrix_element,
+cal_poisson_equation/PCGPME, the ik loop of 1sub-momentum.F90:41-60 and
+PCGPME_WILL), executed here by tests/golden/make_ref_golden.py through
+tests/golden/fortran_exec.py because no Fortran compiler exists.  Each output
+is stored as a sha256 digest of its bytes; the oracle must reproduce every one
+bit for bit (its serial loop order is the reference's).
+"""
+import json
+import pathlib
+import sys
+
+import numpy as np
+import pytest
+
+HERE = pathlib.Path(__file__).resolve().parent
+sys.path.insert(0, str(HERE / "golden"))
+
+import reference_cases as rc  # noqa: E402
+
+RUNS = json.loads((HERE / "golden" / "reference_runs.json").read_text())
+d = rc.digest
+
+
+@pytest.fixture(scope="module")
+def grids():
+    return rc.grid_cases()
+
+
+def _check(stage, got: dict, want: dict):
+    bad = [k for k in want if k in got and got[k] != want[k]]
+    assert not bad, f"{stage}: {bad} differ from the reference's run"
+
+
+def oracle_loop(ora, case, cls, sm, d0, eps0):
+    """The ik loop (1sub-momentum.F90:41-60) through the oracle's routines."""
+    c = case.copy()
+    c.f = cls.f.copy()
+    p = np.zeros(case.inne2 + 2)
+    un = case.un.copy()
+    ik = 0
+    while True:
+        c.un = un
+        sy = ora.rows_rhs_assemble(c, cls, sm)
+        if sy.dmax < d0:
+            break
+        ik += 1
+        if ik > 1000:
+            break
+        r = ora.pcgpme(sy.alu, sy.llu, sy.de[1:], sy.b[1:], sy.mnoe, eps=eps0)
+        p, un = ora.correct(c, cls, sy, r.x, p, un)
+    return ik, sy.dmax, p, un
+
+
+@pytest.mark.parametrize("label", sorted(RUNS["grids"]))
+def test_oracle_reproduces_reference_run(ora, grids, label):
+    want = RUNS["grids"][label]
+    case, solve, loop = grids[label]
+    assert rc.case_digest(case) == want["input"], "the seeded generator changed: regenerate the fixture"
+    cls = ora.set_nflag(case)
+    _check("set_nflag", {"nf": d(cls.nf), "nfb": d(cls.nfb), "f": d(cls.f), "ifln": cls.ifln,
+                         "fln": d(cls.fln[1:]), "isfn": cls.isfn, "sfn": d(cls.sfn[1:])}, want["nflag"])
+    sm = ora.init_matrix(case, cls)
+    rows = ~rc.runs_mask(want["init"]["undefined_rows"], case.inne)
+    _check("init_matrix", {"nl": sm.alu_c.shape[0], "mp": sm.mp, "alu_c": d(sm.alu_c[:, rows]),
+                           "ll_c": d(sm.ll_c[:, rows]), "de_c": d(sm.de_c[rows])}, want["init"])
+    sy = ora.rows_rhs_assemble(case, cls, sm)
+    n = sy.mnoe
+    _check("rows and RHS", {"mnoe": n, "mm2": sy.mm2, "dmax": sy.dmax, "mno": d(sy.mno.ravel()),
+                            "mno2mn": d(sy.mno2mn[1:n + 1]), "b": d(sy.b[1:n + 1])}, want["rows"])
+    _check("cal_matrix_element", {"alu": d(sy.alu[:, :n]), "llu": d(sy.llu[:, :n]), "de": d(sy.de[1:n + 1])},
+           want["asm"])
+    if solve:
+        r = ora.pcgpme(sy.alu, sy.llu, sy.de[1:], sy.b[1:], n, eps=case.eps0, parm=5.0, itmax=10000, nthreads=1)
+        _check("PCGPME", {"iter": r.iters, "eps": r.eps, "ier": r.ier, "x": d(r.x[:n])}, want["solve"])
+    if loop:
+        ik, dmax, p, un = oracle_loop(ora, case, cls, sm, rc.LOOP_D0, rc.LOOP_EPS0)
+        _check("ik loop", {"ik": ik, "dmax": dmax, "p": d(p), "un": d(un)}, want["loop"])
+
+
+@pytest.mark.parametrize("label", sorted(RUNS["will"]))
+def test_oracle_will_reproduces_reference_run(ora, label):
+    want = RUNS["will"][label]
+    ds, eps = rc.will_cases()[label]
+    assert rc.will_digest(ds) == want["input"], "the seeded generator changed: regenerate the fixture"
+    b, _, _ = ora.pcgpme_will(ds.al, ds.ll, ds.d, ds.b, ds.n, eps=eps)
+    assert d(b) == want["b"]
+
+
+def test_fixture_covers_every_stage():
+    """The recorded runs include 3D and 2DV grids, surface pruning cases, solves,
+    multi-pass ik loops and cells init_matrix skips."""
+    g = RUNS["grids"]
+    assert {"nflag", "init", "rows", "asm"} <= set().union(*(v.keys() for v in g.values()))
+    assert sum("solve" in v for v in g.values()) >= 8
+    assert sum("loop" in v and v["loop"]["ik"] >= 2 for v in g.values()) >= 5
+    assert any(v["init"]["nl"] == 4 for v in g.values()) and any(v["init"]["nl"] == 6 for v in g.values())
+    assert any(v["init"]["undefined_rows"] for v in g.values())
+    assert len(RUNS["will"]) >= 3
