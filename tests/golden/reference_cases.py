@@ -1,10 +1,11 @@
 """Inputs on which the reference's own routines were run (tests/golden/make_ref_golden.py)
 and the oracle is checked against their outputs (tests/test_oracle_reference_runs.py).
 
-Every case is rebuilt from the seeded generator, so the committed fixture holds
-only the reference's outputs (hashes of their bytes and scalars).  A digest of
-the inputs is stored beside them: a changed generator shows as an input
-mismatch, not as a false parity failure.
+Every case is rebuilt from the seeded generator and its real-valued fields are
+rounded to a fixed binary grid (the same inputs on x86-64 and aarch64), so the
+committed fixture holds only the reference's outputs (hashes of their bytes and
+scalars).  A digest of the inputs is stored beside them: a changed generator
+shows as an input mismatch, not as a false parity failure.
 """
 from __future__ import annotations
 
@@ -22,6 +23,29 @@ for _p in (HERE.parent.parent, HERE.parent, HERE):
 import __graft_entry__ as ge  # noqa: E402
 
 wl = ge.load_package().workload
+
+
+QUANTUM = 2.0 ** -24
+
+
+def portable(case):
+    """The case with its real-valued fields rounded to multiples of 2**-24.
+    The seeded generator's transcendental functions (numpy's cosh, its normal
+    sampler) differ in the last bits between x86-64 and aarch64; after the
+    rounding both give the same inputs, so outputs recorded on one machine
+    check the code on the other."""
+    c = case.copy()
+    for name in ("f", "fb", "a", "un", "sp", "x", "dx"):
+        v = getattr(c, name)
+        setattr(c, name, np.round(v / QUANTUM) * QUANTUM)
+    return c
+
+
+def portable_will(ds):
+    for name in ("al", "d", "b"):
+        v = getattr(ds, name)
+        setattr(ds, name, np.round(v / QUANTUM) * QUANTUM)
+    return ds
 
 
 def speckled(case, seed: int, droplets: int, bubbles: int):
@@ -67,16 +91,16 @@ def grid_cases():
     out["speckled_20x12x16"] = (speckled(base, seed=42, droplets=40, bubbles=25), True, True)
     base2 = wl.make_case(24, 1, 16, dz=0.05, slope=0.25, n_obstacles=0, seed=43, amplitude=0.08)
     out["speckled2dv_24x1x16"] = (speckled(base2, seed=44, droplets=12, bubbles=8), True, True)
-    return out
+    return {k: (portable(c), s, lp) for k, (c, s, lp) in out.items()}
 
 
 def will_cases():
     """label -> (2DH system, tolerance): PCGPME_WILL inputs."""
     return {
-        "dispersion_14x10": (wl.dispersion_system(14, 10, seed=5), 1e-12),
-        "dispersion_24x18": (wl.dispersion_system(24, 18, seed=7), 1e-10),
-        "dispersion_30x8": (wl.dispersion_system(30, 8, seed=3), 1e-12),
-        "dispersion_40x32": (wl.dispersion_system(40, 32, seed=11), 1e-12),
+        "dispersion_14x10": (portable_will(wl.dispersion_system(14, 10, seed=5)), 1e-12),
+        "dispersion_24x18": (portable_will(wl.dispersion_system(24, 18, seed=7)), 1e-10),
+        "dispersion_30x8": (portable_will(wl.dispersion_system(30, 8, seed=3)), 1e-12),
+        "dispersion_40x32": (portable_will(wl.dispersion_system(40, 32, seed=11)), 1e-12),
     }
 
 

@@ -1,0 +1,56 @@
+"""The CUDA path against the reference's own routines: classification
+(set_nflag), static coefficients (init_matrix), numbering and right-hand side
+(cal_err_of_continuity) and assembly (cal_matrix_element) bit for bit on the 14
+grids of tests/golden/reference_runs.json -- outputs of the reference's Fortran
+source, run on the CPU by tests/golden/make_ref_golden.py.  (The solves are
+compared with the oracle within their tolerance in tests/test_gpu_parity.py and
+tests/test_gpu_configs.py; the oracle reproduces the reference's solves bit for
+bit, tests/test_oracle_reference_runs.py.)"""
+import json
+import pathlib
+import sys
+
+import numpy as np
+import pytest
+
+HERE = pathlib.Path(__file__).resolve().parent
+sys.path.insert(0, str(HERE / "golden"))
+
+import reference_cases as rc  # noqa: E402
+
+pytestmark = pytest.mark.gpu
+
+RUNS = json.loads((HERE / "golden" / "reference_runs.json").read_text())
+d = rc.digest
+
+
+@pytest.fixture(scope="module")
+def grids():
+    return rc.grid_cases()
+
+
+def _check(stage, got: dict, want: dict):
+    bad = [k for k in want if k in got and got[k] != want[k]]
+    assert not bad, f"{stage}: {bad} differ from the reference's run"
+
+
+@pytest.mark.parametrize("label", sorted(RUNS["grids"]))
+def test_gpu_reproduces_reference_run(gpu, grids, label):
+    want = RUNS["grids"][label]
+    case = grids[label][0]
+    if rc.case_digest(case) != want["input"]:
+        pytest.skip("the seeded generator gives other inputs on this machine than where the reference ran")
+    dc, ds = gpu.prepare_dev(case)
+    h = lambda t: t.cpu().numpy()  # noqa: E731
+    _check("set_nflag", {"nf": d(h(dc.nf)), "nfb": d(h(dc.nfb)), "f": d(h(dc.f)), "ifln": ds.ifln,
+                         "fln": d(h(ds.fln)[:ds.ifln]), "isfn": ds.isfn, "sfn": d(h(ds.sfn)[:ds.isfn])},
+           want["nflag"])
+    rows = ~rc.runs_mask(want["init"]["undefined_rows"], case.inne)
+    alu_c, ll_c, de_c = h(ds.alu_c), h(ds.ll_c), h(ds.de_c)
+    _check("init_matrix", {"nl": alu_c.shape[0], "mp": float(ds.mp.item()), "alu_c": d(alu_c[:, rows]),
+                           "ll_c": d(ll_c[:, rows]), "de_c": d(de_c[rows])}, want["init"])
+    n = ds.mnoe
+    _check("rows and RHS", {"mnoe": n, "mm2": ds.mm2, "dmax": ds.dmax, "mno": d(h(ds.mno).ravel()),
+                            "mno2mn": d(h(ds.mno2mn)[:n]), "b": d(h(ds.b)[:n])}, want["rows"])
+    _check("cal_matrix_element", {"alu": d(h(ds.alu)[:, :n]), "llu": d(h(ds.llu)[:, :n]),
+                                  "de": d(h(ds.de)[:n])}, want["asm"])
