@@ -23,10 +23,13 @@ the case data fill the module arrays in the bounds the reference allocates them
 with (0mod-arrays.F90:205-237, 290, 356-370); lf is the identity
 (main_2CLOWNS.F90:33) and dim3d follows main_2CLOWNS.F90:43-44.
 
-Only digests (sha256 of each output's bytes) and scalars are written: the cases
-are rebuilt from the seeded generator by tests/golden/reference_cases.py, and
-tests/test_oracle_reference_runs.py checks the oracle against these outputs bit
-for bit.  The reference is read from REFERENCE_ROOT (default /root/reference).
+Digests (sha256 of each output's bytes) and scalars are written to the JSON
+file, and the solution vectors (pressures, PCGPME_WILL's B) to
+tests/golden/reference_solutions.npz; the cases are rebuilt from the seeded
+generator by tests/golden/reference_cases.py.  tests/test_oracle_reference_runs.py
+checks the oracle against these outputs bit for bit, and
+tests/test_gpu_reference_runs.py the CUDA path (bit for bit, and the solves
+within their tolerance).  The reference is read from REFERENCE_ROOT (default /root/reference).
 
 Usage:  python tests/golden/make_ref_golden.py [REFERENCE_ROOT]
 """
@@ -129,9 +132,12 @@ def vals(a):
     return np.array(a.values())
 
 
-def run_grid(root, case, solve: bool, loop: bool) -> dict:
+SOLUTIONS = {}     # label/x (pressure) and label/b (PCGPME_WILL's B): values, for tolerance checks
+
+
+def run_grid(root, label, case, solve: bool, loop: bool) -> dict:
     d = rc.digest
-    out = {"input": rc.case_digest(case)}
+    out = {"input": rc.case_digest(case), "label": label}
     prog = program(root, GRID_SOURCES)
     V, A = load_grid(prog, case)
     prog.call("set_nflag")
@@ -162,8 +168,10 @@ def run_grid(root, case, solve: bool, loop: bool) -> dict:
                   "llu": d(vals(A.f_llu).reshape(nl, mm2)[:, :mnoe]), "de": d(vals(A.f_de)[:mnoe])}
     if solve:
         prog.call("cal_poisson_equation")
+        x = np.array(vals(A.f_xe)[1:mnoe + 1].tolist())
         out["solve"] = {"iter": V.f_iter, "eps": V.f_eps, "ier": prog.env["s_cal_poisson_equation"].f_ier,
-                        "x": d(vals(A.f_xe)[1:mnoe + 1])}
+                        "x": d(x)}
+        SOLUTIONS[f"{out['label']}/x"] = x
     if loop:
         prog = program(root, GRID_SOURCES)
         prog.fragment("cal_momentum", 41, 60, "ik_loop")
@@ -178,7 +186,7 @@ def run_grid(root, case, solve: bool, loop: bool) -> dict:
     return out
 
 
-def run_will(root, ds, eps) -> dict:
+def run_will(root, label, ds, eps) -> dict:
     prog = program(root, WILL_SOURCES)
     nl, na = ds.al.shape
     n = ds.n
@@ -187,7 +195,9 @@ def run_will(root, ds, eps) -> dict:
     dd = farray("real", ds.d[:n], [(1, n)])
     bb = farray("real", ds.b[:n], [(1, n)])
     prog.call("pcgpme_will", al, nl, na, ll, dd, n, 64, bb, float(eps), 5.0, 10000)
-    return {"input": rc.will_digest(ds), "b": rc.digest(vals(bb))}
+    b = vals(bb)
+    SOLUTIONS[f"{label}/b"] = b
+    return {"input": rc.will_digest(ds), "b": rc.digest(b)}
 
 
 def main(argv):
@@ -195,12 +205,14 @@ def main(argv):
     res = {"grids": {}, "will": {}}
     for label, (case, solve, loop) in rc.grid_cases().items():
         t = time.time()
-        res["grids"][label] = run_grid(root, case, solve, loop)
+        res["grids"][label] = run_grid(root, label, case, solve, loop)
+        del res["grids"][label]["label"]
         print(f"{label}: {time.time() - t:.1f} s", flush=True)
     for label, (ds, eps) in rc.will_cases().items():
-        res["will"][label] = run_will(root, ds, eps)
+        res["will"][label] = run_will(root, label, ds, eps)
         print(f"{label}: done", flush=True)
     (HERE / "reference_runs.json").write_text(json.dumps(res, indent=1, sort_keys=True) + "\n")
+    np.savez_compressed(HERE / "reference_solutions.npz", **SOLUTIONS)
 
 
 if __name__ == "__main__":

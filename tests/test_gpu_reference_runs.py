@@ -54,3 +54,46 @@ def test_gpu_reproduces_reference_run(gpu, grids, label):
                             "mno2mn": d(h(ds.mno2mn)[:n]), "b": d(h(ds.b)[:n])}, want["rows"])
     _check("cal_matrix_element", {"alu": d(h(ds.alu)[:, :n]), "llu": d(h(ds.llu)[:, :n]),
                                   "de": d(h(ds.de)[:n])}, want["asm"])
+
+
+SOL = np.load(HERE / "golden" / "reference_solutions.npz")
+
+
+@pytest.mark.parametrize("label", sorted(k for k, v in RUNS["grids"].items() if "solve" in v))
+def test_gpu_solve_matches_reference_solve(gpu, grids, label):
+    """The GPU's FP64 solve of the system it assembled against the reference's
+    PCGPME on the same system, both to the case's ERR <= eps: within 10 eps
+    relative L2 (the bound the oracle comparison measures at most 4.1 eps
+    against), iteration counts within a sixth (reduction order only)."""
+    import torch
+    want = RUNS["grids"][label]["solve"]
+    case = grids[label][0]
+    if rc.case_digest(case) != RUNS["grids"][label]["input"]:
+        pytest.skip("the seeded generator gives other inputs on this machine than where the reference ran")
+    dc, ds = gpu.prepare_dev(case)
+    n = ds.mnoe
+    x = torch.zeros(ds.mm2, dtype=torch.float64, device="cuda")
+    info = gpu.Solver(n).solve(ds.alu, ds.llu, ds.de, ds.b, x, eps=case.eps0)
+    xr = SOL[label + "/x"]
+    rel = float(np.linalg.norm(x.cpu().numpy()[:n] - xr) / np.linalg.norm(xr))
+    msg = (label, "rel", rel, "iters gpu/reference", info.iter, want["iter"])
+    assert info.ier == 0 and want["ier"] == 0, msg
+    assert rel <= 10 * case.eps0, msg
+    assert abs(info.iter - want["iter"]) <= max(3, want["iter"] // 6), msg
+
+
+@pytest.mark.parametrize("label", sorted(RUNS["will"]))
+def test_gpu_will_matches_reference_will(gpu, label):
+    """PCGPME_WILL on the GPU against the reference's, B after both
+    post-processings within 100 eps relative L2 (the bound of the oracle
+    comparison at eps = 1e-12)."""
+    import torch
+    ds, eps = rc.will_cases()[label]
+    if rc.will_digest(ds) != RUNS["will"][label]["input"]:
+        pytest.skip("the seeded generator gives other inputs on this machine than where the reference ran")
+    dev = lambda a: torch.from_numpy(np.ascontiguousarray(a)).to("cuda")  # noqa: E731
+    b = dev(ds.b)
+    info = gpu.WillSolver(ds.n).solve(dev(ds.al), dev(ds.ll), dev(ds.d), b, eps=eps)
+    br = SOL[label + "/b"]
+    rel = float(np.linalg.norm(b.cpu().numpy() - br) / np.linalg.norm(br))
+    assert info.ier == 0 and rel <= 100 * eps, (label, rel, info.as_dict())

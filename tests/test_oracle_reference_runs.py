@@ -99,3 +99,17 @@ def test_fixture_covers_every_stage():
     assert any(v["init"]["nl"] == 4 for v in g.values()) and any(v["init"]["nl"] == 6 for v in g.values())
     assert any(v["init"]["undefined_rows"] for v in g.values())
     assert len(RUNS["will"]) >= 3
+
+
+def test_stored_solutions_are_the_recorded_runs():
+    """reference_solutions.npz holds the very vectors whose digests the runs
+    recorded (the GPU solves are checked against these values)."""
+    sol = np.load(HERE / "golden" / "reference_solutions.npz")
+    xs = {k[:-2] for k in sol.files if k.endswith("/x")}
+    assert xs == {k for k, v in RUNS["grids"].items() if "solve" in v}
+    for k in xs:
+        assert d(sol[k + "/x"]) == RUNS["grids"][k]["solve"]["x"]
+    bs = {k[:-2] for k in sol.files if k.endswith("/b")}
+    assert bs == set(RUNS["will"])
+    for k in bs:
+        assert d(sol[k + "/b"]) == RUNS["will"][k]["b"]
