@@ -24,8 +24,8 @@ with (0mod-arrays.F90:205-237, 290, 356-370); lf is the identity
 (main_2CLOWNS.F90:33) and dim3d follows main_2CLOWNS.F90:43-44.
 
 Digests (sha256 of each output's bytes) and scalars are written to the JSON
-file, and the solution vectors (pressures, PCGPME_WILL's B) to
-tests/golden/reference_solutions.npz; the cases are rebuilt from the seeded
+file, and the solution vectors (pressures, PCGPME_WILL's B, the ik loop's
+pressure and face velocities) to tests/golden/reference_solutions.npz; the cases are rebuilt from the seeded
 generator by tests/golden/reference_cases.py.  tests/test_oracle_reference_runs.py
 checks the oracle against these outputs bit for bit, and
 tests/test_gpu_reference_runs.py the CUDA path (bit for bit, and the solves
@@ -181,8 +181,9 @@ def run_grid(root, label, case, solve: bool, loop: bool) -> dict:
         prog.call("init_matrix")
         allocate_matrix(prog, V, A)
         prog.call("ik_loop")
-        out["loop"] = {"ik": V.f_ik, "dmax": V.f_dmax, "p": d(vals(A.f_p)),
-                       "un": d(vals(A.f_un).reshape(-1, 3))}
+        pl, unl = vals(A.f_p), vals(A.f_un).reshape(-1, 3)
+        out["loop"] = {"ik": V.f_ik, "dmax": V.f_dmax, "p": d(pl), "un": d(unl)}
+        SOLUTIONS[f"{label}/p"], SOLUTIONS[f"{label}/un"] = pl, unl
     return out
 
 

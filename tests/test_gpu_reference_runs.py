@@ -97,3 +97,30 @@ def test_gpu_will_matches_reference_will(gpu, label):
     br = SOL[label + "/b"]
     rel = float(np.linalg.norm(b.cpu().numpy() - br) / np.linalg.norm(br))
     assert info.ier == 0 and rel <= 100 * eps, (label, rel, info.as_dict())
+
+
+@pytest.mark.parametrize("label", sorted(k for k, v in RUNS["grids"].items() if "loop" in v))
+def test_gpu_session_matches_reference_ik_loop(gpu, grids, label):
+    """The device-resident ik loop (clowns_session_*) against the reference's
+    own (1sub-momentum.F90:41-60) from the raw flags: the same classification
+    bit for bit, the same number of passes, and pressure and face velocities
+    within 1e-10 relative L2 -- each pass solves to ERR <= 1e-7, but the second
+    pass solves for the first one's error, so different reduction orders leave
+    about 1e-16 (measured between the oracle's serial and OpenMP solves)."""
+    want = RUNS["grids"][label]
+    case = grids[label][0]
+    if rc.case_digest(case) != want["input"]:
+        pytest.skip("the seeded generator gives other inputs on this machine than where the reference ran")
+    s = gpu.Session(case)
+    s.set_fields(case.nf, case.nfb, case.f, case.fb, case.a, case.un, case.sp, np.zeros(case.inne2 + 2))
+    ifln, isfn = s.classify()
+    out = s.pressure_loop(case.dt, d0=rc.LOOP_D0, eps0=rc.LOOP_EPS0)
+    got = s.fields()
+    s.close()
+    assert ifln == want["nflag"]["ifln"] and isfn == want["nflag"]["isfn"]
+    assert d(got["nf"]) == want["nflag"]["nf"] and d(got["nfb"]) == want["nflag"]["nfb"]
+    assert out["icon"] == 0 and out["ik"] == want["loop"]["ik"], (out, want["loop"])
+    pr, unr = SOL[label + "/p"], SOL[label + "/un"]
+    rp = float(np.linalg.norm(got["p"] - pr) / np.linalg.norm(pr))
+    ru = float(np.linalg.norm(got["un"].reshape(unr.shape) - unr) / np.linalg.norm(unr))
+    assert rp <= 1e-10 and ru <= 1e-10, (label, rp, ru)
