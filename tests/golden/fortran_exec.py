@@ -302,6 +302,28 @@ def _minloc1(x):
     return pos
 
 
+class _Obj:
+    """An element of a derived-type array: components as attributes f_<name>."""
+
+    def __init__(self, comps):
+        for c in comps:
+            setattr(self, "f_" + c, None)
+
+
+def _new_objs(a, comps):
+    a.d[a.off:a.off + a.size] = [_Obj(comps) for _ in range(a.size)]
+    return a
+
+
+def _asgn_comp(a, specs, comp, value):
+    offs, _ = _sec_offsets_ordered(a, specs)
+    vals = value.v if isinstance(value, AV) else [value] * len(offs)
+    if len(vals) != len(offs):
+        raise IndexError(f"assigning {len(vals)} values to {len(offs)} components")
+    for o, v in zip(offs, vals):
+        setattr(a.d[o], comp, v)
+
+
 def _temp_array(x, kind):
     """An array-valued expression passed to an array dummy: a temporary copy."""
     return FArray(list(x.v), 0, (1,), (len(x.v),), kind)
@@ -357,7 +379,7 @@ RUNTIME = {
     "_cons": _cons, "_minval": _minval, "_maxval": _maxval, "_idiv": _idiv, "_imod": _imod,
     "_isign": _isign, "_fmax": _fmax, "_fmin": _fmin, "_ubound": _ubound, "_lbound": _lbound,
     "_size": _size, "_sum": _sum, "_maxloc1": _maxloc1, "_minloc1": _minloc1,
-    "_temp_array": _temp_array, "FortranError": FortranError, "_Goto": _Goto, "_LoopCtl": _LoopCtl, "FortranStop": FortranStop, "math": math,
+    "_temp_array": _temp_array, "_new_objs": _new_objs, "_asgn_comp": _asgn_comp, "FortranError": FortranError, "_Goto": _Goto, "_LoopCtl": _LoopCtl, "FortranStop": FortranStop, "math": math,
 }
 
 
@@ -1508,9 +1530,19 @@ class Gen:
             return f"{arr}[{subs},]", sym.typ, None
         if isinstance(t, Comp):
             bc, bt, br = self.ex(t.base, ctx)
-            if br:
-                raise FortranError("assignment to an array of components")
             comps = self.types_of(ctx.unit)[bt[5:]]
+            if br:
+                base = t.base
+                if isinstance(base, Name):
+                    specs = "None"
+                elif isinstance(base, Ref):
+                    c, _, _ = self.ref(base, ctx)
+                    arr = self.py(base.name, *[ctx.vis[base.name][i] for i in (0, 2)])
+                    specs = c[len(f"_sec({arr}, "):-1]
+                else:
+                    raise FortranError("component assignment through an expression")
+                arr = self.py(base.name, *[ctx.vis[base.name][i] for i in (0, 2)])
+                return None, comps[t.comp], f"_asgn_comp({arr}, {specs}, 'f_{t.comp}', {{}})"
             return f"{bc}.f_{t.comp}", comps[t.comp], None
         raise FortranError(f"unsupported assignment target {t}")
 
@@ -1603,7 +1635,11 @@ class Gen:
                 lv = self.py(it.name, scope, owner)
                 if scope == "host":
                     ctx.nonlocal_.add(lv)
-                out.append(p + f"{lv} = FArray.new({kind!r}, ({', '.join(bnds)},))")
+                if sym.typ.startswith("type:"):
+                    comps = sorted(self.types_of(ctx.unit).get(sym.typ[5:], {}))
+                    out.append(p + f"{lv} = _new_objs(FArray.new('obj', ({', '.join(bnds)},)), {comps!r})")
+                else:
+                    out.append(p + f"{lv} = FArray.new({kind!r}, ({', '.join(bnds)},))")
         elif k == "bad":
             raise FortranError(s.a)
         elif k == "deallocate":
@@ -1797,6 +1833,12 @@ class Program:
                     uses=u.uses, contains=[], host=u.host, types=u.types)
         frag.body = body
         gen = Gen(self.procs, self.modules, self.undefined)
+        ns = Namespace()
+        self.env["s_" + frag.name] = ns
+        ctx = _Ctx(frag, gen.visible(frag))
+        for n, sym in frag.syms.items():
+            if sym.init is not None and sym.param is None and not sym.rank:
+                setattr(ns, "f_" + n, eval(gen.conv(*gen.ex(sym.init, ctx)[:2], sym.typ), self.env))
         out = []
         gen.unit(frag, 0, out)
         exec(compile("\n".join(out) + "\n", "<fortran-fragment>", "exec"), self.env)

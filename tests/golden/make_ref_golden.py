@@ -17,6 +17,8 @@ reference's own, chained as the model chains them:
   the ik loop            src2LOWNS/1sub-momentum.F90:41-60 (check_dmax 419-463, p -= xe,
                          estimate_velocity2 590-651, momentum_d math_func.F90:251-255)
   PCGPME_WILL            src2LOWNS/pcgpme_2DH.f90:1-373
+  read_data's numbering  src2LOWNS/data_io.F90:168-202 and 255-277 (the statements between the
+                         file reads, on flag grids; alloc_dxdydz 0mod-arrays.F90:196-216)
 
 The module constants come from the reference's module files (0mod-variables.F90);
 the case data fill the module arrays in the bounds the reference allocates them
@@ -187,6 +189,41 @@ def run_grid(root, label, case, solve: bool, loop: bool) -> dict:
     return out
 
 
+def run_numbering(root, dims, nf3, nfb3) -> dict:
+    """read_data's cell numbering (data_io.F90:168-202) and flag table
+    (255-277) -- the reference's statements, without its file reads -- on flag
+    grids over is-1:ie x js-1:je x ks-1:ke, after the allocation read_data
+    makes (alloc_dxdydz(is, js, ks, ie+2, je+2, ke+2), data_io.F90:111-112)."""
+    d = rc.digest
+    prog = program(root, GRID_SOURCES + ["src2LOWNS/data_io.F90"])
+    prog.fragment("read_data", 168, 202, "numbering")
+    prog.fragment("read_data", 255, 277, "cell_flags")
+    V, A = prog.module("variables"), prog.module("arrays")
+    is_, js, ks, ie, je, ke = (int(v) for v in dims)
+    V.f_is, V.f_js, V.f_ks, V.f_ie, V.f_je, V.f_ke = is_, js, ks, ie, je, ke
+    prog.call("alloc_dxdydz", is_, js, ks, ie + 2, je + 2, ke + 2)
+    bounds = [(is_ - 2, ie + 2), (ks - 2, ke + 2), (js - 2, je + 2)]
+    n = (ie - is_ + 5) * (ke - ks + 5) * (je - js + 5)
+    A.f_nf3, A.f_nfb3 = farray("int", [0] * n, bounds), farray("int", [0] * n, bounds)
+    for j in range(js - 1, je + 1):
+        for k in range(ks - 1, ke + 1):
+            for i in range(is_ - 1, ie + 1):
+                g = (j - (js - 1), k - (ks - 1), i - (is_ - 1))
+                A.f_nf3[i, k, j] = int(nf3[g])
+                A.f_nfb3[i, k, j] = int(nfb3[g])
+    prog.call("numbering")
+    inne, inne2 = V.f_inne, V.f_inne2
+    region = ((is_ - 1, ie, None), (ks - 1, ke, None), (js - 1, je, None))
+    out = {"inne": inne, "inne2": inne2, "mn": d(vals(A.f_mn)),
+           "in": d(vals(A.f_in)[:inne2]), "jn": d(vals(A.f_jn)[:inne2]), "kn": d(vals(A.f_kn)[:inne2]),
+           "nfb3": d(np.array(fx._sec(A.f_nfb3, region).v))}
+    prog.call("cell_flags")
+    nff = A.f_nff.values()[:inne2 + 2]
+    out.update({"nf": d(np.array([o.f_f for o in nff])), "nfb": d(np.array([o.f_b for o in nff])),
+                "mn_flags": d(vals(A.f_mn))})
+    return out
+
+
 def run_will(root, label, ds, eps) -> dict:
     prog = program(root, WILL_SOURCES)
     nl, na = ds.al.shape
@@ -203,7 +240,11 @@ def run_will(root, label, ds, eps) -> dict:
 
 def main(argv):
     root = pathlib.Path(argv[1] if len(argv) > 1 else "/root/reference")
-    res = {"grids": {}, "will": {}}
+    res = {"grids": {}, "will": {}, "numbering": {}}
+    for label, (dims, nf3, nfb3) in rc.numbering_cases().items():
+        res["numbering"][label] = dict(run_numbering(root, dims, nf3, nfb3),
+                                       input=rc.digest(np.concatenate([np.ravel(dims), np.ravel(nf3),
+                                                                       np.ravel(nfb3)])))
     for label, (case, solve, loop) in rc.grid_cases().items():
         t = time.time()
         res["grids"][label] = run_grid(root, label, case, solve, loop)

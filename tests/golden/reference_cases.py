@@ -104,6 +104,26 @@ def will_cases():
     }
 
 
+def numbering_cases():
+    """label -> (dims, nf3, nfb3): flag grids over is-1:ie x js-1:je x ks-1:ke
+    ([j][k][i]) for read_data's numbering -- those of every grid case (the
+    ingested flume carries wave-boundary, side-wall, obstacle-surface and lid
+    codes) and seeded random grids that take every branch."""
+    ing = ge.load_package().ingest
+    out = {}
+    for label, (c, _, _) in grid_cases().items():
+        nf3, nfb3 = ing.flag_grids(c)
+        out[label] = (np.asarray(c.dims), nf3, nfb3)
+    rng = np.random.default_rng(77)
+    for k, (nx, ny, nz) in enumerate([(10, 8, 6), (7, 1, 9), (1, 9, 7)]):
+        dims = np.array([3, 3, 3, 3 + nx, 3 + ny, 3 + nz], dtype=np.int32)
+        shape = (ny + 2, nz + 2, nx + 2)
+        nf3 = rng.choice(np.array([-1, 0, 1, 2], dtype=np.int32), size=shape, p=[0.35, 0.2, 0.35, 0.1])
+        nfb3 = rng.choice(np.array([0, 1, 2, 4, 5, 199, 200, 300, -1], dtype=np.int32), size=shape)
+        out[f"random{k}_{nx}x{ny}x{nz}"] = (dims, nf3.astype(np.int32), nfb3.astype(np.int32))
+    return out
+
+
 LOOP_D0, LOOP_EPS0 = 1e-9, 1e-7          # two or more ik passes on the small grids
 
 

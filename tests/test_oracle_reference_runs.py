@@ -118,3 +118,22 @@ def test_stored_solutions_are_the_recorded_runs():
     assert bs == set(RUNS["will"])
     for k in bs:
         assert d(sol[k + "/b"]) == RUNS["will"][k]["b"]
+
+
+@pytest.mark.parametrize("label", sorted(RUNS["numbering"]))
+def test_ingest_numbering_reproduces_reference_read_data(label):
+    """The case reader's cell numbering and flag table (2clowns-3d_gb300/ingest.py)
+    against read_data's own statements (data_io.F90:168-202, 255-277) on the same
+    flag grids: bit for bit."""
+    import __graft_entry__ as ge
+    ing = ge.load_package().ingest
+    want = RUNS["numbering"][label]
+    dims, nf3, nfb3 = rc.numbering_cases()[label]
+    assert d(np.concatenate([np.ravel(dims), np.ravel(nf3), np.ravel(nfb3)])) == want["input"]
+    nb = ing.number_cells(dims, nf3, nfb3)
+    nf, nfb, mn = ing.cell_flags(dims, nf3, nb.nfb3, nb)
+    m = nb.inne2
+    flat = lambda a: d(np.ravel(a))  # noqa: E731
+    _check("read_data numbering", {"inne": nb.inne, "inne2": m, "mn": flat(nb.mn), "in": flat(nb.in_[1:m + 1]),
+                                   "jn": flat(nb.jn[1:m + 1]), "kn": flat(nb.kn[1:m + 1]), "nfb3": flat(nb.nfb3),
+                                   "nf": flat(nf), "nfb": flat(nfb), "mn_flags": flat(mn)}, want)
