@@ -329,6 +329,34 @@ def _temp_array(x, kind):
     return FArray(list(x.v), 0, (1,), (len(x.v),), kind)
 
 
+def _rpowi(x, n):
+    """REAL ** INTEGER as compilers expand it: binary powering by products, the
+    reciprocal for a negative exponent."""
+    if n < 0:
+        return 1.0 / _rpowi(x, -n)
+    r, b = 1.0, x
+    first = True
+    while n:
+        if n & 1:
+            r = b if first else r * b
+            first = False
+        n >>= 1
+        if n:
+            b = b * b
+    return r
+
+
+def _nint(x):
+    """NINT: the nearest integer, halves away from zero."""
+    t = math.trunc(x)
+    f = x - t
+    if f >= 0.5:
+        return t + 1
+    if f <= -0.5:
+        return t - 1
+    return t
+
+
 def _idiv(a, b):
     q = abs(a) // abs(b)
     return q if (a >= 0) == (b > 0) else -q
@@ -379,7 +407,7 @@ RUNTIME = {
     "_cons": _cons, "_minval": _minval, "_maxval": _maxval, "_idiv": _idiv, "_imod": _imod,
     "_isign": _isign, "_fmax": _fmax, "_fmin": _fmin, "_ubound": _ubound, "_lbound": _lbound,
     "_size": _size, "_sum": _sum, "_maxloc1": _maxloc1, "_minloc1": _minloc1,
-    "_temp_array": _temp_array, "_new_objs": _new_objs, "_asgn_comp": _asgn_comp, "FortranError": FortranError, "_Goto": _Goto, "_LoopCtl": _LoopCtl, "FortranStop": FortranStop, "math": math,
+    "_temp_array": _temp_array, "_rpowi": _rpowi, "_nint": _nint, "_new_objs": _new_objs, "_asgn_comp": _asgn_comp, "FortranError": FortranError, "_Goto": _Goto, "_LoopCtl": _LoopCtl, "FortranStop": FortranStop, "math": math,
 }
 
 
@@ -1051,9 +1079,12 @@ def parse_source(text: str, defines: set[str]) -> list[Unit]:
             if m:
                 label, s = int(m.group(1)), m.group(2)
             sl = s.lower()
-            if is_stop(re.sub(r"\s+", " ", sl), stops):
+            head = re.sub(r"\s+", " ", sl)
+            if is_stop(head, stops):
                 if label is not None:
-                    raise FortranError(f"line {no}: labelled block end")
+                    if not re.match(r"^end ?do( \w+)?$", head):
+                        raise FortranError(f"line {no}: labelled block end")
+                    body.append(St("continue", no, label))   # a labelled END DO ends the iteration
                 return body, pos
             st, pos = parse_stmt(pos, no, s, sl, label)
             if st is not None:
@@ -1301,7 +1332,13 @@ class Gen:
         if e.op == "/" and t == "int":
             f = "_idiv({0}, {1})"
         elif e.op == "**":
-            f = "({0} ** {1})" if t == "int" else "math.pow({0}, {1})"
+            if t == "int":
+                f = "({0} ** {1})"
+            elif rt == "int":
+                f = "_rpowi({0}, {1})"
+                b = rc                          # the integer exponent stays an integer
+            else:
+                f = "math.pow({0}, {1})"
         else:
             f = "({0} " + e.op + " {1})"
         if rank:
@@ -1352,8 +1389,7 @@ class Gen:
         if name == "int":
             return f"int({vals[0][0]})", "int", 0
         if name == "nint":
-            return f"int(math.floor({vals[0][0]} + 0.5) if {vals[0][0]} >= 0 else -math.floor(-{vals[0][0]} + 0.5))", \
-                "int", 0
+            return f"_nint({vals[0][0]})", "int", 0
         if name in ("max", "min", "dmax1", "dmin1", "max0", "min0"):
             t = "real" if any(v[1] == "real" for v in vals) else "int"
             f = "_fmax" if "max" in name else "_fmin"

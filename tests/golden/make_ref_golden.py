@@ -19,6 +19,7 @@ reference's own, chained as the model chains them:
   PCGPME_WILL            src2LOWNS/pcgpme_2DH.f90:1-373
   read_data's numbering  src2LOWNS/data_io.F90:168-202 and 255-277 (the statements between the
                          file reads, on flag grids; alloc_dxdydz 0mod-arrays.F90:196-216)
+  set_dx                 src2LOWNS/1sub-main.F90:53-74 (round lib/src/xy_calc.f90:100-112)
 
 The module constants come from the reference's module files (0mod-variables.F90);
 the case data fill the module arrays in the bounds the reference allocates them
@@ -54,7 +55,7 @@ DEFINES = {"RAN", "NORMAL", "OBJECT", "SLIDE0"}
 GRID_SOURCES = ["src2LOWNS/0mod-type_interface.F90", "src2LOWNS/0mod-variables.F90",
                 "src2LOWNS/0mod-arrays.F90", "src2LOWNS/nfd2015.F90", "src2LOWNS/1sub-matrix.F90",
                 "src2LOWNS/1sub-momentum.F90", "src2LOWNS/1sub-main.F90", "lib/src/math_func.F90",
-                "src2LOWNS/pcgpme_para.F90"]
+                "lib/src/xy_calc.f90", "src2LOWNS/pcgpme_para.F90"]
 WILL_SOURCES = ["src2LOWNS/0mod-type_interface.F90", "src2LOWNS/0mod-variables.F90",
                 "src2LOWNS/pcgpme_2DH.f90"]
 # cal_err_of_continuity reads its local k, set only by the numbering branch of
@@ -224,6 +225,25 @@ def run_numbering(root, dims, nf3, nfb3) -> dict:
     return out
 
 
+def run_set_dx(root, dims, x) -> dict:
+    """set_dx (1sub-main.F90:53-74, round lib/src/xy_calc.f90:100-112) on the
+    coordinates x(0:2, 1:mx2) after read_data's allocation (alloc_dxdydz)."""
+    prog = program(root, GRID_SOURCES)
+    V, A = prog.module("variables"), prog.module("arrays")
+    is_, js, ks, ie, je, ke = (int(v) for v in dims)
+    prog.call("alloc_dxdydz", is_, js, ks, ie + 2, je + 2, ke + 2)
+    mx2 = A.f_x.ext[1]
+    if x.shape[0] > mx2:
+        raise ValueError(f"coordinates for {x.shape[0]} cells, x(0:2, {mx2}) allocated")
+    xx = np.zeros((mx2, 3))
+    xx[:x.shape[0]] = x
+    A.f_x = farray("real", xx.ravel(), [(0, 2), (1, mx2)])
+    A.f_ls = farray("int", [is_, js, ks], [(0, 2)])
+    A.f_le = farray("int", [ie, je, ke], [(0, 2)])
+    prog.call("set_dx")
+    return {"mx2": mx2, "x": rc.digest(vals(A.f_x)), "dx": rc.digest(vals(A.f_dx))}
+
+
 def run_will(root, label, ds, eps) -> dict:
     prog = program(root, WILL_SOURCES)
     nl, na = ds.al.shape
@@ -240,7 +260,10 @@ def run_will(root, label, ds, eps) -> dict:
 
 def main(argv):
     root = pathlib.Path(argv[1] if len(argv) > 1 else "/root/reference")
-    res = {"grids": {}, "will": {}, "numbering": {}}
+    res = {"grids": {}, "will": {}, "numbering": {}, "set_dx": {}}
+    for label, (dims, x) in rc.spacing_cases().items():
+        res["set_dx"][label] = dict(run_set_dx(root, dims, x),
+                                    input=rc.digest(np.concatenate([np.ravel(dims), np.ravel(x)])))
     for label, (dims, nf3, nfb3) in rc.numbering_cases().items():
         res["numbering"][label] = dict(run_numbering(root, dims, nf3, nfb3),
                                        input=rc.digest(np.concatenate([np.ravel(dims), np.ravel(nf3),

@@ -124,6 +124,27 @@ def numbering_cases():
     return out
 
 
+def spacing_cases():
+    """label -> (dims, x (mx2, 3), x(l, i) at [i-1, l]): coordinates for set_dx --
+    those of the grid cases, and variants with the last coordinate of an axis
+    missing (0, extrapolated) and spacings from 5e-5 to 50 (the decimal guess)."""
+    out = {}
+    grids = grid_cases()
+    for label in ("tank_6x5x6", "beach_10x6x8", "flume2dv_16x1x8", "section2dv_1x14x8", "bore_40x24x32",
+                  "flume_40x24x20_ingested"):
+        c = grids[label][0]
+        out[label] = (np.asarray(c.dims), np.array(c.x))
+    c = grids["beach_10x6x8"][0]
+    le = [int(v) for v in c.dims[3:]]
+    for scale in (1e3, 2.5e-2, 1e-3):
+        out[f"beach_10x6x8_x{scale:g}"] = (np.asarray(c.dims), np.round(np.array(c.x) * scale / QUANTUM) * QUANTUM)
+    x = np.array(c.x)
+    x[le[0], 0] = 0.0                            # x(0, le(0)+1) missing
+    x[le[2], 2] = 0.0
+    out["beach_10x6x8_open_end"] = (np.asarray(c.dims), x)
+    return out
+
+
 LOOP_D0, LOOP_EPS0 = 1e-9, 1e-7          # two or more ik passes on the small grids
 
 

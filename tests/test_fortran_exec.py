@@ -279,3 +279,28 @@ end subroutine
     assert "io" in p.untranslated and p.call("fine", 1) == (2,)
     with pytest.raises(fx.FortranError):
         p.call("io")
+
+
+def test_integer_powers_nint_and_labelled_end_do():
+    p = prog("""
+subroutine misc(n, a, b, c, d, s)
+    implicit none
+    integer :: n, c, d, s, k, j
+    real*8 :: a, b
+    a = 10d0**n
+    b = 10d0**(-n)
+    c = nint(2.5d0)
+    d = nint(-2.5d0)
+    s = 0
+    do k = 1, 4
+        do j = 1, 3
+            if (j.eq.k) goto 400
+            s = s + 1
+400     end do
+    end do
+end subroutine
+""")
+    r = p.call("misc", 6, 0.0, 0.0, 0, 0, 0)
+    assert r[1] == 1e6 and r[2] == 1.0 / 1e6          # a product, a reciprocal of a product
+    assert r[3] == 3 and r[4] == -3                    # halves away from zero
+    assert r[5] == 9                                   # 12 pairs less the 3 with j == k

@@ -137,3 +137,18 @@ def test_ingest_numbering_reproduces_reference_read_data(label):
     _check("read_data numbering", {"inne": nb.inne, "inne2": m, "mn": flat(nb.mn), "in": flat(nb.in_[1:m + 1]),
                                    "jn": flat(nb.jn[1:m + 1]), "kn": flat(nb.kn[1:m + 1]), "nfb3": flat(nb.nfb3),
                                    "nf": flat(nf), "nfb": flat(nfb), "mn_flags": flat(mn)}, want)
+
+
+@pytest.mark.parametrize("label", sorted(RUNS["set_dx"]))
+def test_ingest_set_dx_reproduces_reference_set_dx(label):
+    """The case reader's spacings (ingest.set_dx) against the reference's set_dx
+    and round (1sub-main.F90:53-74, lib/src/xy_calc.f90:100-112): bit for bit."""
+    import __graft_entry__ as ge
+    ing = ge.load_package().ingest
+    want = RUNS["set_dx"][label]
+    dims, x = rc.spacing_cases()[label]
+    assert d(np.concatenate([np.ravel(dims), np.ravel(x)])) == want["input"]
+    xx = np.zeros((want["mx2"], 3))
+    xx[:x.shape[0]] = x
+    xo, dxo = ing.set_dx(dims, xx)
+    assert d(np.ravel(xo)) == want["x"] and d(np.ravel(dxo)) == want["dx"]
