@@ -33,6 +33,7 @@ from __future__ import annotations
 
 import math
 import re
+import struct
 from dataclasses import dataclass, field
 
 
@@ -357,6 +358,147 @@ def _nint(x):
     return t
 
 
+def _strfix(v, n):
+    """A CHARACTER value stored in a variable of length n: cut or blank-padded."""
+    return v if n is None else v[:n].ljust(n)
+
+
+def _substr(v, lo, hi):
+    lo = 1 if lo is None else lo
+    hi = len(v) if hi is None else hi
+    if lo < 1 or hi > len(v):
+        raise IndexError(f"substring ({lo}:{hi}) of a string of length {len(v)}")
+    return v[lo - 1:hi]
+
+
+def _strcmp(a, b):
+    """Character comparison with the shorter operand padded with blanks."""
+    n = max(len(a), len(b))
+    a, b = a.ljust(n), b.ljust(n)
+    return (a > b) - (a < b)
+
+
+class _IOError(Exception):
+    """A failed OPEN or READ (code > 0) or an end of file (code < 0)."""
+
+    def __init__(self, code, msg):
+        super().__init__(msg)
+        self.code = code
+
+
+class _Record:
+    """Reads one unformatted record's values in order (big-endian)."""
+
+    def __init__(self, data: bytes):
+        self.b, self.p = data, 0
+
+    def _take(self, n):
+        if self.p + n > len(self.b):
+            raise _IOError(2, f"input record of {len(self.b)} bytes too short")
+        v = self.b[self.p:self.p + n]
+        self.p += n
+        return v
+
+    def int(self):
+        return struct.unpack(">i", self._take(4))[0]
+
+    def real(self):
+        return struct.unpack(">d", self._take(8))[0]
+
+    def logical(self):
+        return struct.unpack(">i", self._take(4))[0] != 0
+
+    def char(self, n):
+        return self._take(n).decode("latin-1")
+
+
+class _RecordOut:
+    def __init__(self):
+        self.parts = []
+
+    def int(self, v):
+        self.parts.append(struct.pack(">i", int(v)))
+
+    def real(self, v):
+        self.parts.append(struct.pack(">d", float(v)))
+
+    def logical(self, v):
+        self.parts.append(struct.pack(">i", 1 if v else 0))
+
+    def char(self, v, n=None):
+        v = v if n is None else _strfix(v, n)
+        self.parts.append(v.encode("latin-1"))
+
+    def data(self):
+        return b"".join(self.parts)
+
+
+class FortranFiles:
+    """Unformatted sequential files in memory: name -> bytes, each record framed
+    by big-endian 4-byte lengths (a negative head marks a record continued in
+    the next subrecord)."""
+
+    def __init__(self, files=None):
+        self.files = dict(files or {})
+        self.units = {}
+
+    @staticmethod
+    def records(data: bytes):
+        out, p, cur = [], 0, b""
+        while p < len(data):
+            (n,) = struct.unpack_from(">i", data, p)
+            m = abs(n)
+            cur += data[p + 4:p + 4 + m]
+            p += 8 + m
+            if n >= 0:
+                out.append(cur)
+                cur = b""
+        return out
+
+    def open(self, unit, name, status="unknown", form="formatted"):
+        name = name.strip()
+        if not form.strip().lower().startswith("unformatted"):
+            raise FortranError(f"formatted OPEN of {name}")
+        st = status.strip().lower()
+        if st == "old" and name not in self.files:
+            raise _IOError(29, f"no file {name}")
+        recs = self.records(self.files[name]) if name in self.files and st != "replace" else []
+        self.units[unit] = {"name": name, "recs": recs, "pos": 0, "out": None}
+
+    def read(self, unit):
+        u = self.units.get(unit)
+        if u is None:
+            raise _IOError(29, f"unit {unit} is not open")
+        if u["pos"] >= len(u["recs"]):
+            raise _IOError(-1, f"end of file {u['name']}")
+        u["pos"] += 1
+        return _Record(u["recs"][u["pos"] - 1])
+
+    def write(self, unit, data: bytes):
+        u = self.units[unit]
+        if u["out"] is None:
+            u["out"] = u["recs"][:u["pos"]]
+        u["out"].append(data)
+
+    def close(self, unit):
+        u = self.units.pop(unit, None)
+        if u is not None and u["out"] is not None:
+            self.files[u["name"]] = b"".join(struct.pack(">i", len(r)) + r + struct.pack(">i", len(r))
+                                             for r in u["out"])
+
+
+def _read_into(a, specs, rec, kind, clen=None):
+    offs, _ = _sec_offsets_ordered(a, specs)
+    for o in offs:
+        a.d[o] = rec.char(clen) if kind == "char" else getattr(rec, kind)()
+
+
+def _write_from(w, a, specs, kind):
+    offs, _ = _sec_offsets_ordered(a, specs)
+    for o in offs:
+        getattr(w, kind)(a.d[o])
+
+
 def _idiv(a, b):
     q = abs(a) // abs(b)
     return q if (a >= 0) == (b > 0) else -q
@@ -407,7 +549,8 @@ RUNTIME = {
     "_cons": _cons, "_minval": _minval, "_maxval": _maxval, "_idiv": _idiv, "_imod": _imod,
     "_isign": _isign, "_fmax": _fmax, "_fmin": _fmin, "_ubound": _ubound, "_lbound": _lbound,
     "_size": _size, "_sum": _sum, "_maxloc1": _maxloc1, "_minloc1": _minloc1,
-    "_temp_array": _temp_array, "_rpowi": _rpowi, "_nint": _nint, "_new_objs": _new_objs, "_asgn_comp": _asgn_comp, "FortranError": FortranError, "_Goto": _Goto, "_LoopCtl": _LoopCtl, "FortranStop": FortranStop, "math": math,
+    "_temp_array": _temp_array, "_IOError": _IOError, "_RecordOut": _RecordOut, "_read_into": _read_into,
+    "_write_from": _write_from, "FortranFiles": FortranFiles, "_strfix": _strfix, "_substr": _substr, "_strcmp": _strcmp, "_rpowi": _rpowi, "_nint": _nint, "_new_objs": _new_objs, "_asgn_comp": _asgn_comp, "FortranError": FortranError, "_Goto": _Goto, "_LoopCtl": _LoopCtl, "FortranStop": FortranStop, "math": math,
 }
 
 
@@ -473,6 +616,34 @@ def preprocess(text: str, defines: set[str]) -> list[str]:
     if stack:
         raise FortranError("unterminated #if")
     return out
+
+
+def fixed_to_free(text: str) -> str:
+    """Fixed-form source (comment lines with C, c, * or ! in column 1, labels
+    in columns 1-5, continuation marks in column 6, statements in columns
+    7-72) as free-form lines."""
+    out = []
+    for raw in text.replace("\r\n", "\n").split("\n"):
+        line = raw.expandtabs(6)
+        if line.startswith("#"):                 # preprocessor directives pass through
+            out.append(line)
+            continue
+        if not line.strip() or line[0] in "Cc*!":
+            out.append("")
+            continue
+        body = line[6:72]
+        if len(line) > 5 and line[5] not in " 0":
+            k = len(out) - 1
+            while k >= 0 and not out[k]:
+                k -= 1
+            if k < 0:
+                raise FortranError("continuation line without a statement")
+            out[k] = out[k] + " &"
+            out.append("&" + body)
+            continue
+        label = line[:5].strip()
+        out.append((label + " " if label else "") + body)
+    return "\n".join(out)
 
 
 def _strip_comment(line: str) -> str:
@@ -677,10 +848,17 @@ class Parser:
         return self.rel()
 
     def rel(self):
-        x = self.add()
+        x = self.concat()
         if self.peek()[1] in self._REL:
             op = self._REL[self.take()[1]]
-            x = Bin(op, x, self.add())
+            x = Bin(op, x, self.concat())
+        return x
+
+    def concat(self):
+        x = self.add()
+        while self.peek()[1] == "//":
+            self.take()
+            x = Bin("//", x, self.add())
         return x
 
     def add(self):
@@ -788,6 +966,34 @@ class Parser:
 
 
 @dataclass
+class IDo:
+    """Implied-DO list of an I/O statement: (items, var = lo, hi[, step])."""
+    items: list
+    var: str
+    lo: object
+    hi: object
+    step: object
+
+
+def io_items(text: str) -> list:
+    out = []
+    for part in _split_top(text):
+        if not part:
+            continue
+        if part.startswith("(") and _match_paren(part, 0) == len(part) - 1:
+            inner = _split_top(part[1:-1])
+            k = next((i for i, q in enumerate(inner) if re.match(r"^\w+\s*=(?!=)", q)), None)
+            if k is not None:
+                var, lo = inner[k].split("=", 1)
+                rest = inner[k + 1:]
+                out.append(IDo(io_items(",".join(inner[:k])), var.strip().lower(), px(lo), px(rest[0]),
+                               px(rest[1]) if len(rest) > 1 else None))
+                continue
+        out.append(px(part))
+    return out
+
+
+@dataclass
 class BadExpr:
     msg: str
 
@@ -823,6 +1029,7 @@ class Sym:
     init: object = None
     is_arg: bool = False
     allocatable: bool = False
+    clen: object = None         # CHARACTER length (int), None when assumed or not character
 
     @property
     def rank(self):
@@ -843,6 +1050,7 @@ class Unit:
     host: "Unit | None" = None
     types: dict = field(default_factory=dict)  # derived type -> {component: typ}
     bad: str | None = None                     # why the unit cannot be translated
+    implicit_none: bool = False
 
 
 @dataclass
@@ -931,6 +1139,11 @@ def _dims(spec: str):
 def parse_decl(stmt: str, unit: Unit):
     m = _TYPE_RE.match(stmt)
     typ = _base_type(m.group(1))
+    clen = None
+    if typ == "char":
+        ml = re.match(r"character\s*(?:\*\s*(\d+)|\(\s*(?:len\s*=\s*)?(\d+)\s*\))", m.group(1), re.I)
+        if ml:
+            clen = int(ml.group(1) or ml.group(2))
     rest = stmt[m.end():].strip()
     if "::" in rest:
         attrs_s, ents_s = rest.split("::", 1)
@@ -960,13 +1173,16 @@ def parse_decl(stmt: str, unit: Unit):
             ent, init_s = ent.split("=", 1)
             init = parse_expr(init_s)
         ent = ent.strip()
-        edims = dims
+        edims, elen = dims, clen
+        ml = re.match(r"(\w+)\s*\*\s*(\d+)$", ent)
+        if ml and typ == "char":
+            ent, elen = ml.group(1), int(ml.group(2))
         mm = re.match(r"(\w+)\s*\((.*)\)$", ent)
         if mm:
             ent, edims = mm.group(1), _dims(mm.group(2))
         name = ent.lower()
         sym = unit.syms.get(name) or Sym(name, typ)
-        sym.typ, sym.dims, sym.intent, sym.allocatable = typ, edims, intent, alloc
+        sym.typ, sym.dims, sym.intent, sym.allocatable, sym.clen = typ, edims, intent, alloc, elen
         if param:
             sym.param = init
         else:
@@ -1030,7 +1246,10 @@ def parse_source(text: str, defines: set[str]) -> list[Unit]:
                 only = [x.strip() for x in m.group(2).split(",")] if m.group(2) else None
                 u.uses.append((m.group(1), only))
             elif sl.startswith("implicit"):
-                pass
+                if re.sub(r"\s+", " ", sl) == "implicit none":
+                    u.implicit_none = True
+                else:
+                    u.bad = u.bad or f"line {no}: IMPLICIT with type rules"
             elif re.match(r"^interface\b", sl):
                 while not re.match(r"^end\s*interface", lines[pos][1].lower()):
                     pos += 1
@@ -1070,7 +1289,7 @@ def parse_source(text: str, defines: set[str]) -> list[Unit]:
                 return True
         return False
 
-    def parse_block(pos, stops):
+    def parse_block(pos, stops, end_label=None):
         body = []
         while pos < len(lines):
             no, s = lines[pos]
@@ -1089,6 +1308,8 @@ def parse_source(text: str, defines: set[str]) -> list[Unit]:
             st, pos = parse_stmt(pos, no, s, sl, label)
             if st is not None:
                 body.append(st)
+            if end_label is not None and label == end_label:
+                return body, pos
         raise FortranError("unexpected end of file")
 
     def parse_stmt(pos, no, s, sl, label):
@@ -1122,6 +1343,13 @@ def parse_source(text: str, defines: set[str]) -> list[Unit]:
                     raise FortranError(f"line {n2}: unexpected {s2}")
             inner, _ = parse_stmt(pos, no, tail, tail.lower(), None)
             return St("if", no, label, a=[(cond, [inner])]), pos + 1
+        m = re.match(r"^do\s+(\d+)\s*,?\s*(\w+)\s*=\s*(.*)$", sl)
+        if m:                                   # DO with a terminal label (the labelled statement ends the body)
+            parts = _split_top(s[s.index("=") + 1:])
+            start, end = px(parts[0]), px(parts[1])
+            step = px(parts[2]) if len(parts) > 2 else None
+            body, pos = parse_block(pos + 1, (), end_label=int(m.group(1)))
+            return St("do", no, label, a=m.group(2), b=start, c=end, d=step, body=body), pos
         m = re.match(r"^do\s+(\w+)\s*=\s*(.*)$", sl)
         if m:
             parts = _split_top(s[s.index("=") + 1:])
@@ -1147,7 +1375,41 @@ def parse_source(text: str, defines: set[str]) -> list[Unit]:
             raise FortranError(f"line {no}: CYCLE/EXIT with a construct name")
         if sl.startswith("stop"):
             return St("stop", no, label, a=s[4:].strip()), pos + 1
-        if re.match(r"^(write|print|format|call\s+flush)\b", sl) or re.match(r"^(write|format)\s*\(", sl):
+        m = re.match(r"^(read|write|open|close)\s*\(", sl)
+        if m:
+            k = s.index("(")
+            j = _match_paren(s, k)
+            pos_args, kw = [], {}
+            for c in _split_top(s[k + 1:j]):
+                mk = re.match(r"^(\w+)\s*=(?!=)\s*(.*)$", c)
+                if mk:
+                    kw[mk.group(1).lower()] = mk.group(2).strip()
+                else:
+                    pos_args.append(c.strip())
+            unit = pos_args[0] if pos_args else kw.get("unit")
+            fmt = pos_args[1] if len(pos_args) > 1 else kw.get("fmt")
+            kind = m.group(1)
+            if unit is None:
+                return St("bad", no, label, a=f"line {no}: {kind} without a unit"), pos + 1
+            if kind == "write" and (unit in ("6", "*") or fmt is not None):
+                return St("noop", no, label), pos + 1            # formatted output: not reproduced
+            if kind in ("read", "write") and (unit == "*" or fmt is not None):
+                return St("bad", no, label, a=f"line {no}: formatted {kind}"), pos + 1
+            ctl = {"unit": px(unit)}
+            for key in ("file", "status", "form", "iostat"):
+                if key in kw:
+                    ctl[key] = px(kw[key])
+            for key in ("err", "end"):
+                if key in kw:
+                    if not kw[key].isdigit():
+                        return St("bad", no, label, a=f"line {no}: {key}= {kw[key]}"), pos + 1
+                    ctl[key] = int(kw[key])
+            try:
+                items = io_items(s[j + 1:].strip()) if kind in ("read", "write") else []
+            except FortranError as e:
+                return St("bad", no, label, a=f"line {no}: {e}"), pos + 1
+            return St(kind, no, label, a=ctl, b=items), pos + 1
+        if re.match(r"^(print|format|call\s+flush)\b", sl) or re.match(r"^format\s*\(", sl):
             return St("noop", no, label), pos + 1
         m = re.match(r"^call\s+(\w+)\s*(\(.*\))?$", sl)
         if m:
@@ -1194,7 +1456,7 @@ INTRINSIC_TYPES = {
     "max0": "int", "min0": "int", "mod": "arg", "sign": "arg", "isnan": "logical", "minval": "arg",
     "maxval": "arg", "ubound": "int", "lbound": "int", "size": "int", "omp_get_num_threads": "int",
     "omp_get_thread_num": "int", "omp_get_max_threads": "int", "huge": "arg", "sum": "arg", "maxloc": "int",
-    "minloc": "int",
+    "minloc": "int", "len": "int", "len_trim": "int", "trim": "char", "index": "int",
 }
 
 
@@ -1322,6 +1584,14 @@ class Gen:
             if rank:
                 return f"_ew(lambda a, b: a {e.op} b, {lc}, {rc})", "logical", rank
             return f"({lc} {e.op} {rc})", "logical", 0
+        if e.op == "//":
+            if rank or lt != "char" or rt != "char":
+                raise FortranError("concatenation of non-character operands")
+            return f"({lc} + {rc})", "char", 0
+        if e.op in ("==", "!=", "<", "<=", ">", ">=") and "char" in (lt, rt):
+            if rank:
+                raise FortranError("character array comparison")
+            return f"(_strcmp({lc}, {rc}) {e.op} 0)", "logical", 0
         if e.op in ("==", "!=", "<", "<=", ">", ">="):
             if rank:
                 return f"_ew(lambda a, b: a {e.op} b, {lc}, {rc})", "logical", rank
@@ -1369,7 +1639,12 @@ class Gen:
                 return f"{arr}.g{len(subs)}({', '.join(c for c, _, _ in subs)})", sym.typ, 0
             return f"{arr}[{', '.join(c for c, _, _ in subs)},]", sym.typ, 0
         if v is not None and v[1].typ == "char":
-            raise FortranError("substrings are not supported")
+            if len(e.args) != 1 or not isinstance(e.args[0], Range) or e.args[0].step is not None:
+                raise FortranError(f"reference {e.name}(...) of a character scalar")
+            scope, sym, owner = v
+            lo = self.ex(e.args[0].lo, ctx)[0] if e.args[0].lo is not None else "None"
+            hi = self.ex(e.args[0].hi, ctx)[0] if e.args[0].hi is not None else "None"
+            return f"_substr({self.py(e.name, scope, owner)}, {lo}, {hi})", "char", 0
         return self.call(e.name, e.args, ctx, as_function=True)
 
     def intrinsic(self, name, args, ctx):
@@ -1420,6 +1695,14 @@ class Gen:
             dim = kw.get("dim", pos[1] if len(pos) > 1 else None)
             dc = self.ex(dim, ctx)[0] if dim is not None else "None"
             return f"_{name}({self.py(a.name, scope, owner)}, {dc})", "int", 0 if dim is not None or name == "size" else 1
+        if name == "len":
+            return f"len({vals[0][0]})", "int", 0
+        if name == "len_trim":
+            return f"len({vals[0][0]}.rstrip(' '))", "int", 0
+        if name == "trim":
+            return f"{vals[0][0]}.rstrip(' ')", "char", 0
+        if name == "index":
+            return f"({vals[0][0]}.find({vals[1][0]}) + 1)", "int", 0
         if name == "sum":
             if len(pos) > 1 or kw:
                 raise FortranError("SUM with DIM or MASK is not supported")
@@ -1523,6 +1806,107 @@ class Gen:
         out.append(p + "            raise")
         out.append(p + f"        {pc} = _tab[_g.label]")
 
+    _IOKIND = {"int": "int", "real": "real", "logical": "logical", "char": "char"}
+
+    def io(self, s, ctx, ind, out):
+        p = "    " * ind
+        c = s.a
+        unit = self.ex(c["unit"], ctx)[0]
+        body = []
+        if s.kind == "open":
+            f = lambda key, dflt: self.ex(c[key], ctx)[0] if key in c else repr(dflt)  # noqa: E731
+            body.append(f"_io.open({unit}, {f('file', '')}, {f('status', 'unknown')}, {f('form', 'formatted')})")
+        elif s.kind == "close":
+            body.append(f"_io.close({unit})")
+        elif s.kind == "read":
+            body.append(f"_rec = _io.read({unit})")
+            for it in s.b:
+                self.io_read(it, ctx, 0, body)
+        else:
+            body.append("_w = _RecordOut()")
+            for it in s.b:
+                self.io_write(it, ctx, 0, body)
+            body.append(f"_io.write({unit}, _w.data())")
+        handled = any(key in c for key in ("iostat", "err", "end"))
+        if not handled:
+            out.extend(p + line for line in body)
+            return
+        out.append(p + "try:")
+        out.extend(p + "    " + line for line in body)
+        if "iostat" in c:
+            lv, lt, helper = self.target(c["iostat"], ctx)
+            out.append(p + "    " + (helper.format("0") if helper else f"{lv} = 0"))
+        out.append(p + "except _IOError as _e:")
+        if "iostat" in c:
+            out.append(p + "    " + (helper.format("_e.code") if helper else f"{lv} = _e.code"))
+        if "end" in c:
+            out.append(p + f"    if _e.code < 0: raise _Goto({c['end']})")
+        if "err" in c:
+            out.append(p + f"    if _e.code > 0: raise _Goto({c['err']})")
+        if "iostat" not in c:
+            rest = [k for k in ("end", "err") if k not in c]
+            if rest:
+                out.append(p + "    raise")
+
+    def io_loop(self, it, ctx, ind, out, each):
+        scope, sym, owner = ctx.vis[it.var]
+        vc = self.py(it.var, scope, owner)
+        if scope == "host":
+            ctx.nonlocal_.add(vc)
+        p = "    " * ind
+        n = ctx.fresh()
+        a, b = self.ex(it.lo, ctx)[0], self.ex(it.hi, ctx)[0]
+        st = self.ex(it.step, ctx)[0] if it.step is not None else "1"
+        out.append(p + f"_a{n}, _s{n} = {a}, {st}")
+        out.append(p + f"_t{n} = max(0, _idiv({b} - _a{n} + _s{n}, _s{n}))")
+        out.append(p + f"for {vc} in range(_a{n}, _a{n} + _t{n} * _s{n}, _s{n}):")
+        for x in it.items:
+            each(x, ctx, ind + 1, out)
+        out.append(p + "else:")
+        out.append(p + f"    {vc} = _a{n} + _t{n} * _s{n}")
+
+    def io_read(self, it, ctx, ind, out):
+        p = "    " * ind
+        if isinstance(it, IDo):
+            return self.io_loop(it, ctx, ind, out, self.io_read)
+        if isinstance(it, (Name, Ref)) and it.name in ctx.vis and ctx.vis[it.name][1].rank and (
+                isinstance(it, Name) or any(isinstance(a, Range) for a in it.args)):
+            scope, sym, owner = ctx.vis[it.name]
+            arr = self.py(it.name, scope, owner)
+            specs = "None"
+            if isinstance(it, Ref):
+                c, _, _ = self.ref(it, ctx)
+                specs = c[len(f"_sec({arr}, "):-1]
+            out.append(p + f"_read_into({arr}, {specs}, _rec, {self._IOKIND[sym.typ]!r}, {sym.clen!r})")
+            return
+        lv, lt, helper = self.target(it, ctx)
+        v = f"_rec.char({self.char_len(it, ctx)!r})" if lt == "char" else f"_rec.{self._IOKIND[lt]}()"
+        out.append(p + (helper.format(v) if helper else f"{lv} = {v}"))
+
+    def io_write(self, it, ctx, ind, out):
+        p = "    " * ind
+        if isinstance(it, IDo):
+            return self.io_loop(it, ctx, ind, out, self.io_write)
+        if isinstance(it, (Name, Ref)) and it.name in ctx.vis and ctx.vis[it.name][1].rank and (
+                isinstance(it, Name) or any(isinstance(a, Range) for a in it.args)):
+            scope, sym, owner = ctx.vis[it.name]
+            arr = self.py(it.name, scope, owner)
+            specs = "None"
+            if isinstance(it, Ref):
+                c, _, _ = self.ref(it, ctx)
+                specs = c[len(f"_sec({arr}, "):-1]
+            out.append(p + f"_write_from(_w, {arr}, {specs}, {self._IOKIND[sym.typ]!r})")
+            return
+        c, t, r = self.ex(it, ctx)
+        if r:
+            raise FortranError("array expression in an output list")
+        out.append(p + f"_w.{self._IOKIND[t]}({c})")
+
+    def char_len(self, target, ctx):
+        if isinstance(target, Name) and target.name in ctx.vis:
+            return ctx.vis[target.name][1].clen
+        return None
+
     def loop_body(self, stmts, ctx, ind, out, n):
         loop = {"n": n, "dispatch": ctx.dispatch, "exc": False}
         ctx.loops.append(loop)
@@ -1597,7 +1981,11 @@ class Gen:
             else:
                 if r:
                     raise FortranError(f"line {s.line}: array value assigned to a scalar")
-                out.append(p + f"{lv} = {self.conv(c, t, lt)}")
+                if lt == "char":
+                    n = self.char_len(s.a, ctx)
+                    out.append(p + f"{lv} = _strfix({c}, {n!r})")
+                else:
+                    out.append(p + f"{lv} = {self.conv(c, t, lt)}")
         elif k == "if":
             for j, (cond, body) in enumerate(s.a):
                 c, _, _ = self.ex(cond, ctx)
@@ -1678,6 +2066,8 @@ class Gen:
                     out.append(p + f"{lv} = FArray.new({kind!r}, ({', '.join(bnds)},))")
         elif k == "bad":
             raise FortranError(s.a)
+        elif k in ("open", "close", "read", "write"):
+            self.io(s, ctx, ind, out)
         elif k == "deallocate":
             for it in s.a:
                 scope, sym, owner = ctx.vis[it.name]
@@ -1686,9 +2076,29 @@ class Gen:
             raise FortranError(f"statement {k}")
 
     # -- procedures
+    def implicit_typing(self, u: Unit):
+        """Without IMPLICIT NONE in the unit or a host, undeclared names take
+        INTEGER for I-N and REAL (8 bytes under -r8) otherwise."""
+        x = u
+        while x is not None:
+            if x.implicit_none:
+                return
+            x = x.host
+        typ = lambda n: "int" if n[0] in "ijklmn" else "real"  # noqa: E731
+        for a in u.args:
+            if u.syms[a].typ == "?":
+                u.syms[a].typ = typ(a)
+        if u.kind == "function" and u.syms[u.result].typ in ("?", None):
+            u.syms[u.result].typ = typ(u.result)
+        vis = self.visible(u)
+        known = set(vis) | set(self.procs) | {c.name for c in u.contains} | set(INTRINSIC_TYPES)
+        for n in sorted(_scalar_names(u.body) - known):
+            u.syms[n] = Sym(n, typ(n))
+
     def unit(self, u: Unit, ind: int, out: list):
         if u.bad:
             raise FortranError(u.bad)
+        self.implicit_typing(u)
         ctx = _Ctx(u, self.visible(u))
         ctx.contained = {c.name: c for c in u.contains}
         x = u.host
@@ -1713,6 +2123,8 @@ class Gen:
             sym = u.syms[a]
             if sym.typ == "?":
                 raise FortranError(f"undeclared dummy {a} of {u.name}")
+            if sym.typ == "char" and not sym.rank and sym.clen is not None:
+                out.append(q + f"f_{a} = _strfix(f_{a}, {sym.clen})")
             if sym.rank:
                 if any(d is None or d[1] is None for d in sym.dims):
                     if all(d is None for d in sym.dims):
@@ -1757,11 +2169,77 @@ class _Ctx:
         return self.n
 
 
+def _expr_names(e, out):
+    if isinstance(e, Name):
+        out.add(e.name)
+    elif isinstance(e, Ref):
+        for a in e.args:
+            _expr_names(a, out)
+    elif isinstance(e, Range):
+        for x in (e.lo, e.hi, e.step):
+            if x is not None:
+                _expr_names(x, out)
+    elif isinstance(e, Kw):
+        _expr_names(e.value, out)
+    elif isinstance(e, Comp):
+        _expr_names(e.base, out)
+    elif isinstance(e, Bin):
+        _expr_names(e.l, out)
+        _expr_names(e.r, out)
+    elif isinstance(e, Un):
+        _expr_names(e.x, out)
+    elif isinstance(e, Cons):
+        for x in e.items:
+            _expr_names(x, out)
+
+
+def _scalar_names(stmts) -> set:
+    """Names used without subscripts (variables, not arrays or functions) and DO variables."""
+    out = set()
+    for s in stmts:
+        if s.kind == "assign":
+            _expr_names(s.a, out)
+            _expr_names(s.b, out)
+        elif s.kind == "if":
+            for cond, blk in s.a:
+                _expr_names(cond, out)
+                out |= _scalar_names(blk)
+            if s.orelse:
+                out |= _scalar_names(s.orelse)
+        elif s.kind == "do":
+            out.add(s.a)
+            for x in (s.b, s.c, s.d):
+                if x is not None:
+                    _expr_names(x, out)
+            out |= _scalar_names(s.body)
+        elif s.kind == "dowhile":
+            _expr_names(s.a, out)
+            out |= _scalar_names(s.body)
+        elif s.kind == "call":
+            for a in s.b:
+                _expr_names(a, out)
+        elif s.kind in ("read", "write"):
+            stack = list(s.b or [])
+            while stack:
+                x = stack.pop()
+                if isinstance(x, IDo):
+                    out.add(x.var)
+                    stack.extend(x.items)
+                    for y in (x.lo, x.hi, x.step):
+                        if y is not None:
+                            _expr_names(y, out)
+                else:
+                    _expr_names(x, out)
+    return out
+
+
 def _goto_targets(stmts):
     t = set()
     for s in stmts:
         if s.kind == "goto":
             t.add(s.a)
+        if s.kind in ("open", "read", "write") and isinstance(s.a, dict):
+            t |= {s.a[k] for k in ("err", "end") if k in s.a}
         for blk in ([s.body] if s.body else []) + ([s.orelse] if s.orelse else []) + \
                 ([b for _, b in s.a] if s.kind == "if" else []):
             t |= _goto_targets(blk)
@@ -1784,6 +2262,10 @@ class Program:
         self.modules, self.procs = {}, {}
         self.undefined = {(p.lower(), n.lower()): v for (p, n), v in (undefined or {}).items()}
         for text in sources:
+            if isinstance(text, tuple):
+                text, fixed = text
+                if fixed:
+                    text = fixed_to_free(text)
             for u in parse_source(text, {d.upper() for d in defines}):
                 if u.kind == "module":
                     self.modules[u.name] = u
@@ -1804,11 +2286,21 @@ class Program:
             ctx = _Ctx(mu, gen.visible(mu))
             ns = self.ns[name]
             for n, sym in mu.syms.items():
-                if sym.param is not None:
-                    val = eval(gen.conv(*gen.ex(sym.param, ctx)[:2], sym.typ), env)
-                elif sym.init is not None and not sym.rank:
-                    val = eval(gen.conv(*gen.ex(sym.init, ctx)[:2], sym.typ), env)
-                else:
+                val = None
+                try:
+                    if sym.param is not None:
+                        val = eval(gen.conv(*gen.ex(sym.param, ctx)[:2], sym.typ), env)
+                    elif sym.rank and not sym.allocatable and all(d is not None for d in sym.dims):
+                        bnds = [(eval(gen.ex(lo, ctx)[0], env), eval(gen.ex(hi, ctx)[0], env)) for lo, hi in sym.dims]
+                        kind = sym.typ if sym.typ in ("real", "int") else "obj"
+                        val = FArray.new(kind, bnds)       # a fixed-size module array exists from the start
+                        if sym.typ.startswith("type:"):
+                            _new_objs(val, sorted(gen.types_of(mu).get(sym.typ[5:], {})))
+                        if sym.init is not None:
+                            _asgn(val, None, eval(gen.ex(sym.init, ctx)[0], env))
+                    elif sym.init is not None and not sym.rank:
+                        val = eval(gen.conv(*gen.ex(sym.init, ctx)[:2], sym.typ), env)
+                except (FortranError, NameError, TypeError):
                     val = None
                 setattr(ns, "f_" + n, val)
         self.untranslated = {}

@@ -20,6 +20,8 @@ reference's own, chained as the model chains them:
   read_data's numbering  src2LOWNS/data_io.F90:168-202 and 255-277 (the statements between the
                          file reads, on flag grids; alloc_dxdydz 0mod-arrays.F90:196-216)
   set_dx                 src2LOWNS/1sub-main.F90:53-74 (round lib/src/xy_calc.f90:100-112)
+  the case readers       read_data, read_fdata, read_nsdata (src2LOWNS/data_io.F90:87-397, owari and
+                         hajime lib/src/owari.f) on the files ingest.write_case writes, then set_dx
 
 The module constants come from the reference's module files (0mod-variables.F90);
 the case data fill the module arrays in the bounds the reference allocates them
@@ -244,6 +246,56 @@ def run_set_dx(root, dims, x) -> dict:
     return {"mx2": mx2, "x": rc.digest(vals(A.f_x)), "dx": rc.digest(vals(A.f_dx))}
 
 
+def case_files(case, sparse, t0, p, nor):
+    """The files ingest.write_case writes for the case: basename -> bytes."""
+    import tempfile
+
+    import __graft_entry__ as ge
+    ing = ge.load_package().ingest
+    with tempfile.TemporaryDirectory() as td:
+        ing.write_case(pathlib.Path(td) / "case", case, p=p, nor=nor, sparse=sparse, t=t0)
+        return {f.name: f.read_bytes() for f in sorted(pathlib.Path(td).iterdir())}
+
+
+def files_digest(files) -> str:
+    return rc.digest(np.frombuffer(b"".join(k.encode() + files[k] for k in sorted(files)), dtype=np.uint8))
+
+
+def run_reader(root, files, sparse) -> dict:
+    """The model's readers on the case files, in its order (main_2CLOWNS.F90:
+    363-369, 52): read_data, read_fdata, read_nsdata (data_io.F90:87-397), then
+    set_dx; the porosity file is the terrain fdata (INPUTf0) without drifting
+    bodies, so a = a0 and fb = fb0 (data_io.F90:302-345)."""
+    d = rc.digest
+    texts = [(root / f).read_text(encoding="latin-1") for f in GRID_SOURCES + ["src2LOWNS/data_io.F90"]]
+    texts.append(((root / "lib/src/owari.f").read_text(encoding="latin-1"), True))
+    prog = fx.Program(texts, DEFINES, undefined=UNDEFINED)
+    prog.env["_io"] = fx.FortranFiles(files)
+    V, A = prog.module("variables"), prog.module("arrays")
+    V.f_inputxyz = "case.xyzn" if sparse else "case.xyz"
+    V.f_input, V.f_inputf0 = "case", "case.fdata"
+    V.f_g_read, V.f_nu_read = 9.80665, 1.0e-6
+    for routine in ("read_data", "read_fdata", "read_nsdata", "set_dx"):
+        prog.call(routine)
+    inne2 = V.f_inne2
+    sp = vals(A.f_sp).reshape(3, -1)[:, :inne2 + 2]
+    nor = vals(A.f_nor).reshape(4, -1).T
+    out = {"dims": [V.f_is, V.f_js, V.f_ks, V.f_ie, V.f_je, V.f_ke], "inne": V.f_inne, "inne2": inne2,
+           "x": d(vals(A.f_x)), "dx": d(vals(A.f_dx)), "mn": d(vals(A.f_mn)),
+           "in": d(vals(A.f_in)[:inne2]), "jn": d(vals(A.f_jn)[:inne2]), "kn": d(vals(A.f_kn)[:inne2]),
+           "nf": d(np.array([o.f_f for o in A.f_nff.values()[:inne2 + 2]])),
+           "nfb": d(np.array([o.f_b for o in A.f_nff.values()[:inne2 + 2]])),
+           "u": d(vals(A.f_u)), "f": d(vals(A.f_f)[:inne2 + 2]), "p": d(vals(A.f_p)),
+           "a": d(vals(A.f_a)), "fb": d(vals(A.f_fb)[:inne2 + 2]),
+           # entries the readers never write (border rows of sp and nor) are undefined
+           "sp_undefined": rc.runs(np.flatnonzero(np.isnan(sp).ravel()) + 1),
+           "sp": d(sp[~np.isnan(sp)]), "nor_undefined": rc.runs(np.flatnonzero(np.isnan(nor).ravel()) + 1),
+           "nor": d(nor[~np.isnan(nor)]), "t0": V.f_t0, "g": V.f_g, "nu": V.f_nu}
+    if V.f_t0 > 0.0:
+        out["dt0"] = V.f_dt0
+    return out
+
+
 def run_will(root, label, ds, eps) -> dict:
     prog = program(root, WILL_SOURCES)
     nl, na = ds.al.shape
@@ -260,7 +312,10 @@ def run_will(root, label, ds, eps) -> dict:
 
 def main(argv):
     root = pathlib.Path(argv[1] if len(argv) > 1 else "/root/reference")
-    res = {"grids": {}, "will": {}, "numbering": {}, "set_dx": {}}
+    res = {"grids": {}, "will": {}, "numbering": {}, "set_dx": {}, "reader": {}}
+    for label, (case, sparse, t0, p, nor) in rc.reader_cases().items():
+        files = case_files(case, sparse, t0, p, nor)
+        res["reader"][label] = dict(run_reader(root, files, sparse), input=files_digest(files))
     for label, (dims, x) in rc.spacing_cases().items():
         res["set_dx"][label] = dict(run_set_dx(root, dims, x),
                                     input=rc.digest(np.concatenate([np.ravel(dims), np.ravel(x)])))

@@ -124,6 +124,27 @@ def numbering_cases():
     return out
 
 
+def reader_cases():
+    """label -> (case, sparse, t0, p, nor): cases written by ingest.write_case and
+    read back by the reference's readers -- both file forms (.xyzn sparse,
+    .xyz dense), t0 = 0 (no trailing dt) and t0 > 0, 2DV, boundary cells over
+    the full index range, seeded pressures and surface normals."""
+    grids = grid_cases()
+    rng = np.random.default_rng(91)
+    q = lambda v: np.round(v / QUANTUM) * QUANTUM  # noqa: E731
+    out = {}
+    for label, sparse, t0 in (("beach_10x6x8", True, 0.0), ("beach_10x6x8", False, 0.0),
+                              ("beach_10x6x8", False, 1.5), ("flume2dv_16x1x8", True, 0.5),
+                              ("section2dv_1x14x8", False, 0.0), ("speckled_20x12x16", True, 2.0),
+                              ("flume_40x24x20_ingested", True, 3.0), ("flume_40x24x20_ingested", False, 0.0)):
+        c = grids[label][0]
+        n = c.inne2 + 2
+        p = q(rng.normal(0.0, 50.0, size=n))
+        nor = q(rng.uniform(-1.0, 1.0, size=(n, 4)))
+        out[f"{label}_{'xyzn' if sparse else 'xyz'}_t{t0:g}"] = (c, sparse, t0, p, nor)
+    return out
+
+
 def spacing_cases():
     """label -> (dims, x (mx2, 3), x(l, i) at [i-1, l]): coordinates for set_dx --
     those of the grid cases, and variants with the last coordinate of an axis
@@ -167,21 +188,22 @@ def digest(a) -> str:
     return h.hexdigest()
 
 
-def runs(idx) -> list:
-    """Sorted indices as inclusive [first, last] runs."""
+def runs(idx) -> str:
+    """Sorted 1-based indices as inclusive runs, "first-last,first-last,..."."""
     out = []
     for i in (int(v) for v in idx):
         if out and out[-1][1] == i - 1:
             out[-1][1] = i
         else:
             out.append([i, i])
-    return out
+    return ",".join(f"{a}-{b}" for a, b in out)
 
 
-def runs_mask(r, n: int) -> np.ndarray:
-    """Boolean mask over 1..n (index 0 = row 1) of the rows the runs list."""
+def runs_mask(r: str, n: int) -> np.ndarray:
+    """Boolean mask over 1..n (index 0 = element 1) of the elements the runs list."""
     m = np.zeros(n, dtype=bool)
-    for a, b in r:
+    for part in filter(None, r.split(",")):
+        a, b = (int(v) for v in part.split("-"))
         m[a - 1:b] = True
     return m
 

@@ -304,3 +304,61 @@ end subroutine
     assert r[1] == 1e6 and r[2] == 1.0 / 1e6          # a product, a reciprocal of a product
     assert r[3] == 3 and r[4] == -3                    # halves away from zero
     assert r[5] == 9                                   # 12 pairs less the 3 with j == k
+
+
+def test_fixed_form_implicit_typing_and_characters():
+    src = """C     a comment line
+      subroutine last(text, nx, word, n2)
+      character*12 text
+      character*20 word
+      do 100 n=12,1,-1
+        if(text(n:n).ne.' ') then
+          nx=n
+          goto 200
+        end if
+  100 continue
+  200 word = text(1:nx)//
+     &  '.xyz'
+      x = 2.5
+      n2 = x * 3
+      if (word(nx+1:nx+4) .eq. '.xyz  ') n2 = n2 + 100
+      end
+"""
+    p = fx.Program([(src, True)], set())
+    r = p.call("last", "abc/de", 0, "", 0)
+    assert r[1] == 6 and r[2] == "abc/de.xyz".ljust(20) and r[3] == 107   # n2 = int(7.5) + 100
+
+
+def test_unformatted_io_round_trip():
+    p = prog("""
+subroutine rw(n, m, x)
+    implicit none
+    integer :: n, m, i, j, ist
+    real*8, dimension(0:2, 4) :: x
+    open(9, file='t.bin', status='unknown', form='unformatted')
+    write(9) n, (x(0, i), i = 1, 4)
+    write(9) ((x(j, i), j = 0, 2), i = 1, 2)
+    close(9)
+    x = 0.0d0
+    open(8, file='t.bin', status='old', form='unformatted')
+    read(8) m, (x(1, i), i = 1, 4)
+    read(8) x(0:2, 3), x(0, 4)
+    read(8, iostat=ist) n
+    m = m * 100 + ist
+    close(8)
+    open(8, file='none.bin', status='old', form='unformatted', err=50)
+    m = -1
+50  continue
+end subroutine
+""")
+    p.env["_io"] = fx.FortranFiles()
+    x = fx.FArray.new("real", ((0, 2), (1, 4)), fill=0.0)
+    for l in range(3):
+        for i in range(1, 5):
+            x[l, i] = 10 * i + l
+    r = p.call("rw", 7, 0, x)
+    assert r[1] == 699                      # 7 read back, then the end of file: iostat -1
+    assert [[x[l, i] for i in range(1, 5)] for l in range(3)] == [[0.0, 0.0, 10.0, 20.0], [10.0, 20.0, 11.0, 40.0],
+                                                                  [0.0, 0.0, 12.0, 0.0]]
+    recs = fx.FortranFiles.records(p.env["_io"].files["t.bin"])
+    assert [len(r) for r in recs] == [4 + 32, 48] and recs[0][:4] == b"\x00\x00\x00\x07"   # big-endian

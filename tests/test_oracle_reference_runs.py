@@ -152,3 +152,32 @@ def test_ingest_set_dx_reproduces_reference_set_dx(label):
     xx[:x.shape[0]] = x
     xo, dxo = ing.set_dx(dims, xx)
     assert d(np.ravel(xo)) == want["x"] and d(np.ravel(dxo)) == want["dx"]
+
+
+@pytest.mark.parametrize("label", sorted(RUNS["reader"]))
+def test_ingest_reader_reproduces_reference_readers(tmp_path, label):
+    """ingest.write_case's files read by the reference's own readers (read_data,
+    read_fdata, read_nsdata, set_dx) give exactly what ingest.read_case gives:
+    dimensions, coordinates and spacings, numbering, flags, velocities, F,
+    pressure, porosities, surface positions and normals (the entries the
+    readers define), t0, g, nu and the trailing dt."""
+    import make_ref_golden as mk
+    import __graft_entry__ as ge
+    ing = ge.load_package().ingest
+    want = RUNS["reader"][label]
+    case, sparse, t0, p, nor = rc.reader_cases()[label]
+    files = mk.case_files(case, sparse, t0, p, nor)
+    assert mk.files_digest(files) == want["input"], "the writer's bytes differ from what the reference read"
+    for name, data in files.items():
+        (tmp_path / name).write_bytes(data)
+    got = ing.read_case(tmp_path / "case")
+    c, n2 = got.case, got.case.inne2
+    spm = ~rc.runs_mask(want["sp_undefined"], 3 * (n2 + 2)).reshape(3, n2 + 2)
+    norm = ~rc.runs_mask(want["nor_undefined"], 4 * (n2 + 2)).reshape(n2 + 2, 4)
+    flat = lambda a: d(np.ravel(a))  # noqa: E731
+    _check("readers", {"dims": [int(v) for v in c.dims], "inne": c.inne, "inne2": n2, "x": flat(c.x),
+                       "dx": flat(c.dx), "mn": flat(c.mn), "in": flat(c.in_[1:n2 + 1]), "jn": flat(c.jn[1:n2 + 1]),
+                       "kn": flat(c.kn[1:n2 + 1]), "nf": flat(c.nf), "nfb": flat(c.nfb), "u": flat(c.un),
+                       "f": flat(c.f), "p": flat(got.p[:n2 + 1]), "a": flat(c.a), "fb": flat(c.fb),
+                       "sp": flat(c.sp[spm]), "nor": flat(got.nor[:n2 + 2][norm]), "t0": got.t0, "g": got.g,
+                       "nu": got.nu, "dt0": got.dt0}, want)
