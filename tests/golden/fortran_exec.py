@@ -455,6 +455,12 @@ class FortranFiles:
                 cur = b""
         return out
 
+    def newunit(self):
+        n = -10 - len(self.units)
+        while n in self.units:
+            n -= 1
+        return n
+
     def open(self, unit, name, status="unknown", form="formatted"):
         name = name.strip()
         if not form.strip().lower().startswith("unformatted"):
@@ -1389,6 +1395,15 @@ def parse_source(text: str, defines: set[str]) -> list[Unit]:
             unit = pos_args[0] if pos_args else kw.get("unit")
             fmt = pos_args[1] if len(pos_args) > 1 else kw.get("fmt")
             kind = m.group(1)
+            if kind == "open" and unit is None and "newunit" in kw:
+                ctl = {"unit": None, "newunit": px(kw["newunit"])}
+                for key in ("file", "status", "form", "iostat"):
+                    if key in kw:
+                        ctl[key] = px(kw[key])
+                for key in ("err",):
+                    if key in kw:
+                        ctl[key] = int(kw[key])
+                return St("open", no, label, a=ctl, b=[]), pos + 1
             if unit is None:
                 return St("bad", no, label, a=f"line {no}: {kind} without a unit"), pos + 1
             if kind == "write" and (unit in ("6", "*") or fmt is not None):
@@ -1575,8 +1590,10 @@ class Gen:
 
     def binop(self, e, ctx):
         lc, lt, lr = self.ex(e.l, ctx)
-        if e.op == "**" and isinstance(e.r, Num) and e.r.typ == "int" and 1 <= int(e.r.text) <= 3 and not lr:
+        if e.op == "**" and isinstance(e.r, Num) and e.r.typ == "int" and 1 <= int(e.r.text) <= 3:
             n = int(e.r.text)
+            if lr:
+                return f"_ew(lambda a: {' * '.join(['a'] * n)}, {lc})", lt, lr
             return "(" + " * ".join([f"({lc})"] * n) + ")", lt, 0
         rc, rt, rr = self.ex(e.r, ctx)
         rank = max(lr, rr)
@@ -1811,8 +1828,13 @@ class Gen:
     def io(self, s, ctx, ind, out):
         p = "    " * ind
         c = s.a
-        unit = self.ex(c["unit"], ctx)[0]
         body = []
+        if c.get("unit") is None:                # OPEN(NEWUNIT=v): a fresh unit number, stored in v
+            lv, lt, helper = self.target(c["newunit"], ctx)
+            body.append(helper.format("_io.newunit()") if helper else f"{lv} = _io.newunit()")
+            unit = self.ex(c["newunit"], ctx)[0]
+        else:
+            unit = self.ex(c["unit"], ctx)[0]
         if s.kind == "open":
             f = lambda key, dflt: self.ex(c[key], ctx)[0] if key in c else repr(dflt)  # noqa: E731
             body.append(f"_io.open({unit}, {f('file', '')}, {f('status', 'unknown')}, {f('form', 'formatted')})")

@@ -22,6 +22,8 @@ reference's own, chained as the model chains them:
   set_dx                 src2LOWNS/1sub-main.F90:53-74 (round lib/src/xy_calc.f90:100-112)
   the case readers       read_data, read_fdata, read_nsdata (src2LOWNS/data_io.F90:87-397, owari and
                          hajime lib/src/owari.f) on the files ingest.write_case writes, then set_dx
+  the grid generator's   output_xyzn / output_xyz, output_data, output_fdata, output_nsdata
+  writers                (srcMakeGrid/data_io.F90:639-651, 707-820, 875-897, 1505-1555)
 
 The module constants come from the reference's module files (0mod-variables.F90);
 the case data fill the module arrays in the bounds the reference allocates them
@@ -296,6 +298,66 @@ def run_reader(root, files, sparse) -> dict:
     return out
 
 
+WRITER_SOURCES = ["srcMakeGrid/0mod-type_interface.F90", "srcMakeGrid/0mod-variables.F90",
+                  "srcMakeGrid/0mod-arrays.F90", "srcMakeGrid/data_io.F90"]
+
+
+def run_writer(root, case, sparse, t0, p, nor) -> dict:
+    """The grid generator's writers (srcMakeGrid/data_io.F90: output_xyzn with
+    its recoding pass off, or output_xyz; output_data, output_fdata,
+    output_nsdata) on the case's arrays, in the bounds the generator allocates
+    (make_grid_main.F90:189-256).  The surface cells are listed in ascending
+    order (the generator's own order comes from its surface search, outside
+    this path).  Returns the files' digests, and for the dense form whether the
+    solver's readers accept the generator's files."""
+    import __graft_entry__ as ge
+    ing = ge.load_package().ingest
+    texts = [(root / f).read_text(encoding="latin-1") for f in WRITER_SOURCES]
+    texts.append(((root / "lib/src/owari.f").read_text(encoding="latin-1"), True))
+    prog = fx.Program(texts, set())                # srcMakeGrid/Makefile defines no macros
+    prog.env["_io"] = io = fx.FortranFiles()
+    V, A = prog.module("variables"), prog.module("arrays")
+    is_, js, ks, ie, je, ke = (int(v) for v in case.dims)
+    inne, inne2 = int(case.inne), int(case.inne2)
+    V.f_is, V.f_js, V.f_ks, V.f_ie, V.f_je, V.f_ke = is_, js, ks, ie, je, ke
+    V.f_title, V.f_inne, V.f_inne2 = "case", inne, inne2
+    V.f_t, V.f_g, V.f_nu, V.f_dt = t0, ing.G_ACC, 1.0e-6, case.dt
+    V.f_fg_xyz, A.f_xyzn = (1 if sparse else 0), sparse
+    A.f_x = farray("real", case.x.ravel(), [(0, 2), (1, case.x.shape[0])])
+    A.f_ls, A.f_le = farray("int", [is_, js, ks], [(0, 2)]), farray("int", [ie, je, ke], [(0, 2)])
+    nf3, nfb3 = ing.flag_grids(case)
+    b3 = [(is_ - 1, ie), (ks - 1, ke), (js - 1, je)]
+    A.f_nf3, A.f_nfb3 = farray("int", nf3.ravel(), b3), farray("int", nfb3.ravel(), b3)
+    A.f_mn = farray("int", case.mn.ravel(), [(is_ - 2, ie + 2), (ks - 2, ke + 2), (js - 2, je + 2)])
+    for nm, arr in (("in", case.in_), ("jn", case.jn), ("kn", case.kn)):
+        setattr(A, "f_" + nm, farray("int", arr[1:inne2 + 1], [(1, inne2)]))
+    A.f_nff = farray("obj", [CellFlag(int(f), int(b)) for f, b in zip(case.nf, case.nfb)], [(0, inne2 + 1)])
+    A.f_u = farray("real", case.un[1:inne2 + 1].ravel(), [(0, 2), (1, inne2)])
+    A.f_f = farray("real", case.f[1:inne2 + 1], [(1, inne2)])
+    A.f_p = farray("real", p[1:inne2 + 1], [(1, inne2)])
+    A.f_a = farray("real", case.a[1:inne2 + 1].ravel(), [(0, 2), (1, inne2)])
+    A.f_fb = farray("real", case.fb[1:inne2 + 1], [(1, inne2)])
+    A.f_sp = farray("real", case.sp.ravel(), [(0, inne2 + 1), (0, 2)])
+    A.f_nor = farray("real", nor.T.ravel(), [(0, inne2 + 1), (0, 3)])
+    listed = [nn for nn in range(1, inne + 1) if case.sp[0, nn] != -1.0e4]
+    A.f_sfnoi = farray("int", listed or [0], [(1, max(1, len(listed)))])
+    V.f_mms = len(listed)
+    if sparse:
+        prog.call("output_xyzn", 0)
+    else:
+        prog.call("output_xyz")
+    for routine in ("output_data", "output_fdata", "output_nsdata"):
+        prog.call(routine)
+    out = {"files": {k: rc.digest(np.frombuffer(v, dtype=np.uint8)) for k, v in io.files.items()}}
+    if not sparse:
+        try:
+            run_reader(root, io.files, sparse)
+            out["solver_reads_generator_files"] = True
+        except fx._IOError:
+            out["solver_reads_generator_files"] = False
+    return out
+
+
 def run_will(root, label, ds, eps) -> dict:
     prog = program(root, WILL_SOURCES)
     nl, na = ds.al.shape
@@ -312,10 +374,11 @@ def run_will(root, label, ds, eps) -> dict:
 
 def main(argv):
     root = pathlib.Path(argv[1] if len(argv) > 1 else "/root/reference")
-    res = {"grids": {}, "will": {}, "numbering": {}, "set_dx": {}, "reader": {}}
+    res = {"grids": {}, "will": {}, "numbering": {}, "set_dx": {}, "reader": {}, "writer": {}}
     for label, (case, sparse, t0, p, nor) in rc.reader_cases().items():
         files = case_files(case, sparse, t0, p, nor)
         res["reader"][label] = dict(run_reader(root, files, sparse), input=files_digest(files))
+        res["writer"][label] = run_writer(root, case, sparse, t0, p, nor)
     for label, (dims, x) in rc.spacing_cases().items():
         res["set_dx"][label] = dict(run_set_dx(root, dims, x),
                                     input=rc.digest(np.concatenate([np.ravel(dims), np.ravel(x)])))

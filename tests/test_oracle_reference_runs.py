@@ -181,3 +181,22 @@ def test_ingest_reader_reproduces_reference_readers(tmp_path, label):
                        "f": flat(c.f), "p": flat(got.p[:n2 + 1]), "a": flat(c.a), "fb": flat(c.fb),
                        "sp": flat(c.sp[spm]), "nor": flat(got.nor[:n2 + 2][norm]), "t0": got.t0, "g": got.g,
                        "nu": got.nu, "dt0": got.dt0}, want)
+
+
+@pytest.mark.parametrize("label", sorted(RUNS["writer"]))
+def test_ingest_writer_reproduces_generator_files(label):
+    """ingest.write_case against the grid generator's own writers on the same
+    arrays: every file byte for byte -- except, in the dense form, the .fdata
+    file: the generator writes its sparse form there whatever the form, which
+    the solver's read_fdata cannot read (recorded by the run), so write_case
+    writes the dense .fdata the solver reads (checked by the reader test)."""
+    import make_ref_golden as mk
+    want = RUNS["writer"][label]
+    case, sparse, t0, p, nor = rc.reader_cases()[label]
+    files = mk.case_files(case, sparse, t0, p, nor)
+    assert set(files) == set(want["files"])
+    for name, data in files.items():
+        if name == "case.fdata" and not sparse:
+            assert want["solver_reads_generator_files"] is False
+            continue
+        assert d(np.frombuffer(data, dtype=np.uint8)) == want["files"][name], name
