@@ -10,6 +10,7 @@
 // direction d becomes row i's coefficient toward j in the opposite direction.
 #include "common.cuh"
 #include "grid_index.cuh"
+#include "trace.h"
 
 namespace clowns {
 
@@ -81,6 +82,7 @@ using namespace clowns;
 
 extern "C" int clowns_transpose_dev(int n, int na, int nl, const double* alu, const int* llu, const double* de,
                                     double* alt, int* llt, double* det, int* bad, void* stream) {
+    clowns::TraceRange trace_range_("clowns_transpose_dev");
     if (n < 1 || na < n || (nl != 6 && nl != 4) || !alu || !llu || !de || !alt || !llt || !det || !bad) {
         set_last_error_msg("transpose: invalid arguments");
         return CLOWNS_ERR_ARG;
@@ -99,6 +101,7 @@ extern "C" int clowns_face_grad_dev(const int* dims, int inne, int inne2, int if
                                     const int* in_, const int* jn, const int* kn, const int* nf, const int* mno,
                                     const double* alu_c, const int* ll_c, const double* a, const double* x,
                                     const double* lambda, double* grad, void* stream) {
+    clowns::TraceRange trace_range_("clowns_face_grad_dev");
     if (!grid_dims_ok(dims) || !grid_has_matrix(dims) || inne < 1 || ifln < 0 || !fln || !in_ || !jn || !kn || !nf ||
         !mno || !alu_c || !ll_c || !a || !x || !lambda || !grad) {
         set_last_error_msg("face_grad: invalid arguments");

@@ -10,6 +10,7 @@
 
 #include "common.cuh"
 #include "grid_index.cuh"
+#include "trace.h"
 
 namespace clowns {
 
@@ -318,6 +319,7 @@ extern "C" int clowns_init_matrix_dev(const int* dims, int inne, int mx2, const 
                                       const int* jn, const int* kn, const int* nf, const int* nfb,
                                       const double* a, const double* fb, const double* dx, double* mp,
                                       double* alu_c, int* ll_c, double* de_c, void* stream) {
+    clowns::TraceRange trace_range_("clowns_init_matrix_dev");
     if (!grid_dims_ok(dims) || inne < 1 || mx2 < 1 || !mn || !in_ || !jn || !kn || !nf || !nfb || !a || !fb || !dx || !mp ||
         !alu_c || !ll_c || !de_c) {
         set_last_error_msg("init_matrix: invalid arguments");
@@ -348,6 +350,7 @@ extern "C" int clowns_rows_rhs_dev(const int* dims, int inne2, int mx2, const in
                                    const double* mp, double dt, int ifln, const int* fln, int mm2, int* mno,
                                    int* mno2mn, double* b, double* xe, double* de, int* mnoe_out,
                                    double* dmax_out, void* work, size_t work_bytes, void* stream) {
+    clowns::TraceRange trace_range_("clowns_rows_rhs_dev");
     (void)inne2; (void)mx2;
     if (!grid_dims_ok(dims) || !mn || !in_ || !jn || !kn || !nf || !nfb || !f || !fb || !a || !un || !dx || !mp || !fln ||
         !mno || !mno2mn || !b || !xe || !de || !mnoe_out || ifln < 0 || mm2 < 1 || !work) {
@@ -417,6 +420,7 @@ extern "C" int clowns_assemble_dev(const int* dims, int inne, int inne2, int mx2
                                    const double* sp, int ifln, const int* fln, const int* mno, const double* alu_c,
                                    const int* ll_c, const double* de_c, int mm2, double* alu, int* llu, double* de,
                                    int* err_cell, void* stream) {
+    clowns::TraceRange trace_range_("clowns_assemble_dev");
     (void)mx2;
     if (!grid_dims_ok(dims) || inne < 1 || !in_ || !jn || !kn || !nf || !nfb || !x || !dx || !sp || !fln || !mno || !alu_c ||
         !ll_c || !de_c || mm2 < 1 || !alu || !llu || !de || !err_cell) {
@@ -442,6 +446,7 @@ extern "C" int clowns_correct_dev(const int* dims, int inne, int mx2, const int*
                                   const int* kn, const int* nf, const int* nfb, const double* a, const double* dx,
                                   double dt, int mnoe, const int* mno2mn, const int* mno, const double* xe0,
                                   double* p, double* un, void* stream) {
+    clowns::TraceRange trace_range_("clowns_correct_dev");
     (void)mx2;
     if (!grid_dims_ok(dims) || inne < 1 || !mn || !in_ || !jn || !kn || !nf || !nfb || !a || !dx || mnoe < 0 || !mno2mn ||
         !mno || !xe0 || !p || !un) {

@@ -6,6 +6,7 @@
 
 #include "engine.cuh"
 #include "engine_api.h"
+#include "trace.h"
 
 namespace clowns {
 
@@ -134,6 +135,7 @@ extern "C" int clowns_version(void) { return 10000; }
 extern "C" void pcgpme_gpu(double* al, const int* nl, const int* na, int* ll, double* d,
                            const int* n, const int* n2, double* b, double* x, double* eps,
                            const double* parm, int* iter, int* ier) {
+    clowns::TraceRange trace_range_("pcgpme_gpu");
     if (!al || !nl || !na || !ll || !d || !n || !n2 || !b || !x || !eps || !parm || !iter || !ier) {
         if (ier) *ier = CLOWNS_IER_ARG;
         set_last_error_msg("pcgpme_gpu: NULL argument");
@@ -171,6 +173,7 @@ extern "C" void pcgpme_(double* al, const int* nl, const int* na, int* ll, doubl
 extern "C" int pcgpme_will_gpu(const double* al, const int* nl, const int* na, const int* ll, const double* d,
                                const int* n, const int* n2, double* b, const double* eps, const double* parm,
                                const int* iter) {
+    clowns::TraceRange trace_range_("pcgpme_will_gpu");
     if (!al || !nl || !na || !ll || !d || !n || !n2 || !b || !eps || !parm || !iter) {
         set_last_error_msg("pcgpme_will_gpu: NULL argument");
         return CLOWNS_ERR_ARG;

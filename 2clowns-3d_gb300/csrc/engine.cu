@@ -17,6 +17,7 @@
 
 #include "engine.cuh"
 #include "engine_api.h"
+#include "trace.h"
 
 namespace clowns {
 
@@ -935,6 +936,7 @@ static void wait_params(bool take, long* limit, int* absent) {
 template <typename T>
 static int run_loop(Eng<T> E, const void* work, GridBar* gb, int prec, const LoopShape& sh, cudaStream_t s,
                     bool take_fault = false) {
+    TraceRange trace_range_("iteration loop");
     if (sh.bal && E.M > 1 && E.baltab && (sh.graph == 1 || sh.graph == 2)) {
         // ensembles on the balanced kernels: block tables over the members that iterate
         k_bal_rebuild<<<1, kBalScanThreads, 0, s>>>(E.S, E.M, E.mem_n, (BalBlock*)E.baltab, E.balg, E.ctrl + 4);
@@ -1028,6 +1030,7 @@ constexpr int kTuneIters = 24;
 template <typename T, typename Prime>
 static int tune_loop(Eng<T> E, const void* work, GridBar* gb, long key_nv, int key_prec, Prime prime,
                      cudaStream_t s, LoopShape* out) {
+    TraceRange trace_range_("loop autotuner");
     const int forced = forced_loop_mode();
     const bool wave_ok = E.wave != nullptr && E.M == 1;
     if (forced == 1 || forced == 2) {
@@ -1411,6 +1414,7 @@ int engine_solve_mixed(int M, const MemberIn* ins, double eps, double parm, doub
     CLOWNS_CUDA_TRY(cudaGetLastError());
     std::vector<MemberScalars> h(M);
     for (int sweep = 0; sweep <= max_outer + 1; sweep++) {
+        TraceRange trace_sweep_("refinement sweep");
         sweep_head(s, inner_tol, inner_max);
         t_launches += 8;
         CLOWNS_CUDA_TRY(cudaMemcpyAsync(h.data(), E.S, sizeof(MemberScalars) * M, cudaMemcpyDeviceToHost, s));
@@ -1583,6 +1587,7 @@ static int static_upload_tables(void* work, const EngLayout& L, int n, const Mem
 extern "C" int clowns_pcgpme_static_dev(const double* al, int nl, int na, const int* ll, const double* d, int n,
                                         const double* b, double* x, double eps, double parm, int iter, void* stream,
                                         clowns_solve_info* info) {
+    clowns::TraceRange trace_range_("clowns_pcgpme_static_dev");
     using namespace clowns;
     if (n > kStaticMaxRows) {
         set_last_error_msg("pcgpme_static: n exceeds CLOWNS_STATIC_MAX_ROWS (32768 rows)");

@@ -13,6 +13,7 @@
 
 #include "common.cuh"
 #include "grid_index.cuh"
+#include "trace.h"
 
 namespace clowns {
 
@@ -350,6 +351,7 @@ extern "C" int clowns_set_nflag_dev(const int* dims, int inne, int inne2, int mx
                                     const double* a, const double* dx, const int* objno, int* fln, int* ifln_out,
                                     int* sfn, int* isfn_out, int* passes_out, void* work, size_t work_bytes,
                                     void* stream) {
+    clowns::TraceRange trace_range_("clowns_set_nflag_dev");
     (void)mx2;
     if (!grid_dims_ok(dims) || inne < 1 || !mn || !in_ || !jn || !kn || !nf || !nfb || !f || !fb || !a || !dx || !objno ||
         !fln || !ifln_out || !sfn || !isfn_out || !work) {

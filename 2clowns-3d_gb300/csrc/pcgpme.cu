@@ -5,6 +5,7 @@
 
 #include "engine.cuh"
 #include "engine_api.h"
+#include "trace.h"
 
 using namespace clowns;
 
@@ -34,6 +35,7 @@ extern "C" size_t clowns_pcgpme_workspace_bytes(int n, int nl) {
 extern "C" int clowns_pcgpme_dev(const double* al, int nl, int na, const int* ll, const double* d, int n,
                                  const double* b, double* x, double eps, double parm, int iter, void* work,
                                  size_t work_bytes, void* stream, clowns_solve_info* info) {
+    clowns::TraceRange trace_range_("clowns_pcgpme_dev");
     MemberIn in = member(al, nl, na, ll, d, n, b, x);
     return engine_solve_plain(1, &in, eps, parm, iter, work, work_bytes, (cudaStream_t)stream, info);
 }
@@ -48,6 +50,7 @@ extern "C" int clowns_pcgpme_mixed_dev(const double* al, int nl, int na, const i
                                        const double* b, double* x, double eps, double parm, double inner_tol,
                                        int inner_max, int max_outer, void* work, size_t work_bytes, void* stream,
                                        clowns_solve_info* info) {
+    clowns::TraceRange trace_range_("clowns_pcgpme_mixed_dev");
     MemberIn in = member(al, nl, na, ll, d, n, b, x);
     return engine_solve_mixed(1, &in, eps, parm, inner_tol, inner_max, max_outer, work, work_bytes,
                               (cudaStream_t)stream, info);
@@ -61,6 +64,7 @@ extern "C" size_t clowns_pcgpme_batched_workspace_bytes(int m, const int* n, int
 extern "C" int clowns_pcgpme_batched_dev(int m, const clowns_member* members, int precision, double eps,
                                          double parm, int iter, double inner_tol, int inner_max, int max_outer,
                                          void* work, size_t work_bytes, void* stream, clowns_solve_info* infos) {
+    clowns::TraceRange trace_range_("clowns_pcgpme_batched_dev");
     if (m < 1 || !members || (precision != CLOWNS_PREC_FP64 && precision != CLOWNS_PREC_MIXED)) {
         set_last_error_msg("pcgpme_batched: invalid arguments");
         return CLOWNS_ERR_ARG;
@@ -75,6 +79,7 @@ extern "C" int clowns_pcgpme_batched_dev(int m, const clowns_member* members, in
 extern "C" int clowns_pcgpme_setup_dev(const double* al, int nl, int na, const int* ll, const double* d, int n,
                                        const double* b, double parm, double* al_s, int* ll_s, double* d_s,
                                        double* b_s, int na_out, void* work, size_t work_bytes, void* stream) {
+    clowns::TraceRange trace_range_("clowns_pcgpme_setup_dev");
     if (!al_s || !ll_s || !d_s || !b_s || na_out < n) {
         set_last_error_msg("setup: invalid arguments");
         return CLOWNS_ERR_ARG;
@@ -87,6 +92,7 @@ extern "C" int clowns_pcgpme_setup_dev(const double* al, int nl, int na, const i
 extern "C" int clowns_apply_pm_a_dev(const double* al, int nl, int na, const int* ll, const double* d, int n,
                                      double parm, const double* x, double* y, void* work, size_t work_bytes,
                                      void* stream) {
+    clowns::TraceRange trace_range_("clowns_apply_pm_a_dev");
     if (!x || !y) {
         set_last_error_msg("apply: invalid arguments");
         return CLOWNS_ERR_ARG;

@@ -16,6 +16,7 @@
 #include "engine.cuh"
 #include "engine_api.h"
 #include "grid_index.cuh"
+#include "trace.h"
 
 extern "C" {
 size_t clowns_set_nflag_workspace_bytes(const int* dims, int inne2);
@@ -171,6 +172,7 @@ extern "C" int clowns_session_set_fields(clowns_session* S, const int* nf, const
 
 // set_nflag on the session's fields (called every step by cal_vof, 1sub-vof.F90:37)
 extern "C" int clowns_session_classify(clowns_session* S, int* ifln, int* isfn) {
+    clowns::TraceRange trace_range_("clowns_session_classify");
     if (!S) return CLOWNS_ERR_ARG;
     int passes = 0;
     SESSION_TRY(clowns_set_nflag_dev(S->dims, S->inne, S->inne2, S->mx2, S->mn, S->in_, S->jn, S->kn, S->nf,
@@ -218,6 +220,7 @@ extern "C" int clowns_session_classify(clowns_session* S, int* ifln, int* isfn) 
 extern "C" int clowns_session_pressure_loop(clowns_session* S, double dt, double d0, double eps0, int precision,
                                             int* ik_out, double* dmax_out, int* iter_out, double* err_out,
                                             int* icon_out) {
+    clowns::TraceRange trace_range_("clowns_session_pressure_loop");
     if (!S || S->mm2 == 0 || dt <= 0) {
         set_last_error_msg("session_pressure_loop: classify the fields first");
         return CLOWNS_ERR_ARG;

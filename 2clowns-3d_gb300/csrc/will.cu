@@ -22,6 +22,7 @@
 
 #include "engine.cuh"
 #include "engine_api.h"
+#include "trace.h"
 
 namespace clowns {
 
@@ -111,6 +112,7 @@ extern "C" size_t clowns_pcgpme_will_workspace_bytes(int n, int nl) {
 extern "C" int clowns_pcgpme_will_dev(const double* al, int nl, int na, const int* ll, const double* d, int n,
                                       double* b, double eps, double parm, int iter, void* work, size_t work_bytes,
                                       void* stream, clowns_solve_info* info) {
+    clowns::TraceRange trace_range_("clowns_pcgpme_will_dev");
     if (!al || !ll || !d || !b || !work || n < 1 || na < n || (nl != 4 && nl != 6)) {
         set_last_error_msg("pcgpme_will: invalid arguments");
         return CLOWNS_ERR_ARG;
@@ -143,6 +145,7 @@ extern "C" size_t clowns_will_postprocess_workspace_bytes(int n) { return n < 1 
 
 extern "C" int clowns_will_postprocess_dev(const double* x, const double* r, const int* ll, int nl, int na, int n,
                                            double* b, double* x_out, void* work, size_t work_bytes, void* stream) {
+    clowns::TraceRange trace_range_("clowns_will_postprocess_dev");
     if (!x || !r || !ll || !b || !work || n < 1 || na < n || nl < 1) {
         set_last_error_msg("will_postprocess: invalid arguments");
         return CLOWNS_ERR_ARG;
