@@ -547,7 +547,12 @@ def write_case(prefix, case: Case, *, p: Optional[np.ndarray] = None, nor: Optio
     ``nor`` default to zero, ``dt`` to the case's.  In the sparse form a cell
     is listed in ``.nsdata`` when its surface x position is not -1e4, and the
     data and fdata files skip the cells the generator skips (an air cell at
-    rest with F < 1e-13; a cell with all faces open and porosity 1)."""
+    rest with F < 1e-13; a cell with all faces open and porosity 1).  One
+    file departs from the generator: in the dense form the generator
+    (srcMakeGrid/data_io.F90:785-820) still writes the sparse ``.fdata``,
+    which the solver's read_fdata (src2LOWNS/data_io.F90:302-345) reads only
+    when the xyz file is sparse; here the dense form gets the dense
+    ``.fdata`` (per cell ``a(0:2,nn), fb(nn)``) that the solver reads."""
     prefix = str(prefix)
     dims = check_dims(case.dims)
     is_, js, ks, ie, je, ke = (int(v) for v in dims)
