@@ -176,9 +176,12 @@ def run_grid(root, label, case, solve: bool, loop: bool) -> dict:
     if solve:
         prog.call("cal_poisson_equation")
         x = np.array(vals(A.f_xe)[1:mnoe + 1].tolist())
-        out["solve"] = {"iter": V.f_iter, "eps": V.f_eps, "ier": prog.env["s_cal_poisson_equation"].f_ier,
-                        "x": d(x)}
-        SOLUTIONS[f"{out['label']}/x"] = x
+        rec = {"iter": V.f_iter, "eps": V.f_eps, "ier": prog.env["s_cal_poisson_equation"].f_ier, "x": d(x)}
+        if solve == "cpu":
+            out["solve_cpu"] = rec
+        else:
+            out["solve"] = rec
+            SOLUTIONS[f"{out['label']}/x"] = x
     if loop:
         prog = program(root, GRID_SOURCES)
         prog.fragment("cal_momentum", 41, 60, "ik_loop")

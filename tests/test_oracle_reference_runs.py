@@ -72,9 +72,10 @@ def test_oracle_reproduces_reference_run(ora, grids, label):
                             "mno2mn": d(sy.mno2mn[1:n + 1]), "b": d(sy.b[1:n + 1])}, want["rows"])
     _check("cal_matrix_element", {"alu": d(sy.alu[:, :n]), "llu": d(sy.llu[:, :n]), "de": d(sy.de[1:n + 1])},
            want["asm"])
-    if solve:
-        r = ora.pcgpme(sy.alu, sy.llu, sy.de[1:], sy.b[1:], n, eps=case.eps0, parm=5.0, itmax=10000, nthreads=1)
-        _check("PCGPME", {"iter": r.iters, "eps": r.eps, "ier": r.ier, "x": d(r.x[:n])}, want["solve"])
+    for key in ("solve", "solve_cpu"):
+        if key in want:
+            r = ora.pcgpme(sy.alu, sy.llu, sy.de[1:], sy.b[1:], n, eps=case.eps0, parm=5.0, itmax=10000, nthreads=1)
+            _check("PCGPME", {"iter": r.iters, "eps": r.eps, "ier": r.ier, "x": d(r.x[:n])}, want[key])
     if loop:
         ik, dmax, p, un = oracle_loop(ora, case, cls, sm, rc.LOOP_D0, rc.LOOP_EPS0)
         _check("ik loop", {"ik": ik, "dmax": dmax, "p": d(p), "un": d(un)}, want["loop"])
@@ -95,6 +96,7 @@ def test_fixture_covers_every_stage():
     g = RUNS["grids"]
     assert {"nflag", "init", "rows", "asm"} <= set().union(*(v.keys() for v in g.values()))
     assert sum("solve" in v for v in g.values()) >= 8
+    assert sum("solve_cpu" in v and v["rows"]["mnoe"] >= 9000 for v in g.values()) >= 3
     assert sum("loop" in v and v["loop"]["ik"] >= 2 for v in g.values()) >= 5
     assert any(v["init"]["nl"] == 4 for v in g.values()) and any(v["init"]["nl"] == 6 for v in g.values())
     assert any(v["init"]["undefined_rows"] for v in g.values())
