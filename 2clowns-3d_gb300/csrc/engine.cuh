@@ -133,7 +133,8 @@ struct Eng {
     int* ctrl;                // [0] loop-body count, [1] max ITER over members, [2] bodies of earlier sweeps
     const BalBlock* baltab;   // ensembles: 16 block tables of the balanced kernels (nullptr: none)
     const int* balg;          // ensembles: the blocks of each table's launch (16)
-    int nl;                   // columns the members' matrices fill: 6 (3D) or 4 (2DH); the rest are empty
+    int nl;                   // columns the members' matrices fill: 6 (3D) or 4 (2DV, and the 2DH
+                              // systems of PCGPME_WILL); the rest are empty
     int pf;                   // balanced kernels: rows per block and stream asked of L2 before the
                               // wait on the previous kernel (0: none)
     int* abort;               // set by a kernel whose bounded wait ran out (the grid barrier's flag)
