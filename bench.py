@@ -59,6 +59,11 @@ def measured_peaks():
 TRAFFIC_ROW_ITER_FP64 = 434.2
 TRAFFIC_ROW_ITER_MIXED = 224.6
 
+# What pins the CPU port: run on one thread it reproduces the reference's own
+# PCGPME, executed from its Fortran source, bit for bit.
+PORT_PARITY = ("serially bit-identical to the reference's PCGPME run from its source text "
+               "(tests/test_oracle_reference_runs.py)")
+
 # FP64 arithmetic of one iteration per row, in fused multiply-adds (a multiply or
 # an add counts as one): AXSUB D x + 6 AL = 7 and LDUSUB 6 sweeps = 6 per
 # application (26 for two), RQ 1, e 1, AMU and SS 2, x 2, r 1, RN and C1 2, p 2
@@ -194,7 +199,8 @@ def run_reference(args, world, rank):
         "cpu_baseline": {"value": value, "unit": "solves/s", "cores": threads, "kind": "port",
                          "cpu_model": cpu_model(),
                          "sample": f"full solves of {args.workload} (N={sy.mnoe}, {last.iters} iterations), "
-                                   f"OpenMP restatement of pcgpme_para.F90, {threads} threads"},
+                                   f"OpenMP restatement of pcgpme_para.F90, {threads} threads",
+                         "port_parity": PORT_PARITY},
         "e2e": {"value": value, "unit": "solves/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
     }
     print(json.dumps(line), flush=True)
@@ -721,6 +727,7 @@ def _report(pkg, args, world, rank, case, n, ms, infos, info, it, value, alg, ac
                "sample": f"median of 10 full solves of {args.workload} (N={sy.mnoe}, {r.iters} iterations) after 3 "
                          f"warm-ups, OpenMP restatement of pcgpme_para.F90 on {threads} threads "
                          f"(min {min(times):.3f} s, max {max(times):.3f} s)",
+               "port_parity": PORT_PARITY,
                "one_thread": {"value": 1.0 / t1, "unit": "solves/s", "iters": r1.iters,
                               "sample": f"one full solve on 1 thread, measured ({t1:.1f} s)"}}
         nrm = np.linalg.norm(r.x)
