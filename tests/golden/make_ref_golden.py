@@ -361,6 +361,35 @@ def run_writer(root, case, sparse, t0, p, nor) -> dict:
     return out
 
 
+PCGPME_EDGES = {"cap5": (1e-14, 5), "default_cap": (1e-10, 0), "eps0_small": (0.0, 10000),
+                "tight_tolerance": (2e-15, 10000)}
+
+
+def run_pcgpme_edges(root, case) -> dict:
+    """PCGPME at its argument edges on the system the reference assembles:
+    ITER = 5 (the cap: IER = 3000, ITER = cap + 1), ITER = 0 (the default cap
+    10 (sqrt N + 1), pcgpme_para.F90:52) and EPS(1) = 0 (replaced by SMALL,
+    pcgpme_para.F90:51); each on a fresh assembly, as PCGPME scales and sorts
+    its arguments in place; and EPS(1) = 2e-15, the tightest tolerance above
+    TINY, which runs the iteration down to the rounding floor."""
+    out = {}
+    for name, (eps, itmax) in PCGPME_EDGES.items():
+        prog = program(root, GRID_SOURCES)
+        V, A = load_grid(prog, case)
+        for routine in ("set_nflag", "init_matrix"):
+            prog.call(routine)
+        allocate_matrix(prog, V, A)
+        for routine in ("cal_err_of_continuity", "cal_matrix_element"):
+            prog.call(routine)
+        n, mm2, nl = V.f_mnoe, V.f_mm2, V.f_nl
+        e = farray("real", [eps, 0.0], [(1, 2)])
+        r = prog.call("pcgpme", A.f_alu, nl, mm2, A.f_llu, A.f_de, n, 64, A.f_b, A.f_xe.section_view(1, mm2),
+                      e, 5.0, itmax, 0)
+        x = np.array(vals(A.f_xe)[1:n + 1].tolist())
+        out[name] = {"iter": r[11], "ier": r[12], "eps": e.values()[0], "x": rc.digest(x)}
+    return out
+
+
 def run_will(root, label, ds, eps) -> dict:
     prog = program(root, WILL_SOURCES)
     nl, na = ds.al.shape
@@ -377,7 +406,10 @@ def run_will(root, label, ds, eps) -> dict:
 
 def main(argv):
     root = pathlib.Path(argv[1] if len(argv) > 1 else "/root/reference")
-    res = {"grids": {}, "will": {}, "numbering": {}, "set_dx": {}, "reader": {}, "writer": {}}
+    res = {"grids": {}, "will": {}, "numbering": {}, "set_dx": {}, "reader": {}, "writer": {}, "edges": {}}
+    grids = rc.grid_cases()
+    for label in ("beach_10x6x8", "flume2dv_16x1x8"):
+        res["edges"][label] = run_pcgpme_edges(root, grids[label][0])
     for label, (case, sparse, t0, p, nor) in rc.reader_cases().items():
         files = case_files(case, sparse, t0, p, nor)
         res["reader"][label] = dict(run_reader(root, files, sparse), input=files_digest(files))

@@ -202,3 +202,19 @@ def test_ingest_writer_reproduces_generator_files(label):
             assert want["solver_reads_generator_files"] is False
             continue
         assert d(np.frombuffer(data, dtype=np.uint8)) == want["files"][name], name
+
+
+@pytest.mark.parametrize("label", sorted(RUNS["edges"]))
+def test_oracle_pcgpme_edges_reproduce_reference(ora, grids, label):
+    """PCGPME at its argument edges -- the iteration cap (IER 3000, ITER =
+    cap + 1), ITER = 0 (the default cap), EPS(1) = 0 (SMALL) and the tightest
+    tolerance above TINY (down to the rounding floor) -- against the reference's
+    own PCGPME on the same system: bit for bit."""
+    import make_ref_golden as mk
+    case = grids[label][0]
+    cls = ora.set_nflag(case)
+    sy = ora.rows_rhs_assemble(case, cls, ora.init_matrix(case, cls))
+    for name, (eps, itmax) in mk.PCGPME_EDGES.items():
+        r = ora.pcgpme(sy.alu, sy.llu, sy.de[1:], sy.b[1:], sy.mnoe, eps=eps, itmax=itmax, nthreads=1)
+        _check(f"PCGPME {name}", {"iter": r.iters, "ier": r.ier, "eps": r.eps, "x": d(r.x[:sy.mnoe])},
+               RUNS["edges"][label][name])
