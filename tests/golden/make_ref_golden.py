@@ -406,7 +406,8 @@ def run_will(root, label, ds, eps) -> dict:
 
 def main(argv):
     root = pathlib.Path(argv[1] if len(argv) > 1 else "/root/reference")
-    res = {"grids": {}, "will": {}, "numbering": {}, "set_dx": {}, "reader": {}, "writer": {}, "edges": {}}
+    res = {"grids": {}, "will": {}, "will_cap3": {}, "numbering": {}, "set_dx": {}, "reader": {}, "writer": {},
+           "edges": {}}
     grids = rc.grid_cases()
     for label in ("beach_10x6x8", "flume2dv_16x1x8"):
         res["edges"][label] = run_pcgpme_edges(root, grids[label][0])
@@ -428,6 +429,15 @@ def main(argv):
         print(f"{label}: {time.time() - t:.1f} s", flush=True)
     for label, (ds, eps) in rc.will_cases().items():
         res["will"][label] = run_will(root, label, ds, eps)
+    for label, (ds, eps) in list(rc.will_cases().items())[:2]:
+        # the iteration cap: B after three iterations and the post-processing (pcgpme_2DH.f90:247-280)
+        prog = program(root, WILL_SOURCES)
+        nl, na = ds.al.shape
+        al = farray("real", [ds.al[k, i] for k in range(nl) for i in range(na)], [(1, na), (1, nl)])
+        ll = farray("int", [ds.ll[k, i] for k in range(nl) for i in range(na)], [(1, na), (1, nl)])
+        dd, bb = farray("real", ds.d[:ds.n], [(1, ds.n)]), farray("real", ds.b[:ds.n], [(1, ds.n)])
+        prog.call("pcgpme_will", al, nl, na, ll, dd, ds.n, 64, bb, 1e-14, 5.0, 3)
+        res["will_cap3"][label] = {"input": rc.will_digest(ds), "b": rc.digest(vals(bb))}
         print(f"{label}: done", flush=True)
     (HERE / "reference_runs.json").write_text(json.dumps(res, indent=1, sort_keys=True) + "\n")
     np.savez_compressed(HERE / "reference_solutions.npz", **SOLUTIONS)

@@ -218,3 +218,14 @@ def test_oracle_pcgpme_edges_reproduce_reference(ora, grids, label):
         r = ora.pcgpme(sy.alu, sy.llu, sy.de[1:], sy.b[1:], sy.mnoe, eps=eps, itmax=itmax, nthreads=1)
         _check(f"PCGPME {name}", {"iter": r.iters, "ier": r.ier, "eps": r.eps, "x": d(r.x[:sy.mnoe])},
                RUNS["edges"][label][name])
+
+
+@pytest.mark.parametrize("label", sorted(RUNS["will_cap3"]))
+def test_oracle_will_at_its_iteration_cap_reproduces_reference(ora, label):
+    """PCGPME_WILL stopped by its cap after three iterations (and post-processed
+    as the reference does): the oracle's B equals the reference's bit for bit."""
+    want = RUNS["will_cap3"][label]
+    ds, _ = rc.will_cases()[label]
+    assert rc.will_digest(ds) == want["input"]
+    b, it, reason = ora.pcgpme_will(ds.al, ds.ll, ds.d, ds.b, ds.n, eps=1e-14, itmax=3)
+    assert d(b) == want["b"] and reason == 4
