@@ -193,7 +193,8 @@ def run_grid(root, label, case, solve: bool, loop: bool) -> dict:
         prog.call("ik_loop")
         pl, unl = vals(A.f_p), vals(A.f_un).reshape(-1, 3)
         out["loop"] = {"ik": V.f_ik, "dmax": V.f_dmax, "p": d(pl), "un": d(unl)}
-        SOLUTIONS[f"{label}/p"], SOLUTIONS[f"{label}/un"] = pl, unl
+        if pl.size <= 5000:                       # values kept for the GPU comparison of small loops
+            SOLUTIONS[f"{out['label']}/p"], SOLUTIONS[f"{out['label']}/un"] = pl, unl
     return out
 
 

@@ -87,6 +87,7 @@ def grid_cases():
         out[label] = (small[label], True, False)
     for label in ("beach_48x40x24", "bore_40x24x32", "shore_64x16x24"):
         out[label] = (small[label], "cpu", False)
+    # (the flume's ik loop diverges -- dmax grows pass after pass -- so it runs no loop)
     out["flume_40x24x20_ingested"] = (small["flume_40x24x20_ingested"], False, False)
     base = wl.make_case(20, 12, 16, dz=0.05, slope=0.25, n_obstacles=2, seed=41, amplitude=0.08,
                         step_layers=2)
