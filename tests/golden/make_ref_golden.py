@@ -362,6 +362,25 @@ def run_writer(root, case, sparse, t0, p, nor) -> dict:
     return out
 
 
+def run_one_pass(root, case) -> dict:
+    """One pass of the ik loop body (1sub-momentum.F90:43-59): numbering and
+    right-hand side, assembly, the solve, p -= xe and estimate_velocity2 --
+    on a case whose boundary cells take estimate_velocity2's pressure-boundary
+    branches (nf = -1, nfb = 4: 1sub-momentum.F90:611-621, 638-643)."""
+    d = rc.digest
+    prog = program(root, GRID_SOURCES)
+    prog.fragment("cal_momentum", 52, 57, "p_update")
+    V, A = load_grid(prog, case)
+    V.f_eps0 = rc.LOOP_EPS0
+    for routine in ("set_nflag", "init_matrix"):
+        prog.call(routine)
+    allocate_matrix(prog, V, A)
+    for routine in ("cal_err_of_continuity", "cal_matrix_element", "cal_poisson_equation", "p_update",
+                    "estimate_velocity2"):
+        prog.call(routine)
+    return {"iter": V.f_iter, "dmax": V.f_dmax, "p": d(vals(A.f_p)), "un": d(vals(A.f_un).reshape(-1, 3))}
+
+
 PCGPME_EDGES = {"cap5": (1e-14, 5), "default_cap": (1e-10, 0), "eps0_small": (0.0, 10000),
                 "tight_tolerance": (2e-15, 10000)}
 
@@ -408,10 +427,11 @@ def run_will(root, label, ds, eps) -> dict:
 def main(argv):
     root = pathlib.Path(argv[1] if len(argv) > 1 else "/root/reference")
     res = {"grids": {}, "will": {}, "will_cap3": {}, "numbering": {}, "set_dx": {}, "reader": {}, "writer": {},
-           "edges": {}}
+           "edges": {}, "one_pass": {}}
     grids = rc.grid_cases()
     for label in ("beach_10x6x8", "flume2dv_16x1x8"):
         res["edges"][label] = run_pcgpme_edges(root, grids[label][0])
+    res["one_pass"]["flume_40x24x20_ingested"] = run_one_pass(root, grids["flume_40x24x20_ingested"][0])
     for label, (case, sparse, t0, p, nor) in rc.reader_cases().items():
         files = case_files(case, sparse, t0, p, nor)
         res["reader"][label] = dict(run_reader(root, files, sparse), input=files_digest(files))

@@ -229,3 +229,19 @@ def test_oracle_will_at_its_iteration_cap_reproduces_reference(ora, label):
     assert rc.will_digest(ds) == want["input"]
     b, it, reason = ora.pcgpme_will(ds.al, ds.ll, ds.d, ds.b, ds.n, eps=1e-14, itmax=3)
     assert d(b) == want["b"] and reason == 4
+
+
+@pytest.mark.parametrize("label", sorted(RUNS["one_pass"]))
+def test_oracle_one_ik_pass_reproduces_reference(ora, grids, label):
+    """One pass of the ik loop body on the flume with wave-boundary cells
+    (estimate_velocity2's pressure-boundary branches): the oracle's pressure and
+    face velocities equal the reference's bit for bit."""
+    want = RUNS["one_pass"][label]
+    case = grids[label][0]
+    cls = ora.set_nflag(case)
+    c = case.copy()
+    c.f = cls.f.copy()
+    sy = ora.rows_rhs_assemble(c, cls, ora.init_matrix(case, cls))
+    r = ora.pcgpme(sy.alu, sy.llu, sy.de[1:], sy.b[1:], sy.mnoe, eps=rc.LOOP_EPS0)
+    p, un = ora.correct(c, cls, sy, r.x, np.zeros(case.inne2 + 2), case.un.copy())
+    _check("one ik pass", {"iter": r.iters, "dmax": sy.dmax, "p": d(p), "un": d(un)}, want)
